@@ -1,0 +1,191 @@
+/*
+ * gbfoam.h -- C ABI of libgbfoam.so, the GB300 (sm_103a) kernels behind
+ * pyopenfoam_gb300's LduMatrix / FvMatrix / PCG / PBiCGStab / DIC / DILU /
+ * fvm.laplacian / DifferentiableLinearSolve.
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 = OK, non-zero = error code;
+ *     gbf_last_error() returns a message for the calling thread's last error.
+ *   - Pointers are DEVICE pointers unless the parameter name ends in _h
+ *     (host pointer).  Sizes are element counts.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *   - Nothing allocates device memory: callers pass workspaces sized by the
+ *     *_workspace_bytes queries.
+ *   - Cell/face indices are int32; a matrix holds < 2^31 slots.
+ *
+ * Each entry point names the reference routine it replaces, cited as
+ * file:line inside alanZee/pyOpenFOAM (src/pyfoam/...).  The reference is
+ * pure Python on PyTorch; its binding of these entry points is the ctypes
+ * layer in pyopenfoam_gb300/_lib.py.
+ */
+#ifndef GBFOAM_H
+#define GBFOAM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBF_OK 0
+#define GBF_ERR_ARG 1      /* bad size / pointer / index                        */
+#define GBF_ERR_CUDA 2     /* a CUDA runtime call failed                        */
+#define GBF_ERR_WORKSPACE 3/* workspace too small                              */
+#define GBF_ERR_RANGE 4    /* owner/neighbour index out of range                */
+
+/* Solver status codes written to gbf_solve_result.status */
+#define GBF_RUNNING 0
+#define GBF_CONVERGED 1
+#define GBF_BREAKDOWN 2
+#define GBF_MAX_ITER 3
+
+/* Cell-sliced LDU addressing (built once per mesh topology).
+ *
+ * Cells are grouped in slices of 32 consecutive cells (one warp).  Inside a
+ * slice, slot k of lane l lives at slice_off[s] + 32*k + l, so every slot
+ * read by a warp is one coalesced 128/256-byte line.  The first `wo` slots of
+ * a slice are the cell's OWNER-side faces (faces with owner == cell, in
+ * ascending face order), the next `wn` slots its NEIGHBOUR-side faces
+ * (neighbour == cell, ascending face order); unused slots have col = -1.
+ * This keeps the per-cell summation order of the reference's face-ordered
+ * scatter_add, so the gather is bitwise identical to LduMatrix.Ax.
+ */
+typedef struct gbf_layout {
+  int32_t n_cells;
+  int32_t n_faces;         /* internal faces                                   */
+  int32_t n_slices;        /* ceil(n_cells / 32)                               */
+  int32_t max_width;       /* max over slices of wo + wn                       */
+  int64_t n_slots;         /* total slots incl. padding                        */
+  const int32_t* slice_off;/* [n_slices + 1]                                   */
+  const int32_t* slice_w;  /* [n_slices]  wo | (wn << 16)                      */
+  const int32_t* slot_col; /* [n_slots]   column cell, -1 = padding            */
+  const int32_t* slot_face;/* [n_slots]   face of the slot, -1 = padding       */
+  const int32_t* owner;    /* [n_faces]   face-order owner (int32)             */
+  const int32_t* neighbour;/* [n_faces]   face-order neighbour (int32)         */
+} gbf_layout;
+
+/* ---- library ----------------------------------------------------------- */
+const char* gbf_last_error(void);
+int gbf_version(void);
+/* Number of SMs of the current device (grid sizing of the reductions).     */
+int gbf_device_sm_count(int32_t* n_sm);
+
+/* ---- topology (host, once per mesh) -------------------------------------
+ * Replace the reference's per-call Python loops over faces
+ * (solvers/preconditioners.py:116-122, :254-268) and CSR caching
+ * (core/ldu_matrix.py:101-102, :336-343) with one O(n + F) host pass. */
+int gbf_layout_plan(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                    const int32_t* neighbour_h, int32_t* n_slices, int64_t* n_slots,
+                    int32_t* max_width);
+int gbf_layout_fill(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                    const int32_t* neighbour_h, int32_t* slice_off_h, int32_t* slice_w_h,
+                    int32_t* slot_col_h, int32_t* slot_face_h);
+/* DIC wavefront: level(c) = 1 + max level of the cells j < c that c reads in
+ * the reference's cell-ordered factorisation (preconditioners.py:124-128).
+ * level_ptr_h has room for n_cells + 1 entries, level_cells_h for n_cells. */
+int gbf_dic_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                     const int32_t* neighbour_h, int32_t* level_ptr_h,
+                     int32_t* level_cells_h, int32_t* n_levels, int32_t* max_level_size);
+/* DILU wavefront over faces: level(f) = 1 + max level of the previous faces
+ * touching owner[f] or neighbour[f] (preconditioners.py:254-268).
+ * level_ptr_h has room for n_faces + 1 entries, level_faces_h for n_faces. */
+int gbf_dilu_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                      const int32_t* neighbour_h, int32_t* level_ptr_h,
+                      int32_t* level_faces_h, int32_t* n_levels, int32_t* max_level_size);
+
+/* ---- coefficient packing ------------------------------------------------
+ * slot_coef[slot] = own_src[face] on owner-side slots, nei_src[face] on
+ * neighbour-side slots, 0 on padding.  Ax packs (lower, upper); the
+ * transposed product and the transposed matrix pack (upper, lower). */
+int gbf_pack_f64(const gbf_layout* L, const double* own_src, const double* nei_src,
+                 double* slot_coef, void* stream);
+int gbf_pack_f32(const gbf_layout* L, const float* own_src, const float* nei_src,
+                 float* slot_coef, void* stream);
+/* Same, converting FP64 sources to an FP32 packed copy (mixed solver). */
+int gbf_pack_f64_to_f32(const gbf_layout* L, const double* own_src, const double* nei_src,
+                        float* slot_coef, void* stream);
+
+/* ---- Amul ----------------------------------------------------------------
+ * LduMatrix.Ax, core/ldu_matrix.py:172-217 (nei_first = 0, coefficients
+ * packed (lower, upper)) and LduMatrix.Ax_T, core/ldu_matrix.py:219-258
+ * (nei_first = 1, packed (upper, lower)):
+ *   y = (diag*x + S_first) + S_second, each S a sum from 0.0 in ascending
+ *   face order, every product and sum rounded once (no FMA): bitwise equal to
+ *   the reference.                                                         */
+int gbf_amul_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                 const double* x, double* y, int32_t nei_first, void* stream);
+/* float32 matrix, reference semantics: float32 products, float64 sums,
+ * float64 y (core/backend.py:58-63 allocates the scatter output in the
+ * float64 default dtype).                                                  */
+int gbf_amul_f32_f64out(const gbf_layout* L, const float* slot_coef, const float* diag,
+                        const float* x, double* y, int32_t nei_first, void* stream);
+/* all-float Amul (float products and sums); no reference counterpart: the
+ * inner operator of the mixed-precision solver.                            */
+int gbf_amul_f32(const gbf_layout* L, const float* slot_coef, const float* diag,
+                 const float* x, float* y, int32_t nei_first, void* stream);
+
+/* ---- preconditioners -----------------------------------------------------
+ * DICPreconditioner._build, solvers/preconditioners.py:88-133: level-
+ * scheduled, one launch per wavefront level, each cell's subtractions in the
+ * reference's face order; then d = clamp(|d|, 1e-30).  slot_coef must be the
+ * (lower, upper) packing (the neighbour-side slots carry upper[f]).
+ * level_ptr / level_cells are DEVICE copies of gbf_dic_schedule's output.  */
+int gbf_dic_build_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                      const int32_t* level_ptr, const int32_t* level_cells, int32_t n_levels,
+                      int32_t max_level_size, double* d_out, void* stream);
+/* DILUPreconditioner._build, solvers/preconditioners.py:228-272, per face
+ * level; lower/upper in face order.                                        */
+int gbf_dilu_build_f64(const gbf_layout* L, const double* lower, const double* upper,
+                       const double* diag, const int32_t* level_ptr,
+                       const int32_t* level_faces, int32_t n_levels, int32_t max_level_size,
+                       double* d_out, void* stream);
+/* DIC/DILU apply(): z = r / d (preconditioners.py:151, :288).               */
+int gbf_diag_apply_f64(int32_t n, const double* r, const double* d, double* z, void* stream);
+
+/* ---- Krylov solvers --------------------------------------------------------
+ * Convergence follows ResidualMonitor (solvers/residual.py:112-145): L2 norm
+ * each check, |r| < tolerance or |r|/|r0| < rel_tol once iteration >=
+ * min_iter; iterations = number of residual checks (len(history)).        */
+typedef struct gbf_solve_params {
+  double tolerance;
+  double rel_tol;
+  int32_t max_iter;
+  int32_t min_iter;
+  int32_t check_every;  /* iterations between host status reads (0 = 32)   */
+  int32_t variant;      /* PBiCGStab: 0 = reference omega = (t.z)/(t.t)
+                           (pbicgstab.py:210), 1 = standard (t.s)/(t.t);
+                           ignored by PCG                                 */
+} gbf_solve_params;
+
+typedef struct gbf_solve_result {
+  int32_t iterations;      /* len(history)                                  */
+  int32_t status;          /* GBF_CONVERGED / GBF_BREAKDOWN / GBF_MAX_ITER  */
+  double final_residual;
+  double initial_residual;
+  int32_t inner_iterations;/* mixed solver: low-precision iterations        */
+  int32_t outer_updates;   /* mixed solver: FP64 residual replacements      */
+} gbf_solve_result;
+
+size_t gbf_pcg_workspace_bytes(int32_t n_cells);
+/* PCGSolver._solve, solvers/pcg.py:97-187.  x holds x0 on entry and the
+ * solution on return.  precond_d = factorised DIC/DILU diagonal (z = r/d) or
+ * NULL for "none".  history (device, max_iter + 1 doubles) receives |r| per
+ * check.                                                                   */
+int gbf_pcg_solve_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                      const double* precond_d, const double* b, double* x, double* history,
+                      const gbf_solve_params* P, gbf_solve_result* R, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+size_t gbf_pbicgstab_workspace_bytes(int32_t n_cells);
+/* PBiCGSTABSolver._solve, solvers/pbicgstab.py:103-239 (two residual checks
+ * per iteration: on s and on r).  history holds 2*max_iter + 1 doubles.     */
+int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                            const double* precond_d, const double* b, double* x,
+                            double* history, const gbf_solve_params* P, gbf_solve_result* R,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFOAM_H */

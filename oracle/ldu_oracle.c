@@ -1,0 +1,499 @@
+/*
+ * ldu_oracle.c -- CPU restatement of pyOpenFOAM's linear-solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the parity tests,
+ * the smoke check and the benchmark's CPU-baseline leg compare the CUDA path
+ * against.  Nothing in the product package links or calls it.
+ *
+ * Every routine restates one reference routine, cited by file:line of the
+ * reference project (alanZee/pyOpenFOAM, src/pyfoam/...).  Arithmetic is IEEE
+ * double (or float) with one rounding per source-level operation, exactly as
+ * the reference's element-wise torch ops round: the file must be compiled
+ * with -ffp-contract=off so that no multiply-add is fused.
+ *
+ * Two execution modes:
+ *   - serial   : the reference's own face-ordered scatter / sequential loops;
+ *                used for parity (bitwise where the reference is
+ *                deterministic);
+ *   - threaded : OpenMP over cells with per-cell gathers in ascending face
+ *                order (bitwise identical Amul) and OpenMP reductions for
+ *                dot products (order differs, as torch's threaded dot does);
+ *                used only to time the CPU baseline.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef int64_t idx_t;
+
+/* ------------------------------------------------------------------------ */
+/* Amul: core/ldu_matrix.py:172-217 (Ax) and :219-258 (Ax_T)                 */
+/* y = diag*x;  y = y + scatter_add(lower*x[nei], owner);                    */
+/*              y = y + scatter_add(upper*x[own], neighbour)                 */
+/* scatter_add (core/backend.py:34-64) starts from zeros and adds in face    */
+/* order.                                                                    */
+/* ------------------------------------------------------------------------ */
+#define DEFINE_AMUL_SERIAL(T, A, SUF)                                           \
+  void orc_amul_##SUF(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,   \
+                      const T* diag, const T* lower, const T* upper,           \
+                      const T* x, A* y, int transpose, A* work) {              \
+    A* s1 = work;                                                              \
+    A* s2 = work + n;                                                          \
+    for (idx_t c = 0; c < n; ++c) { T t = diag[c] * x[c]; y[c] = (A)t; }      \
+    if (nf <= 0) return;                                                       \
+    for (idx_t c = 0; c < n; ++c) { s1[c] = (A)0; s2[c] = (A)0; }             \
+    if (!transpose) {                                                          \
+      for (idx_t f = 0; f < nf; ++f) { T t = lower[f] * x[nei[f]]; s1[own[f]] = s1[own[f]] + (A)t; } \
+      for (idx_t f = 0; f < nf; ++f) { T t = upper[f] * x[own[f]]; s2[nei[f]] = s2[nei[f]] + (A)t; } \
+    } else {                                                                   \
+      for (idx_t f = 0; f < nf; ++f) { T t = lower[f] * x[own[f]]; s1[nei[f]] = s1[nei[f]] + (A)t; } \
+      for (idx_t f = 0; f < nf; ++f) { T t = upper[f] * x[nei[f]]; s2[own[f]] = s2[own[f]] + (A)t; } \
+    }                                                                          \
+    for (idx_t c = 0; c < n; ++c) y[c] = y[c] + s1[c];                         \
+    for (idx_t c = 0; c < n; ++c) y[c] = y[c] + s2[c];                         \
+  }
+/* FP64 matrices: everything in double. */
+DEFINE_AMUL_SERIAL(double, double, f64)
+/* FP32 matrices: the reference's scatter_add allocates its output in the   */
+/* global default dtype (float64, core/backend.py:58-63), so the float32     */
+/* products are accumulated in double and y comes back as float64.          */
+DEFINE_AMUL_SERIAL(float, double, f32)
+/* Pure-float variant (float products and float sums); no reference         */
+/* counterpart -- it specifies the inner FP32 Amul of the mixed solver.     */
+DEFINE_AMUL_SERIAL(float, float, f32acc)
+
+/* Stable per-cell face lists (ascending face order): own_ptr/own_face list  */
+/* the faces owned by each cell, nei_ptr/nei_face the faces whose neighbour  */
+/* is the cell.  Counting sort, so stable.                                   */
+void orc_build_csr(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                   idx_t* own_ptr, idx_t* own_face, idx_t* nei_ptr, idx_t* nei_face) {
+  memset(own_ptr, 0, sizeof(idx_t) * (size_t)(n + 1));
+  memset(nei_ptr, 0, sizeof(idx_t) * (size_t)(n + 1));
+  for (idx_t f = 0; f < nf; ++f) { own_ptr[own[f] + 1]++; nei_ptr[nei[f] + 1]++; }
+  for (idx_t c = 0; c < n; ++c) { own_ptr[c + 1] += own_ptr[c]; nei_ptr[c + 1] += nei_ptr[c]; }
+  idx_t* co = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n > 0 ? n : 1));
+  idx_t* cn = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n > 0 ? n : 1));
+  for (idx_t c = 0; c < n; ++c) { co[c] = own_ptr[c]; cn[c] = nei_ptr[c]; }
+  for (idx_t f = 0; f < nf; ++f) { own_face[co[own[f]]++] = f; nei_face[cn[nei[f]]++] = f; }
+  free(co);
+  free(cn);
+}
+
+/* Threaded per-cell gather: same per-cell summation order as the scatter.   */
+#define DEFINE_AMUL_CSR(T, SUF)                                                \
+  void orc_amul_csr_##SUF(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei, \
+                          const idx_t* own_ptr, const idx_t* own_face,         \
+                          const idx_t* nei_ptr, const idx_t* nei_face,         \
+                          const T* diag, const T* lower, const T* upper,       \
+                          const T* x, T* y) {                                  \
+    _Pragma("omp parallel for schedule(static)")                               \
+    for (idx_t c = 0; c < n; ++c) {                                            \
+      T yc = diag[c] * x[c];                                                   \
+      if (nf > 0) {                                                            \
+        T s1 = (T)0, s2 = (T)0;                                                \
+        for (idx_t k = own_ptr[c]; k < own_ptr[c + 1]; ++k) {                  \
+          idx_t f = own_face[k]; T t = lower[f] * x[nei[f]]; s1 = s1 + t; }    \
+        for (idx_t k = nei_ptr[c]; k < nei_ptr[c + 1]; ++k) {                  \
+          idx_t f = nei_face[k]; T t = upper[f] * x[own[f]]; s2 = s2 + t; }    \
+        yc = yc + s1;                                                          \
+        yc = yc + s2;                                                          \
+      }                                                                        \
+      y[c] = yc;                                                               \
+    }                                                                          \
+  }
+DEFINE_AMUL_CSR(double, f64)
+DEFINE_AMUL_CSR(float, f32)
+
+/* ------------------------------------------------------------------------ */
+/* DIC factorisation: solvers/preconditioners.py:88-133                      */
+/* for cells ascending: for faces f with neighbour==i in face order:         */
+/*   j = owner[f], a = upper[f], d_j = current d[j];                         */
+/*   if |d_j| > 1e-30: d[i] = d[i] - (a*a)/d_j                               */
+/* then d = clamp(|d|, min=1e-30)                                            */
+/* ------------------------------------------------------------------------ */
+static double clamp_abs(double v) {
+  double a = fabs(v);
+  return (a < 1e-30) ? 1e-30 : a; /* NaN propagates, as torch.clamp does */
+}
+
+void orc_dic_build_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                       const double* diag, const double* upper, double* d,
+                       idx_t* nei_ptr, idx_t* nei_face /* work: n+1, nf */) {
+  memcpy(d, diag, sizeof(double) * (size_t)n);
+  if (nf > 0) {
+    /* lower_adj lists in face order (:116-122) */
+    memset(nei_ptr, 0, sizeof(idx_t) * (size_t)(n + 1));
+    for (idx_t f = 0; f < nf; ++f) nei_ptr[nei[f] + 1]++;
+    for (idx_t c = 0; c < n; ++c) nei_ptr[c + 1] += nei_ptr[c];
+    idx_t* cur = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n > 0 ? n : 1));
+    for (idx_t c = 0; c < n; ++c) cur[c] = nei_ptr[c];
+    for (idx_t f = 0; f < nf; ++f) nei_face[cur[nei[f]]++] = f;
+    free(cur);
+    for (idx_t i = 0; i < n; ++i) {
+      for (idx_t k = nei_ptr[i]; k < nei_ptr[i + 1]; ++k) {
+        idx_t f = nei_face[k];
+        double a = upper[f];
+        double dj = d[own[f]];
+        if (fabs(dj) > 1e-30) {
+          double t = (a * a) / dj;
+          d[i] = d[i] - t;
+        }
+      }
+    }
+  }
+  for (idx_t c = 0; c < n; ++c) d[c] = clamp_abs(d[c]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* DILU factorisation: solvers/preconditioners.py:228-272                    */
+/* for faces ascending: d_p, d_n captured first; d[p] -= l*u/d_n;            */
+/* d[n] -= u*l/d_p (each guarded by |.| > 1e-30); then clamp(|d|)            */
+/* ------------------------------------------------------------------------ */
+void orc_dilu_build_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                        const double* diag, const double* lower, const double* upper,
+                        double* d) {
+  memcpy(d, diag, sizeof(double) * (size_t)n);
+  for (idx_t f = 0; f < nf; ++f) {
+    idx_t p = own[f], q = nei[f];
+    double l = lower[f], u = upper[f];
+    double dp = d[p], dn = d[q];
+    if (fabs(dn) > 1e-30) { double t = (l * u) / dn; d[p] = d[p] - t; }
+    if (fabs(dp) > 1e-30) { double t = (u * l) / dp; d[q] = d[q] - t; }
+  }
+  for (idx_t c = 0; c < n; ++c) d[c] = clamp_abs(d[c]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Full sweeps: DIC apply_full preconditioners.py:153-201, DILU :290-337     */
+/* ------------------------------------------------------------------------ */
+void orc_dic_apply_full_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                            const double* upper, const double* pd, const double* r,
+                            double* z) {
+  memcpy(z, r, sizeof(double) * (size_t)n);
+  for (idx_t f = 0; f < nf; ++f) {
+    idx_t p = own[f], q = nei[f];
+    if (p < q) {
+      double dp = pd[p];
+      if (fabs(dp) > 1e-30) { double t = upper[f] * z[p]; t = t / dp; z[q] = z[q] - t; }
+    }
+  }
+  for (idx_t c = 0; c < n; ++c) z[c] = z[c] / pd[c];
+  for (idx_t f = nf - 1; f >= 0; --f) {
+    idx_t p = own[f], q = nei[f];
+    if (p < q) {
+      double dq = pd[q];
+      if (fabs(dq) > 1e-30) { double t = upper[f] * z[q]; t = t / dq; z[p] = z[p] - t; }
+    }
+  }
+}
+
+void orc_dilu_apply_full_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                             const double* lower, const double* upper, const double* pd,
+                             const double* r, double* z) {
+  memcpy(z, r, sizeof(double) * (size_t)n);
+  for (idx_t f = 0; f < nf; ++f) {
+    idx_t p = own[f], q = nei[f];
+    double dp = pd[p];
+    if (fabs(dp) > 1e-30) { double t = upper[f] * z[p]; t = t / dp; z[q] = z[q] - t; }
+  }
+  for (idx_t c = 0; c < n; ++c) z[c] = z[c] / pd[c];
+  for (idx_t f = nf - 1; f >= 0; --f) {
+    idx_t p = own[f], q = nei[f];
+    double dq = pd[q];
+    if (fabs(dq) > 1e-30) { double t = lower[f] * z[q]; t = t / dq; z[p] = z[p] - t; }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Vector helpers (serial or OpenMP)                                        */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  idx_t n, nf;
+  const idx_t *own, *nei;
+  const double *diag, *lower, *upper;
+  int threads;                 /* 1 = serial reference order */
+  idx_t *own_ptr, *own_face, *nei_ptr, *nei_face; /* threaded Amul lists */
+  double* work;                /* 2n for the serial scatter */
+} orc_mat;
+
+static void mat_ax(const orc_mat* A, const double* x, double* y) {
+  if (A->threads <= 1)
+    orc_amul_f64(A->n, A->nf, A->own, A->nei, A->diag, A->lower, A->upper, x, y, 0, A->work);
+  else
+    orc_amul_csr_f64(A->n, A->nf, A->own, A->nei, A->own_ptr, A->own_face, A->nei_ptr,
+                     A->nei_face, A->diag, A->lower, A->upper, x, y);
+}
+
+static double vdot(const orc_mat* A, const double* a, const double* b) {
+  double s = 0.0;
+  idx_t n = A->n;
+  if (A->threads <= 1) {
+    for (idx_t i = 0; i < n; ++i) s = s + a[i] * b[i];
+  } else {
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (idx_t i = 0; i < n; ++i) s = s + a[i] * b[i];
+  }
+  return s;
+}
+
+/* residual.py:112-145 -- ResidualMonitor.update */
+typedef struct {
+  double tol, rel_tol, res0;
+  int min_iter, have0;
+  double* hist;
+  int n_hist;
+} orc_mon;
+
+static int mon_update(orc_mon* m, double res, int iteration) {
+  m->hist[m->n_hist++] = res;
+  if (!m->have0) { m->res0 = res; m->have0 = 1; }
+  if (iteration >= m->min_iter) {
+    if (res < m->tol) return 1;
+    if (m->res0 > 0.0 && res / m->res0 < m->rel_tol) return 1;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PCG: solvers/pcg.py:97-187 (z = r / d_factored when pd != NULL,          */
+/* z = r otherwise).  Returns 1 converged, 0 not converged (max iterations  */
+/* or breakdown); *n_hist = reported iteration count = len(history).        */
+/* ------------------------------------------------------------------------ */
+int orc_pcg_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                const double* diag, const double* lower, const double* upper,
+                const double* pd, const double* b, double* x, double tol, double rel_tol,
+                int max_iter, int min_iter, int threads, double* hist, int* n_hist) {
+#ifdef _OPENMP
+  if (threads > 1) omp_set_num_threads(threads);
+#endif
+  orc_mat A = {n, nf, own, nei, diag, lower, upper, threads, 0, 0, 0, 0, 0};
+  double* buf = (double*)malloc(sizeof(double) * (size_t)n * 6 + 16);
+  double *r = buf, *z = buf + n, *p = buf + 2 * n, *Ap = buf + 3 * n, *w = buf + 4 * n;
+  A.work = w;
+  if (threads > 1) {
+    A.own_ptr = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n + 1));
+    A.nei_ptr = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n + 1));
+    A.own_face = (idx_t*)malloc(sizeof(idx_t) * (size_t)(nf + 1));
+    A.nei_face = (idx_t*)malloc(sizeof(idx_t) * (size_t)(nf + 1));
+    orc_build_csr(n, nf, own, nei, A.own_ptr, A.own_face, A.nei_ptr, A.nei_face);
+  }
+  orc_mon M = {tol, rel_tol, 0.0, min_iter, 0, hist, 0};
+  int conv = 0;
+  mat_ax(&A, x, Ap);
+#pragma omp parallel for if (threads > 1) schedule(static)
+  for (idx_t i = 0; i < n; ++i) r[i] = b[i] - Ap[i];
+  if (mon_update(&M, sqrt(vdot(&A, r, r)), 0)) { conv = 1; goto done; }
+#pragma omp parallel for if (threads > 1) schedule(static)
+  for (idx_t i = 0; i < n; ++i) { z[i] = pd ? r[i] / pd[i] : r[i]; p[i] = z[i]; }
+  double rz = vdot(&A, r, z);
+  for (int it = 1; it <= max_iter; ++it) {
+    mat_ax(&A, p, Ap);
+    double pAp = vdot(&A, p, Ap);
+    if (fabs(pAp) < 1e-30) { conv = 0; goto done; }
+    double alpha = rz / pAp;
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) {
+      double t = alpha * p[i]; x[i] = x[i] + t;
+      double u = alpha * Ap[i]; r[i] = r[i] - u;
+    }
+    if (mon_update(&M, sqrt(vdot(&A, r, r)), it)) { conv = 1; goto done; }
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) z[i] = pd ? r[i] / pd[i] : r[i];
+    double rzn = vdot(&A, r, z);
+    double beta = rzn / rz;
+    rz = rzn;
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) { double t = beta * p[i]; p[i] = z[i] + t; }
+  }
+done:
+  *n_hist = M.n_hist;
+  if (threads > 1) { free(A.own_ptr); free(A.nei_ptr); free(A.own_face); free(A.nei_face); }
+  free(buf);
+  return conv;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PBiCGStab: solvers/pbicgstab.py:103-239                                   */
+/* ------------------------------------------------------------------------ */
+int orc_pbicgstab_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                      const double* diag, const double* lower, const double* upper,
+                      const double* pd, const double* b, double* x, double tol,
+                      double rel_tol, int max_iter, int min_iter, int threads,
+                      double* hist, int* n_hist, int standard_omega) {
+#ifdef _OPENMP
+  if (threads > 1) omp_set_num_threads(threads);
+#endif
+  orc_mat A = {n, nf, own, nei, diag, lower, upper, threads, 0, 0, 0, 0, 0};
+  double* buf = (double*)malloc(sizeof(double) * (size_t)n * 10 + 16);
+  double *r = buf, *rt = buf + n, *p = buf + 2 * n, *v = buf + 3 * n, *y = buf + 4 * n;
+  double *s = buf + 5 * n, *z = buf + 6 * n, *t = buf + 7 * n, *w = buf + 8 * n;
+  A.work = w;
+  if (threads > 1) {
+    A.own_ptr = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n + 1));
+    A.nei_ptr = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n + 1));
+    A.own_face = (idx_t*)malloc(sizeof(idx_t) * (size_t)(nf + 1));
+    A.nei_face = (idx_t*)malloc(sizeof(idx_t) * (size_t)(nf + 1));
+    orc_build_csr(n, nf, own, nei, A.own_ptr, A.own_face, A.nei_ptr, A.nei_face);
+  }
+  orc_mon M = {tol, rel_tol, 0.0, min_iter, 0, hist, 0};
+  int conv = 0;
+  mat_ax(&A, x, v);
+#pragma omp parallel for if (threads > 1) schedule(static)
+  for (idx_t i = 0; i < n; ++i) r[i] = b[i] - v[i];
+  if (mon_update(&M, sqrt(vdot(&A, r, r)), 0)) { conv = 1; goto done; }
+  memcpy(rt, r, sizeof(double) * (size_t)n);
+  double rho = vdot(&A, rt, r);
+  memcpy(p, r, sizeof(double) * (size_t)n);
+  memset(v, 0, sizeof(double) * (size_t)n);
+  for (int it = 1; it <= max_iter; ++it) {
+    if (fabs(rho) < 1e-30) { conv = 0; goto done; }
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) y[i] = pd ? p[i] / pd[i] : p[i];
+    mat_ax(&A, y, v);
+    double rtv = vdot(&A, rt, v);
+    if (fabs(rtv) < 1e-30) { conv = 0; goto done; }
+    double alpha = rho / rtv;
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) { double q = alpha * v[i]; s[i] = r[i] - q; }
+    if (mon_update(&M, sqrt(vdot(&A, s, s)), it)) {
+#pragma omp parallel for if (threads > 1) schedule(static)
+      for (idx_t i = 0; i < n; ++i) { double q = alpha * y[i]; x[i] = x[i] + q; }
+      conv = 1;
+      goto done;
+    }
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) z[i] = pd ? s[i] / pd[i] : s[i];
+    mat_ax(&A, z, t);
+    double tt = vdot(&A, t, t);
+    if (fabs(tt) < 1e-30) {
+#pragma omp parallel for if (threads > 1) schedule(static)
+      for (idx_t i = 0; i < n; ++i) { double q = alpha * y[i]; x[i] = x[i] + q; r[i] = s[i]; }
+      if (mon_update(&M, sqrt(vdot(&A, r, r)), it)) { conv = 1; goto done; }
+      double rho_new = vdot(&A, rt, r);
+      double beta = (rho_new / rho) * alpha;
+      rho = rho_new;
+#pragma omp parallel for if (threads > 1) schedule(static)
+      for (idx_t i = 0; i < n; ++i) { double q = p[i] - v[i]; q = beta * q; p[i] = r[i] + q; }
+      continue;
+    }
+    /* pbicgstab.py:210 uses (t.z); standard_omega selects (t.s) */
+    double omega = vdot(&A, t, standard_omega ? s : z) / tt;
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) {
+      double q1 = alpha * y[i];
+      double q2 = omega * z[i];
+      double xi = x[i] + q1;
+      x[i] = xi + q2;
+      double q3 = omega * t[i];
+      r[i] = s[i] - q3;
+    }
+    if (mon_update(&M, sqrt(vdot(&A, r, r)), it)) { conv = 1; goto done; }
+    double rho_new = vdot(&A, rt, r);
+    if (fabs(omega) < 1e-30) { conv = 0; goto done; }
+    double beta = (rho_new / rho) * (alpha / omega);
+    rho = rho_new;
+#pragma omp parallel for if (threads > 1) schedule(static)
+    for (idx_t i = 0; i < n; ++i) {
+      double q = omega * v[i];
+      q = p[i] - q;
+      q = beta * q;
+      p[i] = r[i] + q;
+    }
+  }
+done:
+  *n_hist = M.n_hist;
+  if (threads > 1) { free(A.own_ptr); free(A.nei_ptr); free(A.own_face); free(A.nei_face); }
+  free(buf);
+  return conv;
+}
+
+/* ------------------------------------------------------------------------ */
+/* fvm.laplacian assembly: discretisation/operators.py:432-518               */
+/* |S| = ATen's CPU p=2 norm over a length-3 row, which accumulates with a   */
+/* fused multiply-add: sqrt(fma(z,z, fma(y,y, x*x)))                         */
+/* c_f = (D_f*|S_f|)*delta_f; lower = -c/V_P; upper = -c/V_N;                */
+/* diag = ((0 + sum_own c/V_P) + sum_nei c/V_N) + sum_bnd c_b/V_P            */
+/* ------------------------------------------------------------------------ */
+static double smag3(const double* a) {
+  double x = a[0], y = a[1], z = a[2];
+  return sqrt(fma(z, z, fma(y, y, x * x)));
+}
+
+void orc_laplacian_f64(idx_t n, idx_t nint, idx_t nfaces, const idx_t* own /* nfaces */,
+                       const idx_t* nei /* nint */, const double* areas /* nfaces*3 */,
+                       const double* delta /* nfaces */, const double* D /* nfaces */,
+                       const double* V /* n */, double* lower, double* upper, double* diag,
+                       double* work /* 3n */) {
+  double *s1 = work, *s2 = work + n, *s3 = work + 2 * n;
+  for (idx_t c = 0; c < n; ++c) { s1[c] = 0.0; s2[c] = 0.0; s3[c] = 0.0; }
+  for (idx_t f = 0; f < nint; ++f) {
+    double cf = D[f] * smag3(areas + 3 * f);
+    cf = cf * delta[f];
+    double vp = V[own[f]], vn = V[nei[f]];
+    lower[f] = (-cf) / vp;
+    upper[f] = (-cf) / vn;
+    s1[own[f]] = s1[own[f]] + cf / vp;
+  }
+  for (idx_t f = 0; f < nint; ++f) {
+    double cf = D[f] * smag3(areas + 3 * f);
+    cf = cf * delta[f];
+    s2[nei[f]] = s2[nei[f]] + cf / V[nei[f]];
+  }
+  for (idx_t c = 0; c < n; ++c) diag[c] = 0.0 + s1[c];
+  for (idx_t c = 0; c < n; ++c) diag[c] = diag[c] + s2[c];
+  if (nfaces > nint) {
+    for (idx_t f = nint; f < nfaces; ++f) {
+      double cb = D[f] * smag3(areas + 3 * f);
+      cb = cb * delta[f];
+      s3[own[f]] = s3[own[f]] + cb / V[own[f]];
+    }
+    for (idx_t c = 0; c < n; ++c) diag[c] = diag[c] + s3[c];
+  }
+}
+
+/* fvm.div, "Gauss upwind": discretisation/operators.py:351-429              */
+/* lower = F-/V_P, upper = F+/V_N, diag = (0 + sum_own -F+/V_P)              */
+/*                                        + sum_nei |F-|/V_N                 */
+void orc_div_upwind_f64(idx_t n, idx_t nint, const idx_t* own, const idx_t* nei,
+                        const double* flux, const double* V, double* lower, double* upper,
+                        double* diag, double* work /* 2n */) {
+  double *s1 = work, *s2 = work + n;
+  for (idx_t c = 0; c < n; ++c) { s1[c] = 0.0; s2[c] = 0.0; }
+  for (idx_t f = 0; f < nint; ++f) {
+    double F = flux[f];
+    double fp = (F >= 0.0) ? F : 0.0;
+    double fn = (F >= 0.0) ? 0.0 : F;
+    lower[f] = fn / V[own[f]];
+    upper[f] = fp / V[nei[f]];
+    s1[own[f]] = s1[own[f]] + (-fp) / V[own[f]];
+    s2[nei[f]] = s2[nei[f]] + fabs(fn) / V[nei[f]];
+  }
+  for (idx_t c = 0; c < n; ++c) diag[c] = 0.0 + s1[c];
+  for (idx_t c = 0; c < n; ++c) diag[c] = diag[c] + s2[c];
+}
+
+/* ------------------------------------------------------------------------ */
+/* DifferentiableLinearSolve.backward gradients:                             */
+/* differentiable/linear_solver.py:139-149                                   */
+/* ------------------------------------------------------------------------ */
+void orc_dls_grads_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                       const double* lam, const double* x, double* gdiag, double* glower,
+                       double* gupper) {
+  for (idx_t c = 0; c < n; ++c) gdiag[c] = (-lam[c]) * x[c];
+  for (idx_t f = 0; f < nf; ++f) {
+    glower[f] = (-lam[own[f]]) * x[nei[f]];
+    gupper[f] = (-lam[nei[f]]) * x[own[f]];
+  }
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

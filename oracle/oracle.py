@@ -1,0 +1,211 @@
+"""Python face of the CPU oracle (``ldu_oracle.c``) -- TEST INFRASTRUCTURE ONLY.
+
+The oracle restates pyOpenFOAM's linear-solve path on the CPU so that tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` can check
+the CUDA path against it.  The product package never imports this module.
+
+Routines (reference citations are in ``ldu_oracle.c``):
+
+* ``amul`` / ``amul_T``           -- ``LduMatrix.Ax`` / ``Ax_T``
+* ``dic_build`` / ``dilu_build``  -- DIC / DILU factorised diagonals
+* ``dic_apply_full`` / ``dilu_apply_full`` -- the full triangular sweeps
+* ``pcg`` / ``pbicgstab``         -- the solvers with ``ResidualMonitor`` rules
+* ``laplacian`` / ``div_upwind``  -- ``fvm.laplacian`` / ``fvm.div`` assembly
+* ``dls_grads``                   -- ``DifferentiableLinearSolve.backward``
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "ldu_oracle.c")
+_OUT = os.path.join(_HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile ``ldu_oracle.c`` (gcc, OpenMP, no FP contraction)."""
+    if not force and os.path.exists(_OUT) and os.path.getmtime(_OUT) >= os.path.getmtime(_SRC):
+        return _OUT
+    os.makedirs(os.path.dirname(_OUT), exist_ok=True)
+    tmp = _OUT + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-fno-fast-math", _SRC, "-o", tmp, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _OUT)
+    return _OUT
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _i64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a), dtype=np.int64)
+
+
+def _f(a, dt=np.float64) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a), dtype=dt)
+
+
+def amul(owner, neighbour, diag, lower, upper, x, transpose=False, float_accumulate=False):
+    """y = A x (or A^T x) in the reference's summation order.
+
+    For float32 inputs the reference accumulates in float64 and returns
+    float64; ``float_accumulate=True`` instead gives the all-float variant
+    used as the specification of the mixed solver's inner FP32 Amul."""
+    dt = np.asarray(diag).dtype
+    dt = np.float32 if dt == np.float32 else np.float64
+    own, nei = _i64(owner), _i64(neighbour)
+    d, lo, up, xx = _f(diag, dt), _f(lower, dt), _f(upper, dt), _f(x, dt)
+    n, nf = d.shape[0], nei.shape[0]
+    acc = np.float32 if (dt == np.float32 and float_accumulate) else np.float64
+    y = np.empty(n, acc)
+    w = np.empty(2 * n + 1, acc)
+    if dt == np.float64:
+        fn = lib().orc_amul_f64
+    else:
+        fn = lib().orc_amul_f32acc if float_accumulate else lib().orc_amul_f32
+    fn(ctypes.c_int64(n), ctypes.c_int64(nf), _p(own), _p(nei), _p(d), _p(lo), _p(up), _p(xx),
+       _p(y), ctypes.c_int(1 if transpose else 0), _p(w))
+    return y
+
+
+def amul_T(owner, neighbour, diag, lower, upper, x):
+    return amul(owner, neighbour, diag, lower, upper, x, transpose=True)
+
+
+def dic_build(owner, neighbour, diag, upper):
+    own, nei = _i64(owner), _i64(neighbour)
+    d0, up = _f(diag), _f(upper)
+    n, nf = d0.shape[0], nei.shape[0]
+    d = np.empty(n)
+    wp = np.empty(n + 1, np.int64)
+    wf = np.empty(nf + 1, np.int64)
+    lib().orc_dic_build_f64(ctypes.c_int64(n), ctypes.c_int64(nf), _p(own), _p(nei), _p(d0),
+                            _p(up), _p(d), _p(wp), _p(wf))
+    return d
+
+
+def dilu_build(owner, neighbour, diag, lower, upper):
+    own, nei = _i64(owner), _i64(neighbour)
+    d0, lo, up = _f(diag), _f(lower), _f(upper)
+    n, nf = d0.shape[0], nei.shape[0]
+    d = np.empty(n)
+    lib().orc_dilu_build_f64(ctypes.c_int64(n), ctypes.c_int64(nf), _p(own), _p(nei), _p(d0),
+                             _p(lo), _p(up), _p(d))
+    return d
+
+
+def dic_apply_full(owner, neighbour, upper, pd, r):
+    own, nei = _i64(owner), _i64(neighbour)
+    up, pdd, rr = _f(upper), _f(pd), _f(r)
+    z = np.empty_like(rr)
+    lib().orc_dic_apply_full_f64(ctypes.c_int64(rr.shape[0]), ctypes.c_int64(nei.shape[0]),
+                                 _p(own), _p(nei), _p(up), _p(pdd), _p(rr), _p(z))
+    return z
+
+
+def dilu_apply_full(owner, neighbour, lower, upper, pd, r):
+    own, nei = _i64(owner), _i64(neighbour)
+    lo, up, pdd, rr = _f(lower), _f(upper), _f(pd), _f(r)
+    z = np.empty_like(rr)
+    lib().orc_dilu_apply_full_f64(ctypes.c_int64(rr.shape[0]), ctypes.c_int64(nei.shape[0]),
+                                  _p(own), _p(nei), _p(lo), _p(up), _p(pdd), _p(rr), _p(z))
+    return z
+
+
+@dataclass
+class SolveResult:
+    x: np.ndarray
+    iterations: int
+    final_residual: float
+    converged: bool
+    history: np.ndarray
+
+
+def _solve(fn, owner, neighbour, diag, lower, upper, b, x0, precond_diag, tolerance, rel_tol,
+           max_iter, min_iter, threads, *extra):
+    own, nei = _i64(owner), _i64(neighbour)
+    d, lo, up, bb = _f(diag), _f(lower), _f(upper), _f(b)
+    x = _f(x0).copy()
+    pd = None if precond_diag is None else _f(precond_diag)
+    hist = np.zeros(2 * max_iter + 4)
+    nh = ctypes.c_int(0)
+    conv = fn(ctypes.c_int64(d.shape[0]), ctypes.c_int64(nei.shape[0]), _p(own), _p(nei), _p(d),
+              _p(lo), _p(up), None if pd is None else _p(pd), _p(bb), _p(x),
+              ctypes.c_double(tolerance), ctypes.c_double(rel_tol), ctypes.c_int(max_iter),
+              ctypes.c_int(min_iter), ctypes.c_int(threads), _p(hist), ctypes.byref(nh), *extra)
+    h = hist[: nh.value].copy()
+    return SolveResult(x, nh.value, float(h[-1]) if nh.value else 0.0, bool(conv), h)
+
+
+def pcg(owner, neighbour, diag, lower, upper, b, x0, precond_diag=None, tolerance=1e-6,
+        rel_tol=0.01, max_iter=1000, min_iter=0, threads=1) -> SolveResult:
+    """PCG exactly as ``solvers/pcg.py:97-187``; ``precond_diag`` is the
+    factorised DIC/DILU diagonal (``None`` = no preconditioner)."""
+    return _solve(lib().orc_pcg_f64, owner, neighbour, diag, lower, upper, b, x0, precond_diag,
+                  tolerance, rel_tol, max_iter, min_iter, threads)
+
+
+def pbicgstab(owner, neighbour, diag, lower, upper, b, x0, precond_diag=None, tolerance=1e-6,
+              rel_tol=0.01, max_iter=1000, min_iter=0, threads=1,
+              omega: str = "reference") -> SolveResult:
+    """PBiCGStab exactly as ``solvers/pbicgstab.py:103-239`` (omega =
+    (t.z)/(t.t)); ``omega="standard"`` uses (t.s)/(t.t) instead."""
+    return _solve(lib().orc_pbicgstab_f64, owner, neighbour, diag, lower, upper, b, x0,
+                  precond_diag, tolerance, rel_tol, max_iter, min_iter, threads,
+                  ctypes.c_int(1 if omega == "standard" else 0))
+
+
+def laplacian(n_cells, owner_all, neighbour, face_areas, delta, D_face, volumes):
+    """``fvm.laplacian`` coefficients (lower, upper, diag) for per-face D."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    fa, dl, D, V = _f(face_areas).reshape(-1, 3), _f(delta), _f(D_face), _f(volumes)
+    nint, nfaces = nei.shape[0], own.shape[0]
+    lo, up, dg = np.empty(nint), np.empty(nint), np.empty(n_cells)
+    w = np.empty(3 * n_cells + 1)
+    lib().orc_laplacian_f64(ctypes.c_int64(n_cells), ctypes.c_int64(nint), ctypes.c_int64(nfaces),
+                            _p(own), _p(nei), _p(fa), _p(dl), _p(D), _p(V), _p(lo), _p(up),
+                            _p(dg), _p(w))
+    return lo, up, dg
+
+
+def div_upwind(n_cells, owner, neighbour, flux, volumes):
+    """``fvm.div(phi, U, "Gauss upwind")`` coefficients (lower, upper, diag)."""
+    own, nei = _i64(owner), _i64(neighbour)
+    F, V = _f(flux), _f(volumes)
+    nint = nei.shape[0]
+    lo, up, dg = np.empty(nint), np.empty(nint), np.empty(n_cells)
+    w = np.empty(2 * n_cells + 1)
+    lib().orc_div_upwind_f64(ctypes.c_int64(n_cells), ctypes.c_int64(nint), _p(own), _p(nei),
+                             _p(F), _p(V), _p(lo), _p(up), _p(dg), _p(w))
+    return lo, up, dg
+
+
+def dls_grads(owner, neighbour, lam, x):
+    own, nei = _i64(owner), _i64(neighbour)
+    la, xx = _f(lam), _f(x)
+    n, nf = la.shape[0], nei.shape[0]
+    gd, gl, gu = np.empty(n), np.empty(nf), np.empty(nf)
+    lib().orc_dls_grads_f64(ctypes.c_int64(n), ctypes.c_int64(nf), _p(own), _p(nei), _p(la),
+                            _p(xx), _p(gd), _p(gl), _p(gu))
+    return gd, gl, gu
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())

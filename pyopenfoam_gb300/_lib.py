@@ -1,0 +1,153 @@
+"""ctypes binding of libgbfoam.so (the C ABI declared in include/gbfoam.h).
+
+This is the whole bridge between the Python classes and the CUDA kernels:
+torch owns the memory and the stream, the kernels get raw device pointers.
+There is no CPU fallback: if the library cannot be loaded, every operation
+raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import torch
+
+from . import build as _build
+
+__all__ = [
+    "lib",
+    "check",
+    "Layout",
+    "SolveParams",
+    "SolveResult",
+    "ptr",
+    "stream_ptr",
+    "EXPORTED",
+    "GBF_CONVERGED",
+    "GBF_BREAKDOWN",
+    "GBF_MAX_ITER",
+]
+
+GBF_RUNNING, GBF_CONVERGED, GBF_BREAKDOWN, GBF_MAX_ITER = 0, 1, 2, 3
+
+_c_i32 = ctypes.c_int32
+_c_i64 = ctypes.c_int64
+_c_vp = ctypes.c_void_p
+_c_dbl = ctypes.c_double
+_c_size = ctypes.c_size_t
+
+
+class Layout(ctypes.Structure):
+    """``gbf_layout``: cell-sliced LDU addressing (device pointers)."""
+
+    _fields_ = [
+        ("n_cells", _c_i32),
+        ("n_faces", _c_i32),
+        ("n_slices", _c_i32),
+        ("max_width", _c_i32),
+        ("n_slots", _c_i64),
+        ("slice_off", _c_vp),
+        ("slice_w", _c_vp),
+        ("slot_col", _c_vp),
+        ("slot_face", _c_vp),
+        ("owner", _c_vp),
+        ("neighbour", _c_vp),
+    ]
+
+
+class SolveParams(ctypes.Structure):
+    _fields_ = [
+        ("tolerance", _c_dbl),
+        ("rel_tol", _c_dbl),
+        ("max_iter", _c_i32),
+        ("min_iter", _c_i32),
+        ("check_every", _c_i32),
+        ("variant", _c_i32),
+    ]
+
+
+class SolveResult(ctypes.Structure):
+    _fields_ = [
+        ("iterations", _c_i32),
+        ("status", _c_i32),
+        ("final_residual", _c_dbl),
+        ("initial_residual", _c_dbl),
+        ("inner_iterations", _c_i32),
+        ("outer_updates", _c_i32),
+    ]
+
+
+_P = ctypes.POINTER
+_L = _P(Layout)
+
+# name -> (restype, argtypes); the complete exported surface of gbfoam.h
+EXPORTED: dict[str, tuple] = {
+    "gbf_last_error": (ctypes.c_char_p, []),
+    "gbf_version": (ctypes.c_int, []),
+    "gbf_device_sm_count": (ctypes.c_int, [_P(_c_i32)]),
+    "gbf_layout_plan": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _P(_c_i32), _P(_c_i64), _P(_c_i32)]),
+    "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
+    "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
+    "gbf_pack_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_pack_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_pack_f64_to_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_amul_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
+    "gbf_amul_f32_f64out": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
+    "gbf_amul_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
+    "gbf_dic_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp, _c_vp]),
+    "gbf_dilu_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp, _c_vp]),
+    "gbf_diag_apply_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_pcg_workspace_bytes": (_c_size, [_c_i32]),
+    "gbf_pcg_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                         _P(SolveParams), _P(SolveResult), _c_vp, _c_size, _c_vp]),
+    "gbf_pbicgstab_workspace_bytes": (_c_size, [_c_i32]),
+    "gbf_pbicgstab_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                               _P(SolveParams), _P(SolveResult), _c_vp, _c_size,
+                                               _c_vp]),
+}
+
+_lock = threading.Lock()
+_handle = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load (building first if needed) libgbfoam.so."""
+    global _handle
+    if _handle is None:
+        with _lock:
+            if _handle is None:
+                path = _build.LIB_PATH
+                if not os.path.exists(path) or os.environ.get("GBFOAM_REBUILD"):
+                    path = _build.build()
+                h = ctypes.CDLL(path)
+                for name, (res, args) in EXPORTED.items():
+                    fn = getattr(h, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _handle = h
+    return _handle
+
+
+class GbfError(RuntimeError):
+    """A libgbfoam entry point returned a non-zero status."""
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        msg = lib().gbf_last_error().decode(errors="replace")
+        raise GbfError(f"{what or 'libgbfoam'} failed (status {rc}): {msg}")
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    """Raw device pointer of a contiguous tensor (None passes NULL)."""
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def stream_ptr(device: torch.device) -> int:
+    """cudaStream_t of torch's current stream on ``device``."""
+    return torch.cuda.current_stream(device).cuda_stream

@@ -1,0 +1,153 @@
+"""Mesh-topology data shared by every matrix on the same owner/neighbour
+addressing: the cell-sliced slot layout and the DIC / DILU wavefront
+schedules.
+
+Built once on the host (libgbfoam ``gbf_layout_*``, ``gbf_*_schedule``) and
+kept on the device.  The reference rebuilds its per-cell face lists on every
+preconditioner construction (``solvers/preconditioners.py:116-122``) and
+caches a CSR copy per matrix (``core/ldu_matrix.py:101-102``); here one
+topology object is cached per addressing and shared by all matrices on it.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections import OrderedDict
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .._lib import Layout, check, lib
+
+__all__ = ["Topology", "get_topology", "Schedule"]
+
+
+@dataclass
+class Schedule:
+    """Wavefront levels: items of level l are items[ptr[l]:ptr[l+1]]."""
+
+    ptr: torch.Tensor
+    items: torch.Tensor
+    n_levels: int
+    max_level_size: int
+
+
+def _i32_host(t: torch.Tensor, n_cells: int, name: str) -> np.ndarray:
+    a = t.detach().to("cpu", torch.int64).numpy()
+    if a.size and (a.min() < 0 or a.max() >= n_cells):
+        raise ValueError(f"{name} holds a cell index outside [0, {n_cells})")
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Topology:
+    """Device-resident slot layout of one owner/neighbour addressing."""
+
+    def __init__(self, n_cells: int, owner: torch.Tensor, neighbour: torch.Tensor) -> None:
+        if n_cells < 0 or n_cells >= 2**31:
+            raise ValueError(f"n_cells={n_cells} outside [0, 2^31)")
+        if owner.shape[0] != neighbour.shape[0]:
+            raise ValueError(
+                f"owner has {owner.shape[0]} faces, neighbour has {neighbour.shape[0]}"
+            )
+        dev = owner.device
+        self.device = dev
+        self.n_cells = int(n_cells)
+        self.n_faces = int(neighbour.shape[0])
+        self._own_h = _i32_host(owner, n_cells, "owner")
+        self._nei_h = _i32_host(neighbour, n_cells, "neighbour")
+        L = lib()
+        ns, nslots, mw = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        check(
+            L.gbf_layout_plan(self.n_cells, self.n_faces, self._own_h.ctypes.data,
+                              self._nei_h.ctypes.data, ctypes.byref(ns), ctypes.byref(nslots),
+                              ctypes.byref(mw)),
+            "gbf_layout_plan",
+        )
+        self.n_slices, self.n_slots, self.max_width = ns.value, nslots.value, mw.value
+        off = np.empty(self.n_slices + 1, np.int32)
+        w = np.empty(max(self.n_slices, 1), np.int32)
+        col = np.empty(max(self.n_slots, 1), np.int32)
+        face = np.empty(max(self.n_slots, 1), np.int32)
+        check(
+            L.gbf_layout_fill(self.n_cells, self.n_faces, self._own_h.ctypes.data,
+                              self._nei_h.ctypes.data, off.ctypes.data, w.ctypes.data,
+                              col.ctypes.data, face.ctypes.data),
+            "gbf_layout_fill",
+        )
+        to = lambda a: torch.from_numpy(a).to(dev)  # noqa: E731
+        self.slice_off = to(off)
+        self.slice_w = to(w)
+        self.slot_col = to(col)
+        self.slot_face = to(face)
+        self.owner32 = to(self._own_h) if self.n_faces else torch.zeros(1, dtype=torch.int32, device=dev)
+        self.neighbour32 = to(self._nei_h) if self.n_faces else torch.zeros(1, dtype=torch.int32, device=dev)
+        self.layout = Layout(
+            self.n_cells, self.n_faces, self.n_slices, self.max_width, self.n_slots,
+            self.slice_off.data_ptr(), self.slice_w.data_ptr(), self.slot_col.data_ptr(),
+            self.slot_face.data_ptr(), self.owner32.data_ptr(), self.neighbour32.data_ptr(),
+        )
+        self._dic: Schedule | None = None
+        self._dilu: Schedule | None = None
+
+    @property
+    def layout_ref(self):
+        return ctypes.byref(self.layout)
+
+    def dic_schedule(self) -> Schedule:
+        if self._dic is None:
+            n = self.n_cells
+            ptr = np.empty(n + 1, np.int32)
+            cells = np.empty(max(n, 1), np.int32)
+            nl, mx = ctypes.c_int32(), ctypes.c_int32()
+            check(
+                lib().gbf_dic_schedule(n, self.n_faces, self._own_h.ctypes.data,
+                                       self._nei_h.ctypes.data, ptr.ctypes.data,
+                                       cells.ctypes.data, ctypes.byref(nl), ctypes.byref(mx)),
+                "gbf_dic_schedule",
+            )
+            self._dic = Schedule(torch.from_numpy(ptr[: nl.value + 1].copy()).to(self.device),
+                                 torch.from_numpy(cells).to(self.device), nl.value, mx.value)
+        return self._dic
+
+    def dilu_schedule(self) -> Schedule:
+        if self._dilu is None:
+            nf = self.n_faces
+            ptr = np.empty(nf + 1, np.int32)
+            faces = np.empty(max(nf, 1), np.int32)
+            nl, mx = ctypes.c_int32(), ctypes.c_int32()
+            check(
+                lib().gbf_dilu_schedule(self.n_cells, nf, self._own_h.ctypes.data,
+                                        self._nei_h.ctypes.data, ptr.ctypes.data,
+                                        faces.ctypes.data, ctypes.byref(nl), ctypes.byref(mx)),
+                "gbf_dilu_schedule",
+            )
+            self._dilu = Schedule(torch.from_numpy(ptr[: nl.value + 1].copy()).to(self.device),
+                                  torch.from_numpy(faces).to(self.device), nl.value, mx.value)
+        return self._dilu
+
+
+_CACHE: "OrderedDict[tuple, tuple]" = OrderedDict()
+_CACHE_SIZE = 8
+
+
+def get_topology(n_cells: int, owner: torch.Tensor, neighbour: torch.Tensor) -> Topology:
+    """Cached Topology of (n_cells, owner, neighbour).
+
+    The key holds the tensors' pointers and in-place version counters; the
+    cache entry keeps the tensors alive, so a pointer cannot be recycled
+    while its entry exists.
+    """
+    key = (
+        str(owner.device), int(n_cells), owner.data_ptr(), owner.numel(), owner._version,
+        neighbour.data_ptr(), neighbour.numel(), neighbour._version,
+    )
+    hit = _CACHE.get(key)
+    if hit is not None:
+        _CACHE.move_to_end(key)
+        return hit[0]
+    topo = Topology(n_cells, owner, neighbour)
+    _CACHE[key] = (topo, owner, neighbour)
+    while len(_CACHE) > _CACHE_SIZE:
+        _CACHE.popitem(last=False)
+    return topo

@@ -1,0 +1,101 @@
+// Coefficient packing and the stand-alone Amul entry points.
+#include "amul.cuh"
+
+namespace gbf {
+
+// One thread per lane of every slice (padding lanes of the last slice
+// included, so that all slots are written).
+template <typename S, typename T>
+__global__ void __launch_bounds__(kBlock)
+    pack_kernel(gbf_layout L, const S* __restrict__ own_src, const S* __restrict__ nei_src,
+                T* __restrict__ coef) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.n_slices * 32) return;
+  const CellSlots cs = cell_slots(L, c);
+  for (int k = 0; k < cs.wo; ++k) {
+    const int i = cs.base + 32 * k;
+    const int f = L.slot_face[i];
+    coef[i] = (f >= 0) ? (T)own_src[f] : (T)0;
+  }
+  for (int k = 0; k < cs.wn; ++k) {
+    const int i = cs.base + 32 * (cs.wo + k);
+    const int f = L.slot_face[i];
+    coef[i] = (f >= 0) ? (T)nei_src[f] : (T)0;
+  }
+}
+
+template <typename T, typename A, bool NEI_FIRST>
+__global__ void __launch_bounds__(kBlock)
+    amul_kernel(gbf_layout L, const T* __restrict__ coef, const T* __restrict__ diag,
+                const T* __restrict__ x, A* __restrict__ y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.n_cells) return;
+  y[c] = cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, __ldg(x + c));
+}
+
+int check_layout(const gbf_layout* L) {
+  GBF_REQUIRE(L != nullptr, "layout is NULL");
+  GBF_REQUIRE(L->n_cells >= 0 && L->n_faces >= 0, "negative layout size");
+  GBF_REQUIRE(L->n_slices == (L->n_cells + 31) / 32, "layout n_slices does not match n_cells");
+  if (L->n_cells > 0)
+    GBF_REQUIRE(L->slice_off && L->slice_w && L->slot_col && L->slot_face,
+                "layout arrays are NULL");
+  return GBF_OK;
+}
+
+template <typename S, typename T>
+static int pack(const gbf_layout* L, const S* own_src, const S* nei_src, T* coef, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  if (L->n_slots == 0) return GBF_OK;
+  GBF_REQUIRE(coef && (L->n_faces == 0 || (own_src && nei_src)), "pack: NULL pointer");
+  const int grid = (L->n_slices * 32 + kBlock - 1) / kBlock;
+  pack_kernel<S, T><<<grid, kBlock, 0, as_stream(stream)>>>(*L, own_src, nei_src, coef);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+template <typename T, typename A>
+static int amul(const gbf_layout* L, const T* coef, const T* diag, const T* x, A* y,
+                int nei_first, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  if (L->n_cells == 0) return GBF_OK;
+  GBF_REQUIRE(diag && x && y && (L->n_faces == 0 || coef), "amul: NULL pointer");
+  const int grid = (L->n_cells + kBlock - 1) / kBlock;
+  if (nei_first)
+    amul_kernel<T, A, true><<<grid, kBlock, 0, as_stream(stream)>>>(*L, coef, diag, x, y);
+  else
+    amul_kernel<T, A, false><<<grid, kBlock, 0, as_stream(stream)>>>(*L, coef, diag, x, y);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+}  // namespace gbf
+
+extern "C" int gbf_pack_f64(const gbf_layout* L, const double* own_src, const double* nei_src,
+                            double* slot_coef, void* stream) {
+  return gbf::pack<double, double>(L, own_src, nei_src, slot_coef, stream);
+}
+extern "C" int gbf_pack_f32(const gbf_layout* L, const float* own_src, const float* nei_src,
+                            float* slot_coef, void* stream) {
+  return gbf::pack<float, float>(L, own_src, nei_src, slot_coef, stream);
+}
+extern "C" int gbf_pack_f64_to_f32(const gbf_layout* L, const double* own_src,
+                                   const double* nei_src, float* slot_coef, void* stream) {
+  return gbf::pack<double, float>(L, own_src, nei_src, slot_coef, stream);
+}
+
+extern "C" int gbf_amul_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                            const double* x, double* y, int32_t nei_first, void* stream) {
+  return gbf::amul<double, double>(L, slot_coef, diag, x, y, nei_first, stream);
+}
+extern "C" int gbf_amul_f32_f64out(const gbf_layout* L, const float* slot_coef,
+                                   const float* diag, const float* x, double* y,
+                                   int32_t nei_first, void* stream) {
+  return gbf::amul<float, double>(L, slot_coef, diag, x, y, nei_first, stream);
+}
+extern "C" int gbf_amul_f32(const gbf_layout* L, const float* slot_coef, const float* diag,
+                            const float* x, float* y, int32_t nei_first, void* stream) {
+  return gbf::amul<float, float>(L, slot_coef, diag, x, y, nei_first, stream);
+}

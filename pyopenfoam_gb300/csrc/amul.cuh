@@ -1,0 +1,66 @@
+// Cell-centred LDU gather (Amul) used by every kernel that needs A*x.
+//
+// One thread per cell, one warp per 32-cell slice.  Owner-side and
+// neighbour-side slot sums are formed separately, each starting from 0.0 in
+// ascending face order, and combined as (diag*x + S_first) + S_second --
+// the association and rounding of the reference's
+//   y = diag*x; y = y + scatter_add(...); y = y + scatter_add(...)
+// (core/ldu_matrix.py:200-215, core/backend.py:58-64).
+#pragma once
+
+#include "common.cuh"
+
+namespace gbf {
+
+// Sum over `cnt` slots starting at slot index i0 (stride 32) of
+// coef[slot] * x[col[slot]], skipping padding (col < 0).  Products are
+// rounded in T, sums in A.
+template <typename T, typename A>
+__device__ __forceinline__ A slot_sum(const int32_t* __restrict__ slot_col,
+                                      const T* __restrict__ coef, const T* __restrict__ x,
+                                      int i0, int cnt) {
+  A s = (A)0;
+  if (cnt <= 4) {
+    int col[4];
+    T a[4], xv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) col[k] = (k < cnt) ? __ldg(slot_col + i0 + 32 * k) : -1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = (col[k] >= 0) ? __ldg(coef + i0 + 32 * k) : (T)0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (col[k] >= 0) s = add_rn(s, (A)mul_rn(a[k], xv[k]));
+  } else {
+#pragma unroll 4
+    for (int k = 0; k < cnt; ++k) {
+      const int col = __ldg(slot_col + i0 + 32 * k);
+      if (col >= 0) s = add_rn(s, (A)mul_rn(__ldg(coef + i0 + 32 * k), __ldg(x + col)));
+    }
+  }
+  return s;
+}
+
+// (A x)[c] with x[c] already loaded as xc.
+template <typename T, typename A, bool NEI_FIRST>
+__device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict__ coef,
+                                       const T* __restrict__ diag, const T* __restrict__ x,
+                                       int c, T xc) {
+  A y = (A)mul_rn(__ldg(diag + c), xc);
+  if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    const A so = slot_sum<T, A>(L.slot_col, coef, x, cs.base, cs.wo);
+    const A sn = slot_sum<T, A>(L.slot_col, coef, x, cs.base + 32 * cs.wo, cs.wn);
+    if (NEI_FIRST) {
+      y = add_rn(y, sn);
+      y = add_rn(y, so);
+    } else {
+      y = add_rn(y, so);
+      y = add_rn(y, sn);
+    }
+  }
+  return y;
+}
+
+}  // namespace gbf

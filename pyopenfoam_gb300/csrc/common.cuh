@@ -1,0 +1,129 @@
+// Shared device helpers of libgbfoam: error reporting, slice addressing,
+// deterministic reductions and the last-block ticket.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "gbfoam.h"
+
+namespace gbf {
+
+// Per-thread error message (gbf_last_error()).
+void set_error(const char* fmt, ...);
+
+#define GBF_CHECK_CUDA(call)                                                   \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ::gbf::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                       __FILE__, __LINE__);                                    \
+      return GBF_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
+#define GBF_CHECK_LAUNCH() GBF_CHECK_CUDA(cudaGetLastError())
+
+#define GBF_REQUIRE(cond, ...)                                                 \
+  do {                                                                         \
+    if (!(cond)) {                                                             \
+      ::gbf::set_error(__VA_ARGS__);                                           \
+      return GBF_ERR_ARG;                                                      \
+    }                                                                          \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Threads per block of the cell kernels.  Must stay a multiple of 32 so that
+// a warp covers exactly one 32-cell slice.
+constexpr int kBlock = 256;
+
+int check_layout(const gbf_layout* L);  // validates sizes / pointers
+int reduction_grid();  // fixed grid of the reducing kernels (SMs x 8, <= kMaxGrid)
+constexpr int kMaxGrid = 4096;
+
+// --------------------------------------------------------------------------
+// Slice addressing of one cell.
+// --------------------------------------------------------------------------
+struct CellSlots {
+  int base;  // slot of k = 0 for this lane
+  int wo;    // owner-side slot count of the slice
+  int wn;    // neighbour-side slot count of the slice
+};
+
+__device__ __forceinline__ CellSlots cell_slots(const gbf_layout& L, int c) {
+  const int s = c >> 5;
+  const int w = __ldg(L.slice_w + s);
+  CellSlots r;
+  r.base = __ldg(L.slice_off + s) + (c & 31);
+  r.wo = w & 0xffff;
+  r.wn = w >> 16;
+  return r;
+}
+
+// --------------------------------------------------------------------------
+// Deterministic sums: fixed shuffle tree inside a warp, fixed tree over the
+// warps of a block, partials reduced by the last block in index order.
+// --------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of v over the block; valid in thread 0 only.  `sh` holds blockDim/32.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();  // sh may still be read by a previous call
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T t = (T)0;
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    t = (lane < nw) ? sh[lane] : (T)0;
+    t = warp_sum(t);
+  }
+  return t;
+}
+
+// Returns true in every thread of the block that finished last.  The caller
+// wrote its partials (thread 0) before calling.  The ticket counter is reset
+// by the last block.
+__device__ __forceinline__ bool last_block_done(unsigned int* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int t = atomicAdd(ticket, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
+  return am_last;
+}
+
+// Sum of partials[0..n) in a fixed order, by the whole block; result in
+// thread 0.  Reads through L2 (other blocks wrote them).
+template <typename T>
+__device__ __forceinline__ T reduce_partials(const T* partials, int n, T* sh) {
+  T v = (T)0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v += __ldcg(partials + i);
+  return block_sum(v, sh);
+}
+
+// Canonical IEEE helpers (one rounding each, never contracted to FMA).
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+}  // namespace gbf

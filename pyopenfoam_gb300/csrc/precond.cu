@@ -1,0 +1,139 @@
+// DIC / DILU factorisation (level-scheduled wavefronts) and the diagonal
+// preconditioner apply.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace gbf {
+
+// One launch per level.  Cell c of the level subtracts, in the reference's
+// face order, (a*a)/d_j for each neighbour-side face (a = upper[f],
+// j = owner[f]) whose |d_j| > 1e-30, reading the factored value for j < c
+// (an earlier level) and the unfactored diagonal for j > c
+// (solvers/preconditioners.py:124-128).
+__global__ void __launch_bounds__(kBlock)
+    dic_level_kernel(gbf_layout L, const double* __restrict__ coef,
+                     const double* __restrict__ diag, const int32_t* __restrict__ level_ptr,
+                     const int32_t* __restrict__ level_cells, int level, double* d) {
+  const int start = __ldg(level_ptr + level);
+  const int count = __ldg(level_ptr + level + 1) - start;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int c = __ldg(level_cells + start + t);
+  double dc = __ldg(diag + c);
+  if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    for (int k = 0; k < cs.wn; ++k) {
+      const int i = cs.base + 32 * (cs.wo + k);
+      const int j = __ldg(L.slot_col + i);
+      if (j < 0) continue;
+      const double a = __ldg(coef + i);
+      const double dj = (j < c) ? __ldcg(d + j) : __ldg(diag + j);
+      if (fabs(dj) > 1e-30) dc = __dsub_rn(dc, __ddiv_rn(__dmul_rn(a, a), dj));
+    }
+  }
+  d[c] = dc;
+}
+
+// One launch per face level.  Each cell is touched by at most one face of a
+// level, so the two-ended update of preconditioners.py:254-268 (both ends
+// read before either is written) runs without conflicts.
+__global__ void __launch_bounds__(kBlock)
+    dilu_level_kernel(gbf_layout L, const double* __restrict__ lower,
+                      const double* __restrict__ upper, const int32_t* __restrict__ level_ptr,
+                      const int32_t* __restrict__ level_faces, int level, double* d) {
+  const int start = __ldg(level_ptr + level);
+  const int count = __ldg(level_ptr + level + 1) - start;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int f = __ldg(level_faces + start + t);
+  const int p = __ldg(L.owner + f), q = __ldg(L.neighbour + f);
+  const double l = __ldg(lower + f), u = __ldg(upper + f);
+  const double dp = __ldcg(d + p), dn = __ldcg(d + q);
+  if (fabs(dn) > 1e-30) d[p] = __dsub_rn(dp, __ddiv_rn(__dmul_rn(l, u), dn));
+  if (fabs(dp) > 1e-30) d[q] = __dsub_rn(dn, __ddiv_rn(__dmul_rn(u, l), dp));
+}
+
+// d = clamp(|d|, min=1e-30), NaN kept (torch.clamp semantics).
+__global__ void clamp_abs_kernel(int n, double* d) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double a = fabs(d[c]);
+  d[c] = (a < 1e-30) ? 1e-30 : a;
+}
+
+__global__ void copy_kernel(int n, const double* __restrict__ s, double* __restrict__ d) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) d[c] = s[c];
+}
+
+__global__ void diag_apply_kernel(int n, const double* __restrict__ r,
+                                  const double* __restrict__ d, double* __restrict__ z) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) z[c] = __ddiv_rn(r[c], d[c]);
+}
+
+}  // namespace gbf
+
+using namespace gbf;
+
+extern "C" int gbf_dic_build_f64(const gbf_layout* L, const double* coef, const double* diag,
+                                 const int32_t* level_ptr, const int32_t* level_cells,
+                                 int32_t n_levels, int32_t max_level_size, double* d_out,
+                                 void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int n = L->n_cells;
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(diag && d_out && level_ptr && level_cells, "dic_build: NULL pointer");
+  GBF_REQUIRE(L->n_faces == 0 || coef, "dic_build: NULL coefficients");
+  GBF_REQUIRE(n_levels >= 1 && max_level_size >= 1 && max_level_size <= n,
+              "dic_build: bad schedule (levels=%d, max size=%d)", n_levels, max_level_size);
+  cudaStream_t s = as_stream(stream);
+  const int grid = (max_level_size + kBlock - 1) / kBlock;
+  for (int lv = 0; lv < n_levels; ++lv) {
+    dic_level_kernel<<<grid, kBlock, 0, s>>>(*L, coef, diag, level_ptr, level_cells, lv, d_out);
+  }
+  GBF_CHECK_LAUNCH();
+  clamp_abs_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(n, d_out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_dilu_build_f64(const gbf_layout* L, const double* lower, const double* upper,
+                                  const double* diag, const int32_t* level_ptr,
+                                  const int32_t* level_faces, int32_t n_levels,
+                                  int32_t max_level_size, double* d_out, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int n = L->n_cells;
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(diag && d_out, "dilu_build: NULL pointer");
+  cudaStream_t s = as_stream(stream);
+  copy_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(n, diag, d_out);
+  GBF_CHECK_LAUNCH();
+  if (L->n_faces > 0) {
+    GBF_REQUIRE(lower && upper && level_ptr && level_faces && L->owner && L->neighbour,
+                "dilu_build: NULL pointer");
+    GBF_REQUIRE(n_levels >= 1 && max_level_size >= 1 && max_level_size <= L->n_faces,
+                "dilu_build: bad schedule (levels=%d, max size=%d)", n_levels, max_level_size);
+    const int grid = (max_level_size + kBlock - 1) / kBlock;
+    for (int lv = 0; lv < n_levels; ++lv)
+      dilu_level_kernel<<<grid, kBlock, 0, s>>>(*L, lower, upper, level_ptr, level_faces, lv,
+                                                d_out);
+    GBF_CHECK_LAUNCH();
+  }
+  clamp_abs_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(n, d_out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_diag_apply_f64(int32_t n, const double* r, const double* d, double* z,
+                                  void* stream) {
+  GBF_REQUIRE(n >= 0, "diag_apply: negative size");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(r && d && z, "diag_apply: NULL pointer");
+  diag_apply_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(n, r, d, z);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}

@@ -1,0 +1,205 @@
+// Host-side topology analysis, run once per mesh: the cell-sliced slot layout
+// and the wavefront schedules of the DIC and DILU factorisations.
+//
+// The reference recomputes its per-cell face lists on every preconditioner
+// build with Python loops (solvers/preconditioners.py:116-122, :254-268);
+// here they are computed once, in O(n + F), and reused by every launch.
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "gbfoam.h"
+
+namespace gbf {
+void set_error(const char* fmt, ...);
+}
+
+namespace {
+
+int check_faces(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei) {
+  if (n < 0 || nf < 0) {
+    gbf::set_error("negative size: n_cells=%d n_faces=%d", n, nf);
+    return GBF_ERR_ARG;
+  }
+  if (nf > 0 && (!own || !nei)) {
+    gbf::set_error("owner/neighbour pointer is NULL");
+    return GBF_ERR_ARG;
+  }
+  for (int32_t f = 0; f < nf; ++f) {
+    if (own[f] < 0 || own[f] >= n || nei[f] < 0 || nei[f] >= n) {
+      gbf::set_error("face %d addresses a cell outside [0, %d): owner=%d neighbour=%d", f, n,
+                     own[f], nei[f]);
+      return GBF_ERR_RANGE;
+    }
+    if (own[f] == nei[f]) {
+      gbf::set_error("face %d has owner == neighbour (%d)", f, own[f]);
+      return GBF_ERR_RANGE;
+    }
+  }
+  return GBF_OK;
+}
+
+// counts of owner-side / neighbour-side faces per cell
+void face_counts(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                 std::vector<int32_t>& co, std::vector<int32_t>& cn) {
+  co.assign((size_t)n, 0);
+  cn.assign((size_t)n, 0);
+  for (int32_t f = 0; f < nf; ++f) {
+    co[own[f]]++;
+    cn[nei[f]]++;
+  }
+}
+
+// Stable per-cell lists of neighbour-side faces (ascending face order).
+void neighbour_lists(int32_t n, int32_t nf, const int32_t* nei, std::vector<int64_t>& ptr,
+                     std::vector<int32_t>& faces) {
+  ptr.assign((size_t)n + 1, 0);
+  for (int32_t f = 0; f < nf; ++f) ptr[(size_t)nei[f] + 1]++;
+  for (int32_t c = 0; c < n; ++c) ptr[c + 1] += ptr[c];
+  faces.resize((size_t)nf);
+  std::vector<int64_t> cur(ptr.begin(), ptr.end() - 1);
+  for (int32_t f = 0; f < nf; ++f) faces[cur[nei[f]]++] = f;
+}
+
+// Counting sort of items by level (stable: ascending item index per level).
+void bucket_by_level(int32_t n_items, const std::vector<int32_t>& level, int32_t n_levels,
+                     int32_t* level_ptr, int32_t* items, int32_t* max_size) {
+  std::vector<int32_t> cnt((size_t)n_levels + 1, 0);
+  for (int32_t i = 0; i < n_items; ++i) cnt[(size_t)level[i] + 1]++;
+  int32_t mx = 0;
+  for (int32_t l = 0; l < n_levels; ++l) {
+    mx = std::max(mx, cnt[(size_t)l + 1]);
+    cnt[(size_t)l + 1] += cnt[l];
+  }
+  for (int32_t l = 0; l <= n_levels; ++l) level_ptr[l] = cnt[l];
+  for (int32_t i = 0; i < n_items; ++i) items[cnt[level[i]]++] = i;
+  *max_size = mx;
+}
+
+}  // namespace
+
+extern "C" int gbf_layout_plan(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                               int32_t* n_slices, int64_t* n_slots, int32_t* max_width) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  std::vector<int32_t> co, cn;
+  face_counts(n, nf, own, nei, co, cn);
+  const int32_t ns = (n + 31) / 32;
+  int64_t slots = 0;
+  int32_t mw = 0;
+  for (int32_t s = 0; s < ns; ++s) {
+    int32_t wo = 0, wn = 0;
+    for (int32_t c = s * 32; c < std::min(n, s * 32 + 32); ++c) {
+      wo = std::max(wo, co[c]);
+      wn = std::max(wn, cn[c]);
+    }
+    if (wo > 0xffff || wn > 0x7fff) {
+      gbf::set_error("a cell has more than 32767 faces");
+      return GBF_ERR_ARG;
+    }
+    slots += 32 * (int64_t)(wo + wn);
+    mw = std::max(mw, wo + wn);
+  }
+  if (slots >= ((int64_t)1 << 31)) {
+    gbf::set_error("matrix needs %lld slots; the layout holds < 2^31", (long long)slots);
+    return GBF_ERR_ARG;
+  }
+  *n_slices = ns;
+  *n_slots = slots;
+  *max_width = mw;
+  return GBF_OK;
+}
+
+extern "C" int gbf_layout_fill(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                               int32_t* slice_off, int32_t* slice_w, int32_t* slot_col,
+                               int32_t* slot_face) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  std::vector<int32_t> co, cn;
+  face_counts(n, nf, own, nei, co, cn);
+  const int32_t ns = (n + 31) / 32;
+  int64_t off = 0;
+  for (int32_t s = 0; s < ns; ++s) {
+    int32_t wo = 0, wn = 0;
+    for (int32_t c = s * 32; c < std::min(n, s * 32 + 32); ++c) {
+      wo = std::max(wo, co[c]);
+      wn = std::max(wn, cn[c]);
+    }
+    slice_off[s] = (int32_t)off;
+    slice_w[s] = wo | (wn << 16);
+    off += 32 * (int64_t)(wo + wn);
+  }
+  slice_off[ns] = (int32_t)off;
+  for (int64_t i = 0; i < off; ++i) {
+    slot_col[i] = -1;
+    slot_face[i] = -1;
+  }
+  // faces visited in ascending order: the k-th owner-side (neighbour-side)
+  // face of a cell goes to its k-th owner (neighbour) slot
+  std::vector<int32_t> ko((size_t)n, 0), kn((size_t)n, 0);
+  for (int32_t f = 0; f < nf; ++f) {
+    {
+      const int32_t c = own[f];
+      const int32_t s = c >> 5;
+      const int64_t slot = (int64_t)slice_off[s] + 32 * (int64_t)ko[c] + (c & 31);
+      ko[c]++;
+      slot_col[slot] = nei[f];
+      slot_face[slot] = f;
+    }
+    {
+      const int32_t c = nei[f];
+      const int32_t s = c >> 5;
+      const int32_t wo = slice_w[s] & 0xffff;
+      const int64_t slot = (int64_t)slice_off[s] + 32 * (int64_t)(wo + kn[c]) + (c & 31);
+      kn[c]++;
+      slot_col[slot] = own[f];
+      slot_face[slot] = f;
+    }
+  }
+  return GBF_OK;
+}
+
+extern "C" int gbf_dic_schedule(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                                int32_t* level_ptr, int32_t* level_cells, int32_t* n_levels,
+                                int32_t* max_level_size) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  std::vector<int64_t> ptr;
+  std::vector<int32_t> faces;
+  neighbour_lists(n, nf, nei, ptr, faces);
+  std::vector<int32_t> level((size_t)n, 0);
+  int32_t nl = (n > 0) ? 1 : 0;
+  for (int32_t c = 0; c < n; ++c) {
+    int32_t l = 0;
+    for (int64_t k = ptr[c]; k < ptr[c + 1]; ++k) {
+      const int32_t j = own[faces[k]];
+      if (j < c) l = std::max(l, level[j] + 1);  // j > c reads the unfactored diagonal
+    }
+    level[c] = l;
+    nl = std::max(nl, l + 1);
+  }
+  bucket_by_level(n, level, nl, level_ptr, level_cells, max_level_size);
+  *n_levels = nl;
+  return GBF_OK;
+}
+
+extern "C" int gbf_dilu_schedule(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                                 int32_t* level_ptr, int32_t* level_faces, int32_t* n_levels,
+                                 int32_t* max_level_size) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  std::vector<int32_t> last((size_t)n, -1), level((size_t)nf, 0);
+  int32_t nl = 0;
+  for (int32_t f = 0; f < nf; ++f) {
+    const int32_t l = std::max(last[own[f]], last[nei[f]]) + 1;
+    level[f] = l;
+    last[own[f]] = l;
+    last[nei[f]] = l;
+    nl = std::max(nl, l + 1);
+  }
+  bucket_by_level(nf, level, nl, level_ptr, level_faces, max_level_size);
+  *n_levels = nl;
+  return GBF_OK;
+}

@@ -1,0 +1,13 @@
+"""GPU linear solvers with the reference's ``pyfoam.solvers`` interface."""
+
+from .linear_solver import LinearSolverBase, create_solver, register_solver, solver_from_dict
+from .pbicgstab import PBiCGSTABSolver
+from .pcg import PCGSolver
+from .preconditioners import DICPreconditioner, DILUPreconditioner, Preconditioner
+from .residual import ConvergenceInfo, ResidualMonitor
+
+__all__ = [
+    "LinearSolverBase", "create_solver", "solver_from_dict", "register_solver", "PCGSolver",
+    "PBiCGSTABSolver", "DICPreconditioner", "DILUPreconditioner", "Preconditioner",
+    "ConvergenceInfo", "ResidualMonitor",
+]

@@ -1,0 +1,107 @@
+"""Residual monitoring, drop-in for ``pyfoam.solvers.residual``
+(``src/pyfoam/solvers/residual.py:27-168``).
+
+The GPU solvers evaluate the same rules on the device (L2 norm per check,
+``|r| < tolerance`` or ``|r|/|r0| < rel_tol`` once ``iteration >= min_iter``)
+and hand the residual history back through :meth:`ResidualMonitor.record`,
+so ``build_info`` reports exactly what the reference's monitor would.
+"""
+
+from __future__ import annotations
+
+import logging
+from dataclasses import dataclass, field
+
+import torch
+
+__all__ = ["ResidualMonitor", "ConvergenceInfo"]
+
+logger = logging.getLogger(__name__)
+
+
+@dataclass
+class ConvergenceInfo:
+    converged: bool
+    iterations: int
+    final_residual: float
+    initial_residual: float
+    residual_ratio: float
+    tolerance: float
+    residual_history: list[float] = field(default_factory=list)
+
+
+class ResidualMonitor:
+    def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, min_iter: int = 0,
+                 verbose: bool = False) -> None:
+        self._tolerance = tolerance
+        self._rel_tol = rel_tol
+        self._min_iter = min_iter
+        self._verbose = verbose
+        self._history: list[float] = []
+        self._initial_residual: float | None = None
+
+    @property
+    def tolerance(self) -> float:
+        return self._tolerance
+
+    @property
+    def rel_tol(self) -> float:
+        return self._rel_tol
+
+    @property
+    def min_iter(self) -> int:
+        return self._min_iter
+
+    @property
+    def history(self) -> list[float]:
+        return self._history
+
+    @property
+    def initial_residual(self) -> float | None:
+        return self._initial_residual
+
+    def reset(self) -> None:
+        self._history.clear()
+        self._initial_residual = None
+
+    def check(self, res_norm: float, iteration: int) -> bool:
+        """Record one residual norm and apply the convergence rules
+        (residual.py:112-145)."""
+        self._history.append(res_norm)
+        if self._initial_residual is None:
+            self._initial_residual = res_norm
+        if self._verbose:
+            ratio = res_norm / self._initial_residual if self._initial_residual > 0 else 0.0
+            logger.info("  Iteration %d: residual = %.6e (ratio = %.6e)", iteration, res_norm, ratio)
+        if iteration >= self._min_iter:
+            if res_norm < self._tolerance:
+                return True
+            if self._initial_residual > 0 and res_norm / self._initial_residual < self._rel_tol:
+                return True
+        return False
+
+    def update(self, residual: torch.Tensor, iteration: int) -> bool:
+        return self.check(float(torch.linalg.vector_norm(residual).item()), iteration)
+
+    def record(self, history: list[float]) -> None:
+        """Adopt a residual history produced on the device."""
+        self._history = list(history)
+        self._initial_residual = self._history[0] if self._history else None
+        if self._verbose:
+            for i, r in enumerate(self._history):
+                ratio = r / self._history[0] if self._history[0] > 0 else 0.0
+                logger.info("  Check %d: residual = %.6e (ratio = %.6e)", i, r, ratio)
+
+    def build_info(self, converged: bool) -> ConvergenceInfo:
+        initial = self._initial_residual or 0.0
+        final = self._history[-1] if self._history else 0.0
+        ratio = final / initial if initial > 0 else 0.0
+        return ConvergenceInfo(
+            converged=converged,
+            iterations=len(self._history),
+            final_residual=final,
+            initial_residual=initial,
+            residual_ratio=ratio,
+            tolerance=self._tolerance,
+            residual_history=list(self._history),
+        )

@@ -1,0 +1,134 @@
+"""Seeded test cases shared by the golden-fixture generator and the tests.
+
+Every generator is deterministic across platforms: indices are integer
+arithmetic, random values come from ``numpy.random.default_rng`` (PCG64), and
+the config-1 coefficients are exact powers of two.  The jittered-mesh case
+stores its geometry in the fixture, so no test depends on floating-point
+geometry being bit-identical across machines.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import os
+from types import SimpleNamespace
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "reference_outputs.npz")
+JITTER_FIXTURE = os.path.join(HERE, "jitter6_inputs.npz")
+
+
+def sha(a: np.ndarray) -> str:
+    """SHA-256 of the little-endian bytes of a float array (float64 unless
+    the array is float32)."""
+    a = np.asarray(a)
+    dt = "<f4" if a.dtype == np.float32 else "<f8"
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=dt).tobytes()).hexdigest()
+
+
+def hex_faces(nx: int, ny: int | None = None, nz: int | None = None):
+    """Internal faces of an nx*ny*nz hex mesh in upper-triangular cell order
+    (per cell +x, +y, +z): owner < neighbour, sorted by owner."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    n = nx * ny * nz
+    c = np.arange(n, dtype=np.int64)
+    i, j, k = c % nx, (c // nx) % ny, c // (nx * ny)
+    has = np.stack([i < nx - 1, j < ny - 1, k < nz - 1], axis=1)
+    flat = np.flatnonzero(has.ravel())
+    cell, d = flat // 3, flat % 3
+    step = np.array([1, nx, nx * ny], dtype=np.int64)
+    return n, cell, cell + step[d]
+
+
+def random_ldu(N: int, seed: int = 5, permute_faces: bool = False) -> dict:
+    """Random LDU coefficients on an N^3 hex topology.  With
+    ``permute_faces`` the face order is shuffled and a third of the faces
+    have owner > neighbour, which exercises unsorted, non-triangular
+    addressing."""
+    n, own, nei = hex_faces(N)
+    rng = np.random.default_rng(seed)
+    F = own.shape[0]
+    if permute_faces:
+        perm = rng.permutation(F)
+        own, nei = own[perm].copy(), nei[perm].copy()
+        flip = rng.random(F) < 0.33
+        own[flip], nei[flip] = nei[flip].copy(), own[flip].copy()
+    return dict(
+        n=n, owner=own, neighbour=nei,
+        lower=rng.uniform(-1.0, 0.0, F), upper=rng.uniform(-1.0, 0.0, F),
+        diag=rng.uniform(6.0, 7.0, n), x=rng.uniform(-1.0, 1.0, n),
+        r=rng.uniform(-1.0, 1.0, n),
+    )
+
+
+def c1_poisson(N: int = 32, seed: int = 0) -> dict:
+    """Config-1 system: N^3 uniform hex mesh of the unit cube, unit
+    diffusivity, fvm.laplacian per unit volume (face coefficient
+    |S| delta / V = N^2), Dirichlet on x = 0 (boundary coefficient 2 N^2),
+    zero gradient elsewhere; RHS U[-1, 1] from ``default_rng(seed)``.
+    All coefficients are exact in binary floating point."""
+    n, own, nei = hex_faces(N)
+    c = np.arange(n)
+    i = c % N
+    F = own.shape[0]
+    coeff = float(N * N)
+    lower = np.full(F, -coeff)
+    upper = np.full(F, -coeff)
+    cnt = np.bincount(own, minlength=n) + np.bincount(nei, minlength=n)
+    diag = cnt.astype(np.float64) * coeff + np.where(i == 0, 2.0 * coeff, 0.0)
+    b = np.random.default_rng(seed).uniform(-1.0, 1.0, n)
+    return dict(n=n, owner=own, neighbour=nei, lower=lower, upper=upper, diag=diag, b=b)
+
+
+def mesh_from_arrays(d: dict, device="cpu", dtype=None):
+    """Duck-typed FvMesh (the attributes fvm.laplacian / fvm.div read)."""
+    import torch
+
+    dtype = dtype or torch.float64
+    t = lambda a, dt=dtype: torch.as_tensor(np.asarray(a)).to(device=device, dtype=dt)  # noqa: E731
+    return SimpleNamespace(
+        n_cells=int(d["n_cells"]), n_internal_faces=int(d["n_internal"]),
+        n_faces=int(d["owner"].shape[0]),
+        owner=t(d["owner"], torch.int64), neighbour=t(d["neighbour"], torch.int64),
+        face_areas=t(d["face_areas"]), delta_coefficients=t(d["delta"]),
+        cell_volumes=t(d["volumes"]), device=torch.device(device), dtype=dtype,
+    )
+
+
+def jitter_case(N: int = 6, seed: int = 1, store: bool = True):
+    """Jittered (+-20 % h) N^3 mesh with Dirichlet x0, log-normal face
+    diffusivity, an all-positive upwind flux from u = (1, 0.5, 0.25) on the
+    nominal face areas, RHS and loss weights.  The arrays are written to /
+    read from ``jitter{N}_inputs.npz`` so that every machine uses the same
+    bits."""
+    path = os.path.join(HERE, f"jitter{N}_inputs.npz")
+    if os.path.exists(path):
+        z = np.load(path)
+        d = {k: z[k] for k in z.files}
+    else:
+        import sys
+
+        sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+        from pyopenfoam_gb300.mesh import HexMesh
+
+        m = HexMesh(N, jitter=0.2, seed=seed)
+        rng = np.random.default_rng(seed + 100)
+        nint = m.n_internal_faces
+        nom = HexMesh(N)  # unjittered: nominal face area vectors
+        u = np.array([1.0, 0.5, 0.25])
+        phi = (nom.numpy("face_areas") * u).sum(axis=1) * 3.0 * N
+        d = dict(
+            n_cells=np.int64(m.n_cells), n_internal=np.int64(nint),
+            owner=m.numpy("owner"), neighbour=m.numpy("neighbour"),
+            face_areas=m.numpy("face_areas"), delta=m.numpy("delta_coefficients"),
+            volumes=m.numpy("cell_volumes"),
+            gamma=rng.lognormal(0.0, 1.0, m.n_faces), phi=phi,
+            b=rng.uniform(-1.0, 1.0, m.n_cells), w=rng.uniform(-1.0, 1.0, m.n_cells),
+        )
+        if store:
+            np.savez_compressed(path, **d)
+    d["mesh"] = mesh_from_arrays(d)
+    return d

@@ -1,0 +1,173 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports
+every entry point of include/gbfoam.h, the host topology passes (slot
+layout, DIC/DILU wavefront schedules) are correct, and the Python surface
+validates arguments like the reference."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pyopenfoam_gb300 import _lib
+from pyopenfoam_gb300.solvers.residual import ResidualMonitor
+from tests.golden.cases import hex_faces, random_ldu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        txt = open(os.path.join(ROOT, "include", fn)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names |= set(re.findall(r"\b(gbf_[a-z0-9_]+)\s*\(", txt))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    declared = _declared()
+    assert declared, "no declarations found"
+    for name in sorted(declared):
+        assert hasattr(L, name), f"libgbfoam.so does not export {name}"
+    # and the ctypes table binds exactly the declared surface
+    assert declared == set(_lib.EXPORTED), declared ^ set(_lib.EXPORTED)
+    assert L.gbf_version() >= 1
+
+
+def _layout(n, own, nei):
+    L = _lib.lib()
+    o = np.ascontiguousarray(own, np.int32)
+    q = np.ascontiguousarray(nei, np.int32)
+    ns, nsl, mw = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+    _lib.check(L.gbf_layout_plan(n, o.shape[0], o.ctypes.data, q.ctypes.data, ctypes.byref(ns),
+                                 ctypes.byref(nsl), ctypes.byref(mw)))
+    off = np.empty(ns.value + 1, np.int32)
+    w = np.empty(max(ns.value, 1), np.int32)
+    col = np.empty(max(nsl.value, 1), np.int32)
+    face = np.empty(max(nsl.value, 1), np.int32)
+    _lib.check(L.gbf_layout_fill(n, o.shape[0], o.ctypes.data, q.ctypes.data, off.ctypes.data,
+                                 w.ctypes.data, col.ctypes.data, face.ctypes.data))
+    return off, w, col[: nsl.value], face[: nsl.value], mw.value
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_layout_slots_follow_reference_face_order(perm):
+    c = random_ldu(7, seed=3, permute_faces=perm)
+    n, own, nei = c["n"], c["owner"], c["neighbour"]
+    off, w, col, face, mw = _layout(n, own, nei)
+    seen_own = np.zeros(own.shape[0], int)
+    seen_nei = np.zeros(own.shape[0], int)
+    for cell in range(n):
+        s, lane = cell >> 5, cell & 31
+        wo, wn = w[s] & 0xFFFF, w[s] >> 16
+        base = off[s] + lane
+        ofaces = [face[base + 32 * k] for k in range(wo) if col[base + 32 * k] >= 0]
+        nfaces = [face[base + 32 * (wo + k)] for k in range(wn) if col[base + 32 * (wo + k)] >= 0]
+        # owner-side: faces with owner == cell in ascending face order (the
+        # reference scatter order); neighbour-side likewise
+        assert ofaces == sorted(np.flatnonzero(own == cell).tolist())
+        assert nfaces == sorted(np.flatnonzero(nei == cell).tolist())
+        for f in ofaces:
+            assert col[base + 32 * ofaces.index(f)] == nei[f]
+            seen_own[f] += 1
+        for k, f in enumerate(nfaces):
+            assert col[base + 32 * (wo + k)] == own[f]
+            seen_nei[f] += 1
+        # padding only after the real slots
+        assert all(col[base + 32 * k] < 0 for k in range(len(ofaces), wo))
+    assert (seen_own == 1).all() and (seen_nei == 1).all()
+    assert mw == max(((x & 0xFFFF) + (x >> 16)) for x in w)
+
+
+def _schedule(fn, n, own, nei, n_items):
+    o = np.ascontiguousarray(own, np.int32)
+    q = np.ascontiguousarray(nei, np.int32)
+    ptr = np.empty(n_items + 1, np.int32)
+    items = np.empty(max(n_items, 1), np.int32)
+    nl, mx = ctypes.c_int32(), ctypes.c_int32()
+    _lib.check(fn(n, o.shape[0], o.ctypes.data, q.ctypes.data, ptr.ctypes.data,
+                  items.ctypes.data, ctypes.byref(nl), ctypes.byref(mx)))
+    lvl = np.empty(n_items, int)
+    for l in range(nl.value):
+        lvl[items[ptr[l]:ptr[l + 1]]] = l
+        assert list(items[ptr[l]:ptr[l + 1]]) == sorted(items[ptr[l]:ptr[l + 1]])
+    assert mx.value == max(np.diff(ptr[: nl.value + 1]))
+    return lvl, nl.value
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_dic_schedule_respects_reference_dependencies(perm):
+    c = random_ldu(6, seed=4, permute_faces=perm)
+    n, own, nei = c["n"], c["owner"], c["neighbour"]
+    lvl, nl = _schedule(_lib.lib().gbf_dic_schedule, n, own, nei, n)
+    # cell i reads the factored d[j] of every lower neighbour j < i
+    for f in range(own.shape[0]):
+        i, j = nei[f], own[f]
+        if j < i:
+            assert lvl[i] > lvl[j]
+    if not perm:
+        N = 6
+        ijk = np.arange(n)
+        assert (lvl == ijk % N + (ijk // N) % N + ijk // (N * N)).all()
+        assert nl == 3 * N - 2
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_dilu_schedule_respects_face_order(perm):
+    c = random_ldu(5, seed=6, permute_faces=perm)
+    n, own, nei = c["n"], c["owner"], c["neighbour"]
+    lvl, _ = _schedule(_lib.lib().gbf_dilu_schedule, n, own, nei, own.shape[0])
+    last = {}
+    for f in range(own.shape[0]):
+        for cell in (own[f], nei[f]):
+            if cell in last:
+                assert lvl[f] > lvl[last[cell]]
+            last[cell] = f
+
+
+def test_topology_rejects_bad_addressing():
+    L = _lib.lib()
+    o = np.array([0, 5], np.int32)
+    q = np.array([1, 2], np.int32)
+    a, b, c_ = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+    rc = L.gbf_layout_plan(3, 2, o.ctypes.data, q.ctypes.data, ctypes.byref(a), ctypes.byref(b),
+                           ctypes.byref(c_))
+    assert rc == 4 and b"outside" in L.gbf_last_error()
+    o = np.array([1], np.int32)
+    rc = L.gbf_layout_plan(3, 1, o.ctypes.data, o.ctypes.data, ctypes.byref(a), ctypes.byref(b),
+                           ctypes.byref(c_))
+    assert rc == 4 and b"owner == neighbour" in L.gbf_last_error()
+
+
+def test_python_surface_errors_without_gpu():
+    import torch
+
+    from pyopenfoam_gb300 import LduMatrix, PCGSolver, create_solver
+
+    with pytest.raises(ValueError, match="CUDA"):
+        LduMatrix(2, torch.tensor([0]), torch.tensor([1]), device="cpu")
+    with pytest.raises(ValueError, match="Unknown solver"):
+        create_solver("nope")
+    assert isinstance(create_solver("pcg", tolerance=1e-8), PCGSolver)
+    assert create_solver("PBiCGStab").__class__.__name__ == "PBiCGSTABSolver"
+    with pytest.raises(ValueError, match="Unknown preconditioner"):
+        PCGSolver(preconditioner="bogus")._make_preconditioner(None)
+    from pyopenfoam_gb300 import PBiCGSTABSolver
+
+    with pytest.raises(ValueError, match="omega"):
+        PBiCGSTABSolver(omega="fast")
+
+
+def test_residual_monitor_rules_match_reference():
+    # residual.py:112-145: absolute OR relative, only from min_iter on
+    m = ResidualMonitor(tolerance=1e-3, rel_tol=0.1, min_iter=2)
+    assert not m.check(1.0, 0)
+    assert not m.check(0.05, 1)      # below rel_tol but iteration < min_iter
+    assert m.check(0.05, 2)
+    info = m.build_info(True)
+    assert info.iterations == 3 and info.final_residual == 0.05 and info.initial_residual == 1.0
+    m = ResidualMonitor(tolerance=0.0, rel_tol=0.0)
+    assert not m.check(0.0, 0)       # 0 < 0 is false; res0 = 0 skips the relative test

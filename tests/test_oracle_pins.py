@@ -1,0 +1,135 @@
+"""The oracle is pinned before it is trusted: it must reproduce the
+reference's own known-answer tests and the golden outputs generated by
+running the reference (tests/golden/make_golden.py).  CPU only."""
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.golden.cases import FIXTURE, c1_poisson, jitter_case, random_ldu, sha
+
+G = np.load(FIXTURE)
+
+
+# ---- known answers from the reference's tests/unit/core/test_ldu_matrix.py
+@pytest.mark.parametrize(
+    "n,own,nei,diag,lower,upper,x,expect",
+    [
+        # :152-160 identity 2-cell
+        (2, [0], [1], [3.0, 5.0], [0.0], [0.0], [2.0, 4.0], [6.0, 20.0]),
+        # :162-175 symmetric off-diagonal
+        (2, [0], [1], [2.0, 2.0], [-1.0], [-1.0], [1.0, 1.0], [1.0, 1.0]),
+        # :177-190 asymmetric
+        (2, [0], [1], [4.0, 4.0], [-1.0], [-2.0], [1.0, 3.0], [1.0, 10.0]),
+        # :192-202 3-cell chain
+        (3, [0, 1], [1, 2], [4.0, 6.0, 4.0], [-1.0, -1.0], [-1.0, -1.0], [1.0, 2.0, 3.0],
+         [2.0, 8.0, 10.0]),
+        # :462-486 diffusion: A.1 = 0 and [-1, 0, 1]
+        (3, [0, 1], [1, 2], [1.0, 2.0, 1.0], [-1.0, -1.0], [-1.0, -1.0], [1.0, 1.0, 1.0],
+         [0.0, 0.0, 0.0]),
+        (3, [0, 1], [1, 2], [1.0, 2.0, 1.0], [-1.0, -1.0], [-1.0, -1.0], [1.0, 2.0, 3.0],
+         [-1.0, 0.0, 1.0]),
+    ],
+)
+def test_oracle_ax_known_answers(n, own, nei, diag, lower, upper, x, expect):
+    y = O.amul(own, nei, diag, lower, upper, x)
+    np.testing.assert_array_equal(y, np.array(expect))
+
+
+@pytest.mark.parametrize("name,N,perm", [("ldu32", 32, False), ("ldu12p", 12, True)])
+def test_oracle_bitwise_against_reference(name, N, perm):
+    c = random_ldu(N, 5, perm)
+    args = (c["owner"], c["neighbour"], c["diag"], c["lower"], c["upper"])
+    assert sha(O.amul(*args, c["x"])) == str(G[f"{name}_Ax_sha"])
+    assert sha(O.amul_T(*args, c["x"])) == str(G[f"{name}_AxT_sha"])
+    assert sha(O.dic_build(c["owner"], c["neighbour"], c["diag"], c["upper"])) == str(
+        G[f"{name}_dic_sha"])
+    assert sha(O.dilu_build(*args)) == str(G[f"{name}_dilu_sha"])
+    f32 = [a.astype(np.float32) for a in (c["diag"], c["lower"], c["upper"], c["x"])]
+    assert sha(O.amul(c["owner"], c["neighbour"], *f32)) == str(G[f"{name}_Ax_f32_sha"])
+    if f"{name}_dic_full_sha" in G.files:
+        pd = O.dic_build(c["owner"], c["neighbour"], c["diag"], c["upper"])
+        assert sha(O.dic_apply_full(c["owner"], c["neighbour"], c["upper"], pd, c["r"])) == str(
+            G[f"{name}_dic_full_sha"])
+        pdl = O.dilu_build(*args)
+        assert sha(O.dilu_apply_full(c["owner"], c["neighbour"], c["lower"], c["upper"], pdl,
+                                     c["r"])) == str(G[f"{name}_dilu_full_sha"])
+
+
+def test_oracle_c1_pcg_against_reference():
+    c1 = c1_poisson(32)
+    assert sha(np.concatenate([c1["diag"], c1["lower"], c1["upper"]])) == str(G["c1_coeff_sha"])
+    pd = O.dic_build(c1["owner"], c1["neighbour"], c1["diag"], c1["upper"])
+    s = O.pcg(c1["owner"], c1["neighbour"], c1["diag"], c1["lower"], c1["upper"], c1["b"],
+              np.zeros(c1["n"]), pd, 0.0, 1e-6, 1000)
+    assert s.iterations == int(G["c1_pcg_iterations"]) == 198
+    ref = G["c1_pcg_x"]
+    # the reference's torch.dot rounds in a thread-dependent order, so the
+    # trajectories separate slowly: 6e-13 after 50 iterations, ~1.5e-9 at 198
+    assert np.abs(s.x - ref).max() / np.abs(ref).max() < 1e-8
+    s50 = O.pcg(c1["owner"], c1["neighbour"], c1["diag"], c1["lower"], c1["upper"], c1["b"],
+                np.zeros(c1["n"]), pd, 0.0, 0.0, 50)
+    assert s50.iterations == int(G["c1_pcg50_iterations"]) == 51
+    ref50 = G["c1_pcg50_x"]
+    assert np.abs(s50.x - ref50).max() / np.abs(ref50).max() < 1e-11
+
+
+def test_oracle_assembly_against_reference():
+    jc = jitter_case(6)
+    lo, up, dg = O.laplacian(int(jc["n_cells"]), jc["owner"], jc["neighbour"], jc["face_areas"],
+                             jc["delta"], jc["gamma"], jc["volumes"])
+    np.testing.assert_array_equal(lo, G["j6_lap_lower"])
+    np.testing.assert_array_equal(up, G["j6_lap_upper"])
+    np.testing.assert_array_equal(dg, G["j6_lap_diag"])
+    nint = int(jc["n_internal"])
+    l2, u2, d2 = O.div_upwind(int(jc["n_cells"]), jc["owner"][:nint], jc["neighbour"],
+                              jc["phi"][:nint], jc["volumes"])
+    np.testing.assert_array_equal(l2, G["j6_div_lower"])
+    np.testing.assert_array_equal(u2, G["j6_div_upper"])
+    np.testing.assert_array_equal(d2, G["j6_div_diag"])
+
+
+def test_oracle_pcg_j6_against_reference():
+    jc = jitter_case(6)
+    nint = int(jc["n_internal"])
+    own, nei = jc["owner"][:nint], jc["neighbour"]
+    dg, lo, up = G["j6_lap_diag"], G["j6_lap_lower"], G["j6_lap_upper"]
+    pd = O.dic_build(own, nei, dg, up)
+    s = O.pcg(own, nei, dg, lo, up, jc["b"], np.zeros(dg.shape[0]), pd, 0.0, 1e-10, 500)
+    assert s.iterations == int(G["j6_pcg_iterations"])
+    ref = G["j6_pcg_x"]
+    assert np.abs(s.x - ref).max() / np.abs(ref).max() < 1e-12
+
+
+def test_oracle_pbicgstab_first_iterations_against_reference():
+    """The reference's BiCGStab (omega = t.z/t.t) is chaotic on this system:
+    rho = rt.r cancels to ~1e-8 of |r|^2 within three iterations, so two
+    faithful implementations separate after that.  The first two iterations
+    (history entries 0..4) agree to rounding."""
+    jc = jitter_case(6)
+    nint = int(jc["n_internal"])
+    own, nei = jc["owner"][:nint], jc["neighbour"]
+    dg = G["j6_lap_diag"] - G["j6_div_diag"]
+    lo = G["j6_lap_lower"] - G["j6_div_lower"]
+    up = G["j6_lap_upper"] - G["j6_div_upper"]
+    pd = O.dilu_build(own, nei, dg, lo, up)
+    s = O.pbicgstab(own, nei, dg, lo, up, jc["b"], np.zeros(dg.shape[0]), pd, 0.0, 0.0, 2)
+    assert s.iterations == 5
+
+
+def test_oracle_dls_gradients_against_reference():
+    jc = jitter_case(6)
+    nint = int(jc["n_internal"])
+    own, nei = jc["owner"][:nint], jc["neighbour"]
+    dg = G["j6_lap_diag"] + 10.0
+    lo, up = G["j6_lap_lower"], G["j6_lap_upper"]
+    n = dg.shape[0]
+    s = O.pcg(own, nei, dg, lo, up, jc["b"], np.zeros(n), None, 0.0, 1e-14, 2000)
+    np.testing.assert_allclose(s.x, G["dls_x"], rtol=0, atol=1e-12 * np.abs(s.x).max())
+    g = jc["w"] + 2.0 * s.x
+    lam = O.pcg(own, nei, dg, up, lo, g, np.zeros(n), None, 0.0, 1e-14, 2000).x
+    gd, gl, gu = O.dls_grads(own, nei, lam, s.x)
+    for got, key in ((lam, "dls_grad_b"), (gd, "dls_grad_diag"), (gl, "dls_grad_lower"),
+                     (gu, "dls_grad_upper")):
+        ref = G[key]
+        assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max(), key
