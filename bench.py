@@ -1,0 +1,442 @@
+#!/usr/bin/env python
+"""Benchmark of the linear-solve hot path on one GB300 (or N replicas).
+
+Workload (the configuration the headline metric is quoted on): the 256^3
+Poisson system on the uniform unit-cube hex mesh (16,777,216 cells,
+50,135,040 internal faces), fixed value on x = 0, zero gradient elsewhere,
+RHS U[-1, 1] (seed 2), solved by PCG + DIC to a 1e-10 relative residual.
+
+One step = one solve from a freshly set matrix: coefficient packing, DIC
+factorisation and the Krylov iterations of the mixed-precision refined PCG
+(FP32 inner iterations, FP64 reliable updates).  ``value`` is seconds per
+solve with the system resident in HBM (inputs of ~1.9 GB are far larger than
+the 129 MB L2, so no flush is needed between steps).  The FP64 PCG solve of
+the same system is timed once beside it for the speed-up.
+
+``e2e`` repeats the step through the public API with HOST buffers: the
+matrix coefficients and RHS are copied from pinned host memory and x is read
+back inside the timed region.
+
+``roofline``: the dominant kernel is the FP32 Amul + p.Ap reduction of the
+inner iteration; its algorithmic bytes per launch are
+B_amul(4) = 3*4*n + 2*4*F + 8*F (diag, x, y; lower, upper; int32 owner and
+neighbour), divided by the launch durations recorded with CUDA events on the
+launching stream during the timed steps.
+
+``--impl reference`` times the reference algorithm on the host cores
+instead: the CPU restatement of the reference's PCG+DIC (the reference is
+pure Python on PyTorch and cannot run here), threaded over all host cores,
+on a bounded sample (DIC factorisation + 20 iterations) extrapolated to the
+iteration count of the full solve.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to 1e-10 rel. residual: mixed-prec refined vs FP64 PCG on GPU; Amul HBM GB/s"
+WORKLOAD = "256^3 Poisson (unit-cube hex, x0 fixed value), PCG+DIC to 1e-10 relative residual"
+# Iterations of FP64 PCG+DIC to 1e-10 on this system, counted like the
+# reference (len(history)); measured with the FP64 GPU solver on GB300 and
+# used only to extrapolate the bounded CPU sample of the reference arm.
+FP64_ITERATIONS_256 = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n", type=int, default=256, help="cells per direction")
+    p.add_argument("--rel-tol", type=float, default=1e-10)
+    p.add_argument("--delta", type=float, default=0.1)
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return p.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+def b_amul(s: int, n: int, F: int) -> int:
+    return 3 * s * n + 2 * s * F + 8 * F
+
+
+def load_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def make_matrix(sysd, dev):
+    from pyopenfoam_gb300 import LduMatrix
+
+    m = LduMatrix(sysd["n"], torch.as_tensor(sysd["owner"]), torch.as_tensor(sysd["neighbour"]),
+                  device=dev)
+    m.diag = torch.as_tensor(sysd["diag"])
+    m.lower = torch.as_tensor(sysd["lower"])
+    m.upper = torch.as_tensor(sysd["upper"])
+    m.topology()
+    return m
+
+
+def true_rel_residual(m, x, b) -> float:
+    r = b - m.Ax(x)
+    return float(torch.linalg.vector_norm(r) / torch.linalg.vector_norm(b))
+
+
+def time_amul(m, dev, reps=20):
+    from pyopenfoam_gb300 import _lib
+
+    n, F = m.n_cells, m.n_internal_faces
+    x = torch.rand(n, dtype=torch.float64, device=dev)
+    topo = m.topology()
+    L = _lib.lib()
+    st = torch.cuda.current_stream(dev)
+    out = {}
+    y64 = torch.empty_like(x)
+    coef64 = m.packed()
+    coef32 = m.packed(dtype=torch.float32)
+    d32, x32 = m.diag.float(), x.float()
+    y32 = torch.empty_like(x32)
+    fns = {
+        "f64": lambda: L.gbf_amul_f64(topo.layout_ref, coef64.data_ptr(), m.diag.data_ptr(),
+                                      x.data_ptr(), y64.data_ptr(), 0, st.cuda_stream),
+        "f32": lambda: L.gbf_amul_f32(topo.layout_ref, coef32.data_ptr(), d32.data_ptr(),
+                                      x32.data_ptr(), y32.data_ptr(), 0, st.cuda_stream),
+    }
+    for name, fn in fns.items():
+        s = 8 if name == "f64" else 4
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"us": ms * 1e3, "GBs": b_amul(s, n, F) / (ms * 1e-3) / 1e9}
+    return out
+
+
+def cpu_sample(sysd, iters=20, threads=None):
+    """Reference algorithm on the host: DIC build + `iters` PCG iterations,
+    threaded over all host cores (oracle restatement of the reference)."""
+    from oracle import oracle as O
+
+    threads = threads or len(os.sched_getaffinity(0))
+    own, nei = sysd["owner"], sysd["neighbour"]
+    t0 = time.perf_counter()
+    pd = O.dic_build(own, nei, sysd["diag"], sysd["upper"])
+    t_dic = time.perf_counter() - t0
+    x0 = np.zeros(sysd["n"])
+    O.pcg(own, nei, sysd["diag"], sysd["lower"], sysd["upper"], sysd["b"], x0, pd, 0.0, 0.0, 2,
+          threads=threads)
+    t0 = time.perf_counter()
+    O.pcg(own, nei, sysd["diag"], sysd["lower"], sysd["upper"], sysd["b"], x0, pd, 0.0, 0.0,
+          iters, threads=threads)
+    t_it = (time.perf_counter() - t0) / iters
+    return t_dic, t_it, threads
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+# --------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    from pyopenfoam_gb300.mesh.poisson import hex_poisson
+
+    if rank != 0:
+        return
+    sysd = hex_poisson(args.n, seed=2)
+    iters_full = FP64_ITERATIONS_256 if args.n == 256 and FP64_ITERATIONS_256 else None
+    samples = []
+    for i in range(args.warmup + args.steps):
+        t_dic, t_it, threads = cpu_sample(sysd, iters=20)
+        if i >= args.warmup:
+            samples.append((t_dic, t_it))
+    t_dic = statistics.median(s[0] for s in samples)
+    t_it = statistics.median(s[1] for s in samples)
+    n_it = iters_full or 1
+    value = t_dic + t_it * n_it
+    sample = (f"DIC factorisation + 20 PCG iterations of the {args.n}^3 system per step, "
+              f"extrapolated to {n_it} iterations" + ("" if iters_full else " (count unknown: 1)"))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD.replace("256^3", f"{args.n}^3"), "n_cells": sysd["n"],
+                   "n_faces": int(sysd["owner"].shape[0]), "rel_tol": args.rel_tol,
+                   "rhs_seed": 2},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                         "sample": sample, "cpu": cpu_model(), "dic_build_s": t_dic,
+                         "s_per_iteration": t_it},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    from pyopenfoam_gb300 import MixedPrecisionPCGSolver, PCGSolver, _lib
+    from pyopenfoam_gb300.mesh.poisson import hex_poisson
+
+    dev = torch.device("cuda", local)
+    sysd = hex_poisson(args.n, seed=2)
+    n, F = sysd["n"], int(sysd["owner"].shape[0])
+    m = make_matrix(sysd, dev)
+    b = torch.as_tensor(sysd["b"]).to(dev)
+    x0 = torch.zeros(n, dtype=torch.float64, device=dev)
+    L = _lib.lib()
+    extra = {}
+
+    mixed = MixedPrecisionPCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
+                                    preconditioner="DIC", delta=args.delta)
+
+    def step():
+        m.invalidate_cache()  # re-pack + re-factorise each solve, like the reference
+        return mixed(m, b, x0)
+
+    # --- FP64 comparison (same system, same API) ---
+    x64 = None
+    if not args.no_fp64:
+        fp64 = PCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
+                         preconditioner="DIC")
+        m.invalidate_cache()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x64, it64, res64 = fp64(m, b, x0)
+        torch.cuda.synchronize()
+        extra["fp64_pcg_s"] = time.perf_counter() - t0
+        extra["fp64_iterations"] = it64
+        extra["fp64_true_rel_residual"] = true_rel_residual(m, x64, b)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    L.gbf_timing_enable(1, 100000)
+    launches = 0
+    iters = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            x, it, res = step()
+            r = mixed.last_result
+            iters.append(it)
+            launches += r.launches
+        e1.record()
+        torch.cuda.synchronize()
+    ms_total = e0.elapsed_time(e1)
+    import ctypes
+
+    cnt, tot = ctypes.c_int32(), ctypes.c_double()
+    _lib.check(L.gbf_timing_read(1, ctypes.byref(cnt), ctypes.byref(tot)))
+    L.gbf_timing_enable(0, 0)
+    # launches outside the solver loop: pack f64 + pack f32 + DIC levels + clamp
+    dic_levels = m.topology().dic_schedule().n_levels
+    launches += args.steps * (2 + dic_levels + 1)
+    sec = max_over_ranks(ms_total / 1e3 / args.steps, world)
+    barrier(world)
+
+    peaks = load_peaks()
+    avg_ms = tot.value / max(cnt.value, 1)
+    achieved = b_amul(4, n, F) / (avg_ms * 1e-3) / 1e9
+    extra["iterations"] = iters[-1]
+    extra["outer_updates"] = mixed.last_result.outer_updates
+    extra["true_rel_residual"] = true_rel_residual(m, x, b)
+    if x64 is not None:
+        extra["x_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(x - x64) /
+                                           torch.linalg.vector_norm(x64))
+        extra["speedup_vs_fp64"] = extra["fp64_pcg_s"] / sec
+    extra["amul"] = time_amul(m, dev)
+
+    # --- end to end through the public API with host buffers ---
+    host = {k: torch.as_tensor(sysd[k]).pin_memory() for k in ("diag", "lower", "upper", "b")}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = n * 8
+    xs_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.diag = host["diag"].to(dev, non_blocking=True)
+        m.lower = host["lower"].to(dev, non_blocking=True)
+        m.upper = host["upper"].to(dev, non_blocking=True)
+        bb = host["b"].to(dev, non_blocking=True)
+        xe, _, _ = mixed(m, bb, x0)
+        xs_host.copy_(xe, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e = max_over_ranks(statistics.mean(e2e_times), world)
+
+    cpu = None
+    if rank == 0 and world >= 1 and not args.no_cpu:
+        t_dic, t_it, threads = cpu_sample(sysd, iters=20)
+        n_it = extra.get("fp64_iterations") or iters[-1]
+        cpu = {"value": t_dic + t_it * n_it, "unit": "s", "cores": threads, "kind": "port",
+               "sample": (f"oracle restatement of the reference PCG+DIC: DIC factorisation + "
+                          f"20 threaded iterations at {args.n}^3, extrapolated to {n_it} "
+                          f"iterations"),
+               "cpu": cpu_model(), "dic_build_s": t_dic, "s_per_iteration": t_it}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("256^3", f"{args.n}^3"), "n_cells": n,
+                       "n_faces": F, "rel_tol": args.rel_tol, "rhs_seed": 2,
+                       "solver": f"mixed FP32/FP64 reliable-update PCG+DIC, delta={args.delta}",
+                       "l2": "no flush: resident inputs (~1.9 GB) exceed the 129 MB L2",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "mp_ap_kernel (FP32 Amul + p.Ap)",
+                         "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                         "traffic": None, "bytes_per_launch": b_amul(4, n, F),
+                         "timed_launches": cnt.value, "avg_launch_us": avg_ms * 1e3},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "extra": extra,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

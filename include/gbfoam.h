@@ -70,6 +70,15 @@ const char* gbf_last_error(void);
 int gbf_version(void);
 /* Number of SMs of the current device (grid sizing of the reductions).     */
 int gbf_device_sm_count(int32_t* n_sm);
+/* Kernel timing probes (no reference counterpart; used by the benchmark to
+ * time the dominant kernel inside a solve).  While enabled, the solvers
+ * bracket the launches of their Amul kernels with CUDA events on the
+ * launching stream; gbf_timing_read synchronises and returns, per probe,
+ * the number of timed launches and their summed duration in ms.
+ * Probe ids: 0 = FP64 PCG Amul+dot, 1 = mixed PCG FP32 Amul+dot,
+ * 2 = PBiCGStab Amul+dot (v and t), 3 = mixed PCG FP64 true residual.     */
+int gbf_timing_enable(int32_t enable, int32_t max_events_per_probe);
+int gbf_timing_read(int32_t probe, int32_t* launches, double* total_ms);
 
 /* ---- topology (host, once per mesh) -------------------------------------
  * Replace the reference's per-call Python loops over faces
@@ -165,6 +174,8 @@ typedef struct gbf_solve_result {
   double initial_residual;
   int32_t inner_iterations;/* mixed solver: low-precision iterations        */
   int32_t outer_updates;   /* mixed solver: FP64 residual replacements      */
+  int32_t launches;        /* kernels launched by this call                 */
+  int32_t reserved;
 } gbf_solve_result;
 
 size_t gbf_pcg_workspace_bytes(int32_t n_cells);
@@ -184,6 +195,24 @@ int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* slot_coef, const 
                             const double* precond_d, const double* b, double* x,
                             double* history, const gbf_solve_params* P, gbf_solve_result* R,
                             void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- mixed precision -------------------------------------------------------
+ * No reference counterpart (the north-star's precision pattern): PCG whose
+ * Krylov recurrence, Amul (coef32 = FP32 packing of the FP64 matrix) and
+ * diagonal preconditioner run in FP32, with FP64 reliable updates: when the
+ * FP32 residual has dropped by `delta` (0 < delta < 1) since the last update
+ * or below max(tolerance, rel_tol*|r0|), the FP32 correction is folded into
+ * the FP64 x and the residual is replaced by the true b - A64 x (bitwise
+ * reference-order FP64 Amul).  Convergence is declared on true residuals
+ * only.  precond_d = FP64 factorised DIC/DILU diagonal or NULL.  history
+ * receives |r0| and the true |r| of every update (hist_cap entries max).
+ * R->iterations = inner iterations + 1, R->outer_updates = FP64 updates.  */
+size_t gbf_mixed_pcg_workspace_bytes(int32_t n_cells);
+int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double* diag64,
+                        const float* coef32, const double* precond_d, const double* b,
+                        double* x, double delta, double* history, int32_t hist_cap,
+                        const gbf_solve_params* P, gbf_solve_result* R, void* workspace,
+                        size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -76,6 +76,8 @@ class SolveResult(ctypes.Structure):
         ("initial_residual", _c_dbl),
         ("inner_iterations", _c_i32),
         ("outer_updates", _c_i32),
+        ("launches", _c_i32),
+        ("reserved", _c_i32),
     ]
 
 
@@ -87,6 +89,8 @@ EXPORTED: dict[str, tuple] = {
     "gbf_last_error": (ctypes.c_char_p, []),
     "gbf_version": (ctypes.c_int, []),
     "gbf_device_sm_count": (ctypes.c_int, [_P(_c_i32)]),
+    "gbf_timing_enable": (ctypes.c_int, [_c_i32, _c_i32]),
+    "gbf_timing_read": (ctypes.c_int, [_c_i32, _P(_c_i32), _P(_c_dbl)]),
     "gbf_layout_plan": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _P(_c_i32), _P(_c_i64), _P(_c_i32)]),
     "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
@@ -103,6 +107,10 @@ EXPORTED: dict[str, tuple] = {
     "gbf_pcg_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_pcg_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                          _P(SolveParams), _P(SolveResult), _c_vp, _c_size, _c_vp]),
+    "gbf_mixed_pcg_workspace_bytes": (_c_size, [_c_i32]),
+    "gbf_mixed_pcg_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl,
+                                           _c_vp, _c_i32, _P(SolveParams), _P(SolveResult),
+                                           _c_vp, _c_size, _c_vp]),
     "gbf_pbicgstab_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_pbicgstab_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                                _P(SolveParams), _P(SolveResult), _c_vp, _c_size,

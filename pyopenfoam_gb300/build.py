@@ -21,12 +21,13 @@ BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libgbfoam.so")
 
 SOURCES = [
-    "capi.cpp",
+    "capi.cu",
     "topology.cpp",
     "amul.cu",
     "precond.cu",
     "pcg.cu",
     "pbicgstab.cu",
+    "mixed.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

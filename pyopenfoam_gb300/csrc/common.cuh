@@ -40,6 +40,13 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 constexpr int kBlock = 256;
 
 int check_layout(const gbf_layout* L);  // validates sizes / pointers
+
+// Kernel timing probes (gbf_timing_enable): timing_begin returns true when
+// an event was recorded; the caller then calls timing_end after the launch.
+constexpr int kNumProbes = 4;
+enum { kProbePcgAp = 0, kProbeMixedAp = 1, kProbeBicgAmul = 2, kProbeMixedTrue = 3 };
+bool timing_begin(int probe, cudaStream_t s);
+void timing_end(int probe, cudaStream_t s);
 int reduction_grid();  // fixed grid of the reducing kernels (SMs x 8, <= kMaxGrid)
 constexpr int kMaxGrid = 4096;
 

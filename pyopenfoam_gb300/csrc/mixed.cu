@@ -1,0 +1,334 @@
+// Mixed-precision PCG: FP32 inner iterations with FP64 reliable updates.
+//
+// No reference counterpart: this is the precision pattern of the north-star
+// (FP32 Amul / preconditioner / vectors, FP64 outer residual r = b - A x,
+// FP64 solution update and FP64 dot-product reductions).  It follows the
+// reliable-update scheme of Sleijpen & van der Vorst ("Reliable updated
+// residuals in hybrid Bi-CG methods", Computing 56, 1996), in the mixed
+// precision form of Clark et al. (2010): the Krylov recurrence runs in
+// FP32; whenever the iterated residual has dropped by `delta` since the last
+// update (or below the target), the FP32 correction is folded into the FP64
+// solution and the FP32 residual is replaced by the true FP64 residual
+// b - A x.  The search direction p is kept, so -- unlike restarted defect
+// correction -- no Krylov information is lost.  Convergence is only ever
+// declared on a true FP64 residual.
+//
+// Per inner iteration (four launches; K_true returns at once unless an
+// update is due):
+//   K_ap   : Ap = A32 p, p.Ap                       -> alpha
+//   K_upd  : x32 += alpha p (or fold x64 += x32 + alpha p, x32 = 0),
+//            r -= alpha Ap, z = rD r, r.r, r.z      -> beta, update decision
+//   K_true : r64 = b - A64 x64 (reference-order Amul), r = (float) r64,
+//            z = rD r, |r64|, r.z                   -> convergence, beta
+//   K_p    : p = z + beta p
+// Dot products of FP32 vectors accumulate exact FP32 products in FP64.
+#include <math.h>
+#include <string.h>
+
+#include "amul.cuh"
+
+namespace gbf {
+
+enum { MP_NORMAL = 0, MP_TRUE_RESIDUAL = 1 };
+
+struct MixedState {
+  double rz, alpha, beta, res0, res, rmax, target, pAp;
+  int inner, status, n_hist, phase, fold_pending, updates, pad0, pad1;
+  unsigned int ticket[8];
+};
+
+struct MixedVecs {
+  float *r, *z, *p, *Ap, *xlo, *rD, *d32;
+  double* partials;
+  MixedState* st;
+};
+
+__device__ __forceinline__ double dprod(float a, float b) { return (double)a * (double)b; }
+
+// r64 = b - A64 x64 for cell c; writes r, z; returns r64.
+__device__ __forceinline__ double true_residual_cell(const gbf_layout& L,
+                                                     const double* __restrict__ coef64,
+                                                     const double* __restrict__ diag64,
+                                                     const double* __restrict__ b,
+                                                     const double* __restrict__ x, int c) {
+  const double y = cell_amul<double, double, false>(L, coef64, diag64, x, c, __ldg(x + c));
+  return __dsub_rn(__ldg(b + c), y);
+}
+
+__global__ void __launch_bounds__(kBlock)
+    mp_init_kernel(gbf_layout L, const double* __restrict__ coef64,
+                   const double* __restrict__ diag64, const double* __restrict__ pd,
+                   const double* __restrict__ b, const double* __restrict__ x, MixedVecs v,
+                   double* hist, gbf_solve_params P) {
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x;
+  double rr = 0.0, rz = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
+    const double rh = true_residual_cell(L, coef64, diag64, b, x, c);
+    const float rD = pd ? (float)(1.0 / __ldg(pd + c)) : 1.0f;
+    const float r = (float)rh;
+    const float z = rD * r;
+    v.rD[c] = rD;
+    v.d32[c] = (float)__ldg(diag64 + c);
+    v.r[c] = r;
+    v.z[c] = z;
+    v.p[c] = z;
+    v.xlo[c] = 0.0f;
+    rr = fma(rh, rh, rr);
+    rz += dprod(r, z);
+  }
+  rr = block_sum(rr, sh);
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) {
+    v.partials[blockIdx.x] = rr;
+    v.partials[G + blockIdx.x] = rz;
+  }
+  if (last_block_done(&v.st->ticket[0])) {
+    const double trr = reduce_partials(v.partials, G, sh);
+    const double trz = reduce_partials(v.partials + G, G, sh);
+    if (threadIdx.x == 0) {
+      MixedState* st = v.st;
+      const double res = sqrt(trr);
+      hist[0] = res;
+      st->n_hist = 1;
+      st->res0 = res;
+      st->res = res;
+      st->rmax = res;
+      st->rz = trz;
+      st->inner = 0;
+      st->target = fmax(P.tolerance, P.rel_tol * res);
+      const bool conv = (0 >= P.min_iter) &&
+                        (res < P.tolerance || (res > 0.0 && res / res < P.rel_tol));
+      st->status = conv ? GBF_CONVERGED : (P.max_iter < 1 ? GBF_MAX_ITER : GBF_RUNNING);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    mp_ap_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v) {
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x;
+  double acc = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
+    const float pc = __ldg(v.p + c);
+    const float y = cell_amul<float, float, false>(L, coef32, v.d32, v.p, c, pc);
+    v.Ap[c] = y;
+    acc += dprod(pc, y);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) v.partials[blockIdx.x] = acc;
+  if (last_block_done(&v.st->ticket[1])) {
+    const double pAp = reduce_partials(v.partials, G, sh);
+    if (threadIdx.x == 0) {
+      MixedState* st = v.st;
+      st->pAp = pAp;
+      if (fabs(pAp) < 1e-30)
+        st->status = GBF_BREAKDOWN;
+      else
+        st->alpha = st->rz / pAp;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    mp_update_kernel(int n, double* __restrict__ x, MixedVecs v, double delta,
+                     gbf_solve_params P) {
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x;
+  const float alpha = (float)v.st->alpha;
+  const bool fold = v.st->fold_pending != 0;
+  double rr = 0.0, rz = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += G * blockDim.x) {
+    const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
+    if (fold) {
+      x[c] += (double)xl;
+      v.xlo[c] = 0.0f;
+    } else {
+      v.xlo[c] = xl;
+    }
+    const float r = fmaf(-alpha, v.Ap[c], v.r[c]);
+    const float z = __ldg(v.rD + c) * r;
+    v.r[c] = r;
+    v.z[c] = z;
+    rr += dprod(r, r);
+    rz += dprod(r, z);
+  }
+  rr = block_sum(rr, sh);
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) {
+    v.partials[blockIdx.x] = rr;
+    v.partials[G + blockIdx.x] = rz;
+  }
+  if (last_block_done(&v.st->ticket[2])) {
+    const double trr = reduce_partials(v.partials, G, sh);
+    const double trz = reduce_partials(v.partials + G, G, sh);
+    if (threadIdx.x == 0) {
+      MixedState* st = v.st;
+      st->inner += 1;
+      const double res = sqrt(trr);
+      st->res = res;
+      if (fold) {
+        st->fold_pending = 0;
+        st->phase = MP_TRUE_RESIDUAL;  // K_true replaces r and sets beta
+      } else {
+        st->beta = trz / st->rz;
+        st->rz = trz;
+        st->rmax = fmax(st->rmax, res);
+        if (res < delta * st->rmax || res < st->target || st->inner >= P.max_iter)
+          st->fold_pending = 1;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    mp_true_kernel(gbf_layout L, const double* __restrict__ coef64,
+                   const double* __restrict__ diag64, const double* __restrict__ b,
+                   const double* __restrict__ x, MixedVecs v, double* hist, int hist_cap,
+                   gbf_solve_params P) {
+  if (v.st->status != GBF_RUNNING || v.st->phase != MP_TRUE_RESIDUAL) return;
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x;
+  double rr = 0.0, rz = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
+    const double rh = true_residual_cell(L, coef64, diag64, b, x, c);
+    const float r = (float)rh;
+    const float z = __ldg(v.rD + c) * r;
+    v.r[c] = r;
+    v.z[c] = z;
+    rr = fma(rh, rh, rr);
+    rz += dprod(r, z);
+  }
+  rr = block_sum(rr, sh);
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) {
+    v.partials[blockIdx.x] = rr;
+    v.partials[G + blockIdx.x] = rz;
+  }
+  if (last_block_done(&v.st->ticket[3])) {
+    const double trr = reduce_partials(v.partials, G, sh);
+    const double trz = reduce_partials(v.partials + G, G, sh);
+    if (threadIdx.x == 0) {
+      MixedState* st = v.st;
+      const double res = sqrt(trr);
+      st->res = res;
+      st->updates += 1;
+      if (st->n_hist < hist_cap) hist[st->n_hist] = res;
+      st->n_hist += 1;
+      st->phase = MP_NORMAL;
+      const bool conv = st->inner >= P.min_iter &&
+                        (res < P.tolerance || (st->res0 > 0.0 && res / st->res0 < P.rel_tol));
+      if (conv) {
+        st->status = GBF_CONVERGED;
+      } else if (st->inner >= P.max_iter) {
+        st->status = GBF_MAX_ITER;
+      } else {
+        st->beta = trz / st->rz;
+        st->rz = trz;
+        st->rmax = res;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) mp_p_kernel(int n, MixedVecs v) {
+  if (v.st->status != GBF_RUNNING) return;
+  const float beta = (float)v.st->beta;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+    v.p[c] = fmaf(beta, v.p[c], v.z[c]);
+}
+
+// Folds any remaining FP32 correction into x (breakdown / iteration limit;
+// after convergence x32 is already zero).
+__global__ void mp_fold_kernel(int n, double* __restrict__ x, MixedVecs v) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const float xl = v.xlo[c];
+    if (xl != 0.0f) x[c] += (double)xl;
+    v.xlo[c] = 0.0f;
+  }
+}
+
+static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace gbf
+
+using namespace gbf;
+
+extern "C" size_t gbf_mixed_pcg_workspace_bytes(int32_t n) {
+  if (n < 0) return 0;
+  return 7 * a256(sizeof(float) * (size_t)n) + a256(sizeof(double) * 2 * kMaxGrid) +
+         a256(sizeof(MixedState));
+}
+
+extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
+                                   const double* diag64, const float* coef32,
+                                   const double* pd, const double* b, double* x, double delta,
+                                   double* hist, int32_t hist_cap, const gbf_solve_params* P,
+                                   gbf_solve_result* R, void* ws, size_t ws_bytes,
+                                   void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  GBF_REQUIRE(P && R, "mixed_pcg: NULL params/result");
+  GBF_REQUIRE(P->max_iter >= 0, "mixed_pcg: negative max_iter");
+  GBF_REQUIRE(delta > 0.0 && delta < 1.0, "mixed_pcg: delta must be in (0, 1), got %g", delta);
+  const int n = L->n_cells;
+  memset(R, 0, sizeof(*R));
+  if (n == 0) {
+    const bool conv = (0 >= P->min_iter) && (0.0 < P->tolerance);
+    R->iterations = 1;
+    R->status = conv ? GBF_CONVERGED : (P->max_iter < 1 ? GBF_MAX_ITER : GBF_BREAKDOWN);
+    return GBF_OK;
+  }
+  GBF_REQUIRE(diag64 && b && x && hist && hist_cap >= 1 && ws &&
+                  (L->n_faces == 0 || (coef64 && coef32)),
+              "mixed_pcg: NULL pointer");
+  GBF_REQUIRE(ws_bytes >= gbf_mixed_pcg_workspace_bytes(n), "mixed_pcg: workspace too small");
+  cudaStream_t s = as_stream(stream);
+  char* w = static_cast<char*>(ws);
+  const size_t vb = a256(sizeof(float) * (size_t)n);
+  MixedVecs v;
+  float** vecs[7] = {&v.r, &v.z, &v.p, &v.Ap, &v.xlo, &v.rD, &v.d32};
+  for (int i = 0; i < 7; ++i) *vecs[i] = reinterpret_cast<float*>(w + i * vb);
+  v.partials = reinterpret_cast<double*>(w + 7 * vb);
+  v.st = reinterpret_cast<MixedState*>(w + 7 * vb + a256(sizeof(double) * 2 * kMaxGrid));
+
+  int G = reduction_grid();
+  const int need = (n + kBlock - 1) / kBlock;
+  if (G > need) G = need;
+  GBF_CHECK_CUDA(cudaMemsetAsync(v.st, 0, sizeof(MixedState), s));
+  mp_init_kernel<<<G, kBlock, 0, s>>>(*L, coef64, diag64, pd, b, x, v, hist, *P);
+  GBF_CHECK_LAUNCH();
+  const int chunk = P->check_every > 0 ? P->check_every : 32;
+  MixedState hs;
+  GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+  // bounded: every launched iteration advances `inner` until max_iter, where
+  // a fold + true residual ends the solve (at most max_iter + 2 iterations)
+  int launched = 0;
+  const int limit = P->max_iter + 2;
+  while (hs.status == GBF_RUNNING && launched < limit) {
+    for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
+      const bool tb = timing_begin(kProbeMixedAp, s);
+      mp_ap_kernel<<<G, kBlock, 0, s>>>(*L, coef32, v);
+      if (tb) timing_end(kProbeMixedAp, s);
+      mp_update_kernel<<<G, kBlock, 0, s>>>(n, x, v, delta, *P);
+      mp_true_kernel<<<G, kBlock, 0, s>>>(*L, coef64, diag64, b, x, v, hist, hist_cap, *P);
+      mp_p_kernel<<<G, kBlock, 0, s>>>(n, v);
+    }
+    GBF_CHECK_LAUNCH();
+    GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+  }
+  mp_fold_kernel<<<G, kBlock, 0, s>>>(n, x, v);
+  GBF_CHECK_LAUNCH();
+  R->iterations = hs.inner + 1;
+  R->status = (hs.status == GBF_RUNNING) ? GBF_MAX_ITER : hs.status;
+  R->final_residual = hs.res;
+  R->initial_residual = hs.res0;
+  R->inner_iterations = hs.inner;
+  R->outer_updates = hs.updates;
+  R->launches = 2 + 4 * launched;
+  return GBF_OK;
+}

@@ -314,7 +314,9 @@ extern "C" int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* coef,
   int launched = 0;
   while (hs.status == GBF_RUNNING && launched < P->max_iter) {
     for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
+      const bool tb = timing_begin(kProbeBicgAmul, s);
       bicg_v_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      if (tb) timing_end(kProbeBicgAmul, s);
       if (pd)
         bicg_s_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
       else
@@ -334,5 +336,6 @@ extern "C" int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* coef,
   R->status = (hs.status == GBF_RUNNING) ? GBF_MAX_ITER : hs.status;
   R->final_residual = hs.res;
   R->initial_residual = hs.res0;
+  R->launches = 1 + 5 * launched;
   return GBF_OK;
 }

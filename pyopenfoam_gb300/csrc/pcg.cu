@@ -232,7 +232,9 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
   int launched = 0;
   while (hs.status == GBF_RUNNING && launched < P->max_iter) {
     for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
+      const bool tb = timing_begin(kProbePcgAp, s);
       pcg_ap_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      if (tb) timing_end(kProbePcgAp, s);
       if (pd)
         pcg_update_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
       else
@@ -247,5 +249,6 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
   R->status = (hs.status == GBF_RUNNING) ? GBF_MAX_ITER : hs.status;
   R->final_residual = hs.res;
   R->initial_residual = hs.res0;
+  R->launches = 1 + 3 * launched;
   return GBF_OK;
 }

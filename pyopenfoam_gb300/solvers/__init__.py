@@ -1,6 +1,7 @@
 """GPU linear solvers with the reference's ``pyfoam.solvers`` interface."""
 
 from .linear_solver import LinearSolverBase, create_solver, register_solver, solver_from_dict
+from .mixed import MixedPrecisionPCGSolver
 from .pbicgstab import PBiCGSTABSolver
 from .pcg import PCGSolver
 from .preconditioners import DICPreconditioner, DILUPreconditioner, Preconditioner
@@ -8,6 +9,6 @@ from .residual import ConvergenceInfo, ResidualMonitor
 
 __all__ = [
     "LinearSolverBase", "create_solver", "solver_from_dict", "register_solver", "PCGSolver",
-    "PBiCGSTABSolver", "DICPreconditioner", "DILUPreconditioner", "Preconditioner",
+    "PBiCGSTABSolver", "MixedPrecisionPCGSolver", "DICPreconditioner", "DILUPreconditioner", "Preconditioner",
     "ConvergenceInfo", "ResidualMonitor",
 ]

@@ -71,11 +71,13 @@ _SOLVER_REGISTRY: dict[str, type[LinearSolverBase]] = {}
 def _register_defaults() -> None:
     if _SOLVER_REGISTRY:
         return
+    from .mixed import MixedPrecisionPCGSolver
     from .pbicgstab import PBiCGSTABSolver
     from .pcg import PCGSolver
 
     _SOLVER_REGISTRY["PCG"] = PCGSolver
     _SOLVER_REGISTRY["PBICGSTAB"] = PBiCGSTABSolver
+    _SOLVER_REGISTRY["MIXEDPCG"] = MixedPrecisionPCGSolver
 
 
 def register_solver(name: str, cls: type[LinearSolverBase]) -> None:

@@ -11,9 +11,12 @@ from __future__ import annotations
 
 import hashlib
 import os
+import sys
 from types import SimpleNamespace
 
 import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "reference_outputs.npz")
@@ -28,19 +31,7 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype=dt).tobytes()).hexdigest()
 
 
-def hex_faces(nx: int, ny: int | None = None, nz: int | None = None):
-    """Internal faces of an nx*ny*nz hex mesh in upper-triangular cell order
-    (per cell +x, +y, +z): owner < neighbour, sorted by owner."""
-    ny = nx if ny is None else ny
-    nz = nx if nz is None else nz
-    n = nx * ny * nz
-    c = np.arange(n, dtype=np.int64)
-    i, j, k = c % nx, (c // nx) % ny, c // (nx * ny)
-    has = np.stack([i < nx - 1, j < ny - 1, k < nz - 1], axis=1)
-    flat = np.flatnonzero(has.ravel())
-    cell, d = flat // 3, flat % 3
-    step = np.array([1, nx, nx * ny], dtype=np.int64)
-    return n, cell, cell + step[d]
+from pyopenfoam_gb300.mesh.poisson import hex_faces, hex_poisson  # noqa: E402
 
 
 def random_ldu(N: int, seed: int = 5, permute_faces: bool = False) -> dict:
@@ -65,22 +56,8 @@ def random_ldu(N: int, seed: int = 5, permute_faces: bool = False) -> dict:
 
 
 def c1_poisson(N: int = 32, seed: int = 0) -> dict:
-    """Config-1 system: N^3 uniform hex mesh of the unit cube, unit
-    diffusivity, fvm.laplacian per unit volume (face coefficient
-    |S| delta / V = N^2), Dirichlet on x = 0 (boundary coefficient 2 N^2),
-    zero gradient elsewhere; RHS U[-1, 1] from ``default_rng(seed)``.
-    All coefficients are exact in binary floating point."""
-    n, own, nei = hex_faces(N)
-    c = np.arange(n)
-    i = c % N
-    F = own.shape[0]
-    coeff = float(N * N)
-    lower = np.full(F, -coeff)
-    upper = np.full(F, -coeff)
-    cnt = np.bincount(own, minlength=n) + np.bincount(nei, minlength=n)
-    diag = cnt.astype(np.float64) * coeff + np.where(i == 0, 2.0 * coeff, 0.0)
-    b = np.random.default_rng(seed).uniform(-1.0, 1.0, n)
-    return dict(n=n, owner=own, neighbour=nei, lower=lower, upper=upper, diag=diag, b=b)
+    """Config-1 system (see pyopenfoam_gb300.mesh.poisson.hex_poisson)."""
+    return hex_poisson(N, seed)
 
 
 def mesh_from_arrays(d: dict, device="cpu", dtype=None):
