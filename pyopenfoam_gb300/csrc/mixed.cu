@@ -21,7 +21,12 @@
 //   K_true : r64 = b - A64 x64 (reference-order Amul), r = (float) r64,
 //            z = rD r, |r64|, r.z                   -> convergence, beta
 //   K_p    : p = z + beta p
-// Dot products of FP32 vectors accumulate exact FP32 products in FP64.
+// Dot products of FP32 vectors are accumulated per thread in double-float
+// arithmetic on the FP32 pipes -- each product split exactly into p + e with
+// a fused multiply-add (Dekker's TwoProduct), summed with Knuth's TwoSum --
+// and the per-thread (hi, lo) pairs are combined in FP64.  This keeps ~48
+// significant bits without issuing FP64 instructions per element (GB300's
+// FP64 rate is a small fraction of its FP32 rate).
 #include <math.h>
 #include <string.h>
 
@@ -44,6 +49,23 @@ struct MixedVecs {
 };
 
 __device__ __forceinline__ double dprod(float a, float b) { return (double)a * (double)b; }
+
+// Double-float accumulator: hi + lo carries the running sum of exact FP32
+// products.  Every operation is an explicitly rounded intrinsic so that the
+// compiler cannot contract or reassociate the error-free transformations.
+struct DFAcc {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);  // a*b - p exactly (TwoProduct)
+    const float s = __fadd_rn(hi, p);     // TwoSum(hi, p)
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 // r64 = b - A64 x64 for cell c; writes r, z; returns r64.
 __device__ __forceinline__ double true_residual_cell(const gbf_layout& L,
@@ -109,14 +131,14 @@ __global__ void __launch_bounds__(kBlock)
   if (v.st->status != GBF_RUNNING) return;
   __shared__ double sh[kBlock / 32];
   const int G = gridDim.x;
-  double acc = 0.0;
+  DFAcc a;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
     const float pc = __ldg(v.p + c);
     const float y = cell_amul<float, float, false>(L, coef32, v.d32, v.p, c, pc);
     v.Ap[c] = y;
-    acc += dprod(pc, y);
+    a.add_prod(pc, y);
   }
-  acc = block_sum(acc, sh);
+  const double acc = block_sum(a.value(), sh);
   if (threadIdx.x == 0) v.partials[blockIdx.x] = acc;
   if (last_block_done(&v.st->ticket[1])) {
     const double pAp = reduce_partials(v.partials, G, sh);
@@ -139,7 +161,7 @@ __global__ void __launch_bounds__(kBlock)
   const int G = gridDim.x;
   const float alpha = (float)v.st->alpha;
   const bool fold = v.st->fold_pending != 0;
-  double rr = 0.0, rz = 0.0;
+  DFAcc arr, arz;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += G * blockDim.x) {
     const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
     if (fold) {
@@ -152,11 +174,11 @@ __global__ void __launch_bounds__(kBlock)
     const float z = __ldg(v.rD + c) * r;
     v.r[c] = r;
     v.z[c] = z;
-    rr += dprod(r, r);
-    rz += dprod(r, z);
+    arr.add_prod(r, r);
+    arz.add_prod(r, z);
   }
-  rr = block_sum(rr, sh);
-  rz = block_sum(rz, sh);
+  const double rr = block_sum(arr.value(), sh);
+  const double rz = block_sum(arz.value(), sh);
   if (threadIdx.x == 0) {
     v.partials[blockIdx.x] = rr;
     v.partials[G + blockIdx.x] = rz;
