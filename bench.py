@@ -52,7 +52,7 @@ WORKLOAD = "256^3 Poisson (unit-cube hex, x0 fixed value), PCG+DIC to 1e-10 rela
 # Iterations of FP64 PCG+DIC to 1e-10 on this system, counted like the
 # reference (len(history)); measured with the FP64 GPU solver on GB300 and
 # used only to extrapolate the bounded CPU sample of the reference arm.
-FP64_ITERATIONS_256 = None
+FP64_ITERATIONS_256 = 1991
 
 
 def parse():
