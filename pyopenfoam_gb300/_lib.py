@@ -107,6 +107,8 @@ EXPORTED: dict[str, tuple] = {
     "gbf_pcg_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_pcg_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                          _P(SolveParams), _P(SolveResult), _c_vp, _c_size, _c_vp]),
+    "gbf_pcg_solve_f64_noalloc": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                 _P(SolveParams), _P(SolveResult), _c_vp]),
     "gbf_mixed_pcg_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_mixed_pcg_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl,
                                            _c_vp, _c_i32, _P(SolveParams), _P(SolveResult),

@@ -252,3 +252,140 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
   R->launches = 1 + 3 * launched;
   return GBF_OK;
 }
+
+// ---------------------------------------------------------------------------
+// gbf_pcg_solve_f64_noalloc: the FP64 PCG solve without a caller workspace.
+//
+// Who needs it: callers that cannot allocate device memory at the moment they
+// solve.  Examples are code that records its work into a CUDA stream capture
+// (cudaMalloc and cudaFree are not allowed there, and cudaFree synchronises
+// the whole device), real-time or embedded time loops that must never wait
+// on the allocator or handle an out-of-memory error mid-step, and host
+// programs that run under a fixed device-memory budget and pass the solver
+// only their own input and output buffers.  Such a caller keeps x, b, the
+// matrix and the history buffer; everything else the solve needs (the four
+// iteration vectors r, z, p, Ap, the per-block partial sums and the state
+// block) lives in one file-scope device array of fixed size.
+//
+// Limits and rules:
+//   * at most kNoAllocMaxCells (1,048,576) cells; larger systems are refused
+//     with GBF_ERR_ARG -- use gbf_pcg_solve_f64 with a workspace for them;
+//   * the array occupies 32.1 MiB on every GPU that loads the library, until
+//     the process exits;
+//   * the first call on a device looks up the array's device address on that
+//     device (cudaGetSymbolAddress, with the device current) and caches it;
+//     make that first call before any stream capture that includes this
+//     entry point;
+//   * all calls share the one array, which keeps the previous call's
+//     contents: the state block is cleared at the start of every call, and
+//     calls whose work overlaps on the GPU (different streams, or different
+//     host threads on one device) race on the array and must be serialised
+//     by the caller;
+//   * nothing here calls cudaMalloc, cudaFree or any allocating routine.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace gbf {
+
+constexpr int kNoAllocMaxCells = 1 << 20;
+constexpr size_t kNoAllocVecBytes = sizeof(double) * (size_t)kNoAllocMaxCells;  // 256-aligned
+constexpr size_t kNoAllocPartialBytes = ((sizeof(double) * 2 * kMaxGrid) + 255) & ~(size_t)255;
+constexpr size_t kNoAllocStateBytes = (sizeof(PcgState) + 255) & ~(size_t)255;
+constexpr size_t kNoAllocBytes = 4 * kNoAllocVecBytes + kNoAllocPartialBytes + kNoAllocStateBytes;
+
+static __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (looked up once
+// per device).
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  GBF_CHECK_CUDA(cudaGetDevice(&dev));
+  GBF_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "pcg_noalloc: device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    GBF_CHECK_CUDA(cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch));
+    GBF_REQUIRE(p != nullptr, "pcg_noalloc: scratch address lookup returned NULL");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return GBF_OK;
+}
+
+}  // namespace gbf
+
+extern "C" int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* coef,
+                                         const double* diag, const double* pd, const double* b,
+                                         double* x, double* hist, const gbf_solve_params* P,
+                                         gbf_solve_result* R, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  GBF_REQUIRE(P && R, "pcg_noalloc: NULL params/result");
+  GBF_REQUIRE(P->max_iter >= 0, "pcg_noalloc: negative max_iter");
+  const int n = L->n_cells;
+  GBF_REQUIRE(n <= kNoAllocMaxCells,
+              "pcg_noalloc: %d cells exceed the fixed scratch limit of %d cells; use "
+              "gbf_pcg_solve_f64 with a workspace",
+              n, kNoAllocMaxCells);
+  memset(R, 0, sizeof(*R));
+  if (n == 0) {
+    const bool conv = (0 >= P->min_iter) && (0.0 < P->tolerance);
+    R->iterations = 1;
+    R->status = conv ? GBF_CONVERGED : (P->max_iter < 1 ? GBF_MAX_ITER : GBF_BREAKDOWN);
+    return GBF_OK;
+  }
+  GBF_REQUIRE(diag && b && x && hist && (L->n_faces == 0 || coef), "pcg_noalloc: NULL pointer");
+  void* scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t s = as_stream(stream);
+
+  char* w = static_cast<char*>(scratch);
+  PcgVecs v;
+  v.r = reinterpret_cast<double*>(w);
+  v.z = reinterpret_cast<double*>(w + kNoAllocVecBytes);
+  v.p = reinterpret_cast<double*>(w + 2 * kNoAllocVecBytes);
+  v.Ap = reinterpret_cast<double*>(w + 3 * kNoAllocVecBytes);
+  v.partials = reinterpret_cast<double*>(w + 4 * kNoAllocVecBytes);
+  v.st = reinterpret_cast<PcgState*>(w + 4 * kNoAllocVecBytes + kNoAllocPartialBytes);
+
+  int G = reduction_grid();
+  const int need = (n + kBlock - 1) / kBlock;
+  if (G > need) G = need;
+  // the state block (status, scalars, reduction tickets) must start at zero
+  GBF_CHECK_CUDA(cudaMemsetAsync(v.st, 0, sizeof(PcgState), s));
+  if (pd)
+    pcg_init_kernel<true><<<G, kBlock, 0, s>>>(*L, coef, diag, pd, b, x, v, hist, *P);
+  else
+    pcg_init_kernel<false><<<G, kBlock, 0, s>>>(*L, coef, diag, pd, b, x, v, hist, *P);
+  GBF_CHECK_LAUNCH();
+
+  const int chunk = P->check_every > 0 ? P->check_every : 32;
+  PcgState hs;
+  GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+  int launched = 0;
+  while (hs.status == GBF_RUNNING && launched < P->max_iter) {
+    for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
+      pcg_ap_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      if (pd)
+        pcg_update_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
+      else
+        pcg_update_kernel<false><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
+      pcg_p_kernel<<<G, kBlock, 0, s>>>(n, v);
+    }
+    GBF_CHECK_LAUNCH();
+    GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+  }
+  R->iterations = hs.n_hist;
+  R->status = (hs.status == GBF_RUNNING) ? GBF_MAX_ITER : hs.status;
+  R->final_residual = hs.res;
+  R->initial_residual = hs.res0;
+  R->launches = 1 + 3 * launched;
+  return GBF_OK;
+}
