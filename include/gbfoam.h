@@ -103,6 +103,25 @@ int gbf_dilu_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
                       const int32_t* neighbour_h, int32_t* level_ptr_h,
                       int32_t* level_faces_h, int32_t* n_levels, int32_t* max_level_size);
 
+/* Per-cell boundary-face lists (ascending face order) for the assembly:
+ * owner_b = owner of boundary faces n_internal..n_internal+n_bnd-1; bnd_ptr
+ * has n_cells + 1 entries, bnd_face n_bnd (face ids).                      */
+int gbf_boundary_lists(int32_t n_cells, int32_t n_internal, int32_t n_bnd,
+                       const int32_t* owner_b_h, int32_t* bnd_ptr_h, int32_t* bnd_face_h);
+
+/* Wavefront schedule of the face-ordered triangular sweeps of the full
+ * DIC / DILU solves (preconditioners.py:153-201, :290-337): forward
+ * (reverse = 0: faces ascending, owner read, neighbour updated) or backward
+ * (reverse = 1: faces descending, neighbour read, owner updated);
+ * lower_only keeps only faces with owner < neighbour (DIC).  Levels respect
+ * read-after-write, write-after-write and write-after-read order, so the
+ * sweep is bitwise the sequential one for any face order.  level_ptr_h has
+ * room for n_faces + 1 entries, level_faces_h for n_faces.                */
+int gbf_sweep_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                       const int32_t* neighbour_h, int32_t reverse, int32_t lower_only,
+                       int32_t* level_ptr_h, int32_t* level_faces_h, int32_t* n_levels,
+                       int32_t* max_level_size);
+
 /* ---- coefficient packing ------------------------------------------------
  * slot_coef[slot] = own_src[face] on owner-side slots, nei_src[face] on
  * neighbour-side slots, 0 on padding.  Ax packs (lower, upper); the
@@ -150,6 +169,12 @@ int gbf_dilu_build_f64(const gbf_layout* L, const double* lower, const double* u
                        const int32_t* level_faces, int32_t n_levels, int32_t max_level_size,
                        double* d_out, void* stream);
 /* DIC/DILU apply(): z = r / d (preconditioners.py:151, :288).               */
+/* One triangular sweep of apply_full: for the faces of each level,
+ * res[W] -= (coef[f] * res[R]) / d[R] if |d[R]| > 1e-30 (coef in face order:
+ * upper for the forward sweeps, upper (DIC) or lower (DILU) backward).     */
+int gbf_sweep_f64(const gbf_layout* L, const double* coef, const double* d,
+                  const int32_t* level_ptr, const int32_t* level_faces, int32_t n_levels,
+                  int32_t max_level_size, int32_t reverse, double* res, void* stream);
 int gbf_diag_apply_f64(int32_t n, const double* r, const double* d, double* z, void* stream);
 
 /* ---- Krylov solvers --------------------------------------------------------
@@ -208,6 +233,57 @@ int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* slot_coef, const 
                             const double* precond_d, const double* b, double* x,
                             double* history, const gbf_solve_params* P, gbf_solve_result* R,
                             void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- finite-volume assembly -----------------------------------------------
+ * fvm.laplacian, discretisation/operators.py:432-518: for internal faces
+ *   c = (D_f * |S_f|) * delta_f, lower = -c/V_P, upper = -c/V_N;
+ *   diag = ((0 + sum_own c/V_P) + sum_nei c/V_N) + sum_bnd c_b/V_P,
+ * |S| = sqrt(fma(z,z, fma(y,y, x*x))) (ATen's CPU row norm), all in the
+ * reference's order: bitwise equal.  d_mode 0: D = d_value; 1: per face
+ * d_face[n_faces_total]; 2: per cell d_cell[n_cells] interpolated with
+ * weights (LinearInterpolation, interpolation.py:101-145).
+ * face_areas is [n_faces_total][3]; delta and weights [n_faces_total].     */
+int gbf_laplacian_assemble_f64(const gbf_layout* L, int32_t n_faces_total,
+                               const int32_t* owner_all, const int32_t* bnd_ptr,
+                               const int32_t* bnd_face, const double* face_areas,
+                               const double* delta, int32_t d_mode, double d_value,
+                               const double* d_face, const double* d_cell, const double* weights,
+                               const double* volumes, double* lower, double* upper, double* diag,
+                               void* stream);
+/* fvm.div with the "Gauss upwind" scheme, operators.py:351-429 (no deferred
+ * correction): lower = F-/V_P, upper = F+/V_N,
+ * diag = (0 + sum_own (-F+)/V_P) + sum_nei |F-|/V_N.  flux[n_internal].    */
+int gbf_div_upwind_assemble_f64(const gbf_layout* L, const double* flux, const double* volumes,
+                                double* lower, double* upper, double* diag, void* stream);
+/* Linear-interpolation weights |d_N| / (|d_P| + |d_N|) (boundary: 1),
+ * discretisation/weights.py:21-95.                                         */
+int gbf_centre_weights_f64(int32_t n_internal, int32_t n_faces, const int32_t* owner,
+                           const int32_t* neighbour, const double* cell_centres,
+                           const double* face_centres, double* weights, void* stream);
+
+/* ---- differentiation -------------------------------------------------------
+ * Backward of gbf_laplacian_assemble_f64 for a per-face diffusivity (the
+ * reference obtains it from autograd through operators.py:488-517):
+ * g_gamma[f] = |S| delta ((g_diag_P - g_lower_f)/V_P + (g_diag_N - g_upper_f)/V_N),
+ * boundary faces |S| delta g_diag_P / V_P.                                 */
+int gbf_laplacian_grad_gamma_f64(const gbf_layout* L, int32_t n_faces_total,
+                                 const int32_t* owner_all, const double* face_areas,
+                                 const double* delta, const double* volumes,
+                                 const double* g_lower, const double* g_upper,
+                                 const double* g_diag, double* g_gamma, void* stream);
+/* DifferentiableLinearSolve.backward, differentiable/linear_solver.py:139-149:
+ * g_diag = -lam*x, g_lower = -lam[own]*x[nei], g_upper = -lam[nei]*x[own]
+ * (bitwise the reference's rounding).                                      */
+int gbf_dls_grads_f64(const gbf_layout* L, const double* lam, const double* x, double* g_diag,
+                      double* g_lower, double* g_upper, void* stream);
+/* Fused adjoint face gradient of A(D) x = b, A from gbf_laplacian_assemble:
+ * g_gamma[f] (+)= scale * (-lam^T dA/dD_f x), i.e. the two kernels above in
+ * one pass without the per-coefficient gradients.                          */
+int gbf_adjoint_face_grad_f64(const gbf_layout* L, int32_t n_faces_total,
+                              const int32_t* owner_all, const double* face_areas,
+                              const double* delta, const double* volumes, const double* lam,
+                              const double* x, double scale, int32_t accumulate,
+                              double* g_gamma, void* stream);
 
 /* ---- mixed precision -------------------------------------------------------
  * No reference counterpart (the north-star's precision pattern): PCG whose

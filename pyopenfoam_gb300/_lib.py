@@ -95,6 +95,22 @@ EXPORTED: dict[str, tuple] = {
     "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
+    "gbf_sweep_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
+                                          _c_vp, _P(_c_i32), _P(_c_i32)]),
+    "gbf_sweep_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_i32,
+                                     _c_vp, _c_vp]),
+    "gbf_boundary_lists": (ctypes.c_int, [_c_i32, _c_i32, _c_i32, _c_vp, _c_vp, _c_vp]),
+    "gbf_laplacian_assemble_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                  _c_i32, _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                  _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_div_upwind_assemble_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_centre_weights_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                              _c_vp]),
+    "gbf_laplacian_grad_gamma_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                    _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_dls_grads_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_adjoint_face_grad_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                 _c_vp, _c_dbl, _c_i32, _c_vp, _c_vp]),
     "gbf_pack_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f64_to_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),

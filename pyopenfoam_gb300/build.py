@@ -28,6 +28,7 @@ SOURCES = [
     "pcg.cu",
     "pbicgstab.cu",
     "mixed.cu",
+    "assemble.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

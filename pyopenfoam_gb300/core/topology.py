@@ -89,6 +89,7 @@ class Topology:
         )
         self._dic: Schedule | None = None
         self._dilu: Schedule | None = None
+        self._sweeps: dict = {}
 
     @property
     def layout_ref(self):
@@ -125,6 +126,26 @@ class Topology:
             self._dilu = Schedule(torch.from_numpy(ptr[: nl.value + 1].copy()).to(self.device),
                                   torch.from_numpy(faces).to(self.device), nl.value, mx.value)
         return self._dilu
+
+    def sweep_schedule(self, reverse: bool, lower_only: bool) -> Schedule:
+        """Level schedule of one triangular sweep of the full DIC/DILU solve
+        (see ``gbf_sweep_schedule``)."""
+        key = (bool(reverse), bool(lower_only))
+        hit = self._sweeps.get(key)
+        if hit is None:
+            nf = self.n_faces
+            ptr = np.empty(nf + 1, np.int32)
+            faces = np.empty(max(nf, 1), np.int32)
+            nl, mx = ctypes.c_int32(), ctypes.c_int32()
+            check(lib().gbf_sweep_schedule(self.n_cells, nf, self._own_h.ctypes.data,
+                                           self._nei_h.ctypes.data, int(reverse),
+                                           int(lower_only), ptr.ctypes.data, faces.ctypes.data,
+                                           ctypes.byref(nl), ctypes.byref(mx)),
+                  "gbf_sweep_schedule")
+            hit = Schedule(torch.from_numpy(ptr[: nl.value + 1].copy()).to(self.device),
+                           torch.from_numpy(faces).to(self.device), nl.value, mx.value)
+            self._sweeps[key] = hit
+        return hit
 
 
 _CACHE: "OrderedDict[tuple, tuple]" = OrderedDict()

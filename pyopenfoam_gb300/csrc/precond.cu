@@ -137,3 +137,51 @@ extern "C" int gbf_diag_apply_f64(int32_t n, const double* r, const double* d, d
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Triangular sweeps of the full DIC / DILU solves, one launch per level of
+// gbf_sweep_schedule: res[W] = res[W] - (coef[f] * res[R]) / d[R] when
+// |d[R]| > 1e-30, rounded as the reference's
+// `result[n] - upper[f] * result[p] / d_p` (preconditioners.py:176-182).
+// ---------------------------------------------------------------------------
+namespace gbf {
+__global__ void __launch_bounds__(kBlock)
+    sweep_level_kernel(const int32_t* __restrict__ own, const int32_t* __restrict__ nei,
+                       const double* __restrict__ coef, const double* __restrict__ d,
+                       const int32_t* __restrict__ level_ptr,
+                       const int32_t* __restrict__ level_faces, int level, int reverse,
+                       double* res) {
+  const int start = __ldg(level_ptr + level);
+  const int count = __ldg(level_ptr + level + 1) - start;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int f = __ldg(level_faces + start + t);
+  const int R = reverse ? __ldg(nei + f) : __ldg(own + f);
+  const int W = reverse ? __ldg(own + f) : __ldg(nei + f);
+  const double dr = __ldg(d + R);
+  if (fabs(dr) > 1e-30) {
+    const double u = __ddiv_rn(__dmul_rn(__ldg(coef + f), __ldcg(res + R)), dr);
+    res[W] = __dsub_rn(__ldcg(res + W), u);
+  }
+}
+}  // namespace gbf
+
+extern "C" int gbf_sweep_f64(const gbf_layout* L, const double* coef, const double* d,
+                             const int32_t* level_ptr, const int32_t* level_faces,
+                             int32_t n_levels, int32_t max_level_size, int32_t reverse,
+                             double* res, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  if (L->n_faces == 0 || n_levels == 0) return GBF_OK;
+  GBF_REQUIRE(coef && d && level_ptr && level_faces && res && L->owner && L->neighbour,
+              "sweep: NULL pointer");
+  GBF_REQUIRE(n_levels > 0 && max_level_size > 0 && max_level_size <= L->n_faces,
+              "sweep: bad schedule (levels=%d, max size=%d)", n_levels, max_level_size);
+  cudaStream_t s = as_stream(stream);
+  const int grid = (max_level_size + kBlock - 1) / kBlock;
+  for (int lv = 0; lv < n_levels; ++lv)
+    sweep_level_kernel<<<grid, kBlock, 0, s>>>(L->owner, L->neighbour, coef, d, level_ptr,
+                                               level_faces, lv, reverse ? 1 : 0, res);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}

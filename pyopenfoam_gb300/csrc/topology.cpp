@@ -203,3 +203,77 @@ extern "C" int gbf_dilu_schedule(int32_t n, int32_t nf, const int32_t* own, cons
   *n_levels = nl;
   return GBF_OK;
 }
+
+// Per-cell lists of boundary faces in ascending face order (the order in
+// which fvm.laplacian's boundary scatter_add, operators.py:508-515, adds
+// them).  owner_b holds owner[n_internal .. n_internal + n_bnd); the listed
+// face ids are n_internal + k.
+extern "C" int gbf_boundary_lists(int32_t n, int32_t n_internal, int32_t n_bnd,
+                                  const int32_t* owner_b, int32_t* bnd_ptr, int32_t* bnd_face) {
+  if (n < 0 || n_internal < 0 || n_bnd < 0 || (n_bnd > 0 && !owner_b) || !bnd_ptr ||
+      (n_bnd > 0 && !bnd_face)) {
+    gbf::set_error("boundary_lists: bad arguments");
+    return GBF_ERR_ARG;
+  }
+  for (int32_t k = 0; k < n_bnd; ++k)
+    if (owner_b[k] < 0 || owner_b[k] >= n) {
+      gbf::set_error("boundary face %d has owner %d outside [0, %d)", n_internal + k, owner_b[k], n);
+      return GBF_ERR_RANGE;
+    }
+  for (int32_t c = 0; c <= n; ++c) bnd_ptr[c] = 0;
+  for (int32_t k = 0; k < n_bnd; ++k) bnd_ptr[owner_b[k] + 1]++;
+  for (int32_t c = 0; c < n; ++c) bnd_ptr[c + 1] += bnd_ptr[c];
+  std::vector<int32_t> cur(bnd_ptr, bnd_ptr + (n > 0 ? n : 0));
+  for (int32_t k = 0; k < n_bnd; ++k) bnd_face[cur[owner_b[k]]++] = n_internal + k;
+  return GBF_OK;
+}
+
+// Wavefront schedule of a face-ordered triangular sweep (the full DIC / DILU
+// solves, solvers/preconditioners.py:153-201, :290-337).  Face f reads cell
+// R and updates cell W (forward: R = owner, W = neighbour, faces ascending;
+// reverse: R = neighbour, W = owner, faces descending); with lower_only the
+// faces with owner >= neighbour are skipped (the DIC sweeps' "if p < n").
+// A face's level follows the last writer of R (read after write) and the last
+// reader or writer of W (write after read / write), so every level can run
+// in parallel and each cell sees its updates in the reference's face order.
+extern "C" int gbf_sweep_schedule(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                                  int32_t reverse, int32_t lower_only, int32_t* level_ptr,
+                                  int32_t* level_faces, int32_t* n_levels,
+                                  int32_t* max_level_size) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  std::vector<int32_t> last_w((size_t)n, -1), last_a((size_t)n, -1);
+  std::vector<int32_t> level((size_t)nf, -1);
+  int32_t nl = 0, used = 0;
+  for (int32_t i = 0; i < nf; ++i) {
+    const int32_t f = reverse ? nf - 1 - i : i;
+    if (lower_only && !(own[f] < nei[f])) continue;
+    const int32_t R = reverse ? nei[f] : own[f];
+    const int32_t W = reverse ? own[f] : nei[f];
+    const int32_t l = std::max(last_w[R], last_a[W]) + 1;
+    level[f] = l;
+    last_w[W] = l;
+    last_a[W] = l;
+    last_a[R] = std::max(last_a[R], l);
+    nl = std::max(nl, l + 1);
+    ++used;
+  }
+  // bucket by level; inside a level, faces in sweep order
+  std::vector<int32_t> cnt((size_t)nl + 1, 0);
+  for (int32_t f = 0; f < nf; ++f)
+    if (level[f] >= 0) cnt[(size_t)level[f] + 1]++;
+  int32_t mx = 0;
+  for (int32_t l = 0; l < nl; ++l) {
+    mx = std::max(mx, cnt[(size_t)l + 1]);
+    cnt[(size_t)l + 1] += cnt[l];
+  }
+  for (int32_t l = 0; l <= nl; ++l) level_ptr[l] = cnt[l];
+  for (int32_t i = 0; i < nf; ++i) {
+    const int32_t f = reverse ? nf - 1 - i : i;
+    if (level[f] >= 0) level_faces[cnt[level[f]]++] = f;
+  }
+  *n_levels = nl;
+  *max_level_size = mx;
+  (void)used;
+  return GBF_OK;
+}

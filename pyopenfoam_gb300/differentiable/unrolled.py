@@ -1,0 +1,193 @@
+"""Gradients through unrolled implicit time steps with checkpointing.
+
+    A(gamma) x_{t+1} = x_t / dt,   A = I/dt + fvm.laplacian(gamma)   (t < T)
+    L = || x_T - x_target ||^2
+
+The gradient with respect to every face diffusivity gamma_f comes from the
+discrete adjoint: g_T = 2 (x_T - x_target); for t = T .. 1 solve
+A^T lam_t = g_t, accumulate dL/dgamma -= lam_t^T (dA/dgamma) x_t with the
+fused face kernel ``gbf_adjoint_face_grad_f64``, and pass g_{t-1} = lam_t/dt.
+Only every ``checkpoint_every``-th state is kept during the forward sweep;
+the backward sweep recomputes each segment from its checkpoint, so memory
+holds (T / k) + k states instead of T.
+
+No reference counterpart as a whole: the reference differentiates one solve
+at a time (``DifferentiableLinearSolve``) and through ``fvm.laplacian`` by
+autograd; chaining those over T steps stores every state.
+``UnrolledDiffusion`` is the autograd entry point; ``loss_and_grad`` the
+explicit one used by the benchmark.
+"""
+
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import torch
+
+from .. import _lib
+from ..core.ldu_matrix import LduMatrix
+from ..discretisation.operators import fvm, mesh_data
+from ..solvers.pcg import PCGSolver
+
+__all__ = ["UnrolledImplicitDiffusion", "UnrolledDiffusion", "GradStats"]
+
+
+@dataclass
+class GradStats:
+    forward_s: float = 0.0
+    backward_s: float = 0.0
+    forward_solves: int = 0
+    backward_solves: int = 0
+    recompute_solves: int = 0
+    iterations: list = field(default_factory=list)
+    peak_bytes: int = 0
+
+
+class UnrolledImplicitDiffusion:
+    """Implicit diffusion steps on ``mesh`` with per-face diffusivity.
+
+    Parameters
+    ----------
+    mesh : duck-typed FvMesh on a CUDA device
+    dt, steps : time step and number of implicit steps
+    checkpoint_every : states kept every k steps (k = steps keeps only x_0)
+    solver : linear solver for forward and adjoint systems (default FP64
+        PCG+DIC to a 1e-14 relative residual)
+    """
+
+    def __init__(self, mesh, dt: float = 1e-3, steps: int = 20, checkpoint_every: int = 5,
+                 solver=None) -> None:
+        if steps < 1 or checkpoint_every < 1:
+            raise ValueError("steps and checkpoint_every must be >= 1")
+        self.mesh = mesh
+        self.md = mesh_data(mesh)
+        self.dt = float(dt)
+        self.steps = int(steps)
+        self.k = int(checkpoint_every)
+        self.solver = solver or PCGSolver(tolerance=0.0, rel_tol=1e-14, max_iter=50000,
+                                          preconditioner="DIC")
+        self.stats = GradStats()
+
+    # ------------------------------------------------------------------
+    def system(self, gamma: torch.Tensor) -> LduMatrix:
+        """A = I/dt + Laplacian(gamma) (no autograd)."""
+        with torch.no_grad():
+            lap = fvm.laplacian(gamma.detach(), torch.zeros(1), mesh=self.mesh)
+        A = LduMatrix(self.md.n_cells, lap.owner, lap.neighbour, device=lap.device)
+        A._topology = lap.topology()
+        A.diag = lap.diag + 1.0 / self.dt
+        A.lower = lap.lower
+        A.upper = lap.upper
+        return A
+
+    @staticmethod
+    def transpose(A: LduMatrix) -> LduMatrix:
+        At = LduMatrix(A.n_cells, A.owner, A.neighbour, device=A.device)
+        At._topology = A.topology()
+        At.diag, At.lower, At.upper = A.diag, A.upper, A.lower
+        return At
+
+    def _step(self, A: LduMatrix, x: torch.Tensor) -> torch.Tensor:
+        # warm start from the previous state
+        xn, it, _ = self.solver(A, x / self.dt, x)
+        self.stats.iterations.append(it)
+        return xn
+
+    def forward_states(self, A: LduMatrix, x0: torch.Tensor):
+        """x_T and the checkpoints {t: x_t} (t multiple of k, t < T)."""
+        ckpt = {0: x0}
+        x = x0
+        for t in range(1, self.steps + 1):
+            x = self._step(A, x)
+            self.stats.forward_solves += 1
+            if t % self.k == 0 and t < self.steps:
+                ckpt[t] = x
+        return x, ckpt
+
+    def backward_grad(self, A: LduMatrix, ckpt: dict, xT: torch.Tensor, gT: torch.Tensor):
+        """(dL/dgamma over all faces, dL/dx_0) for dL/dx_T = gT."""
+        md = self.md
+        At = self.transpose(A)
+        topo = A.topology()
+        dev = md.device
+        grad = torch.zeros(max(md.n_faces, 1), device=dev, dtype=torch.float64)
+        areas = md.field("face_areas")
+        delta = md.field("delta_coefficients")
+        vols = md.field("cell_volumes")
+        g = gT
+        starts = sorted(ckpt)
+        L = _lib.lib()
+        for s in reversed(starts):
+            e = min(s + self.k, self.steps)
+            # recompute x_{s+1} .. x_{e-1}; x_e is the next checkpoint or x_T
+            seg = {s: ckpt[s]}
+            x = ckpt[s]
+            for t in range(s + 1, e):
+                x = self._step(A, x)
+                self.stats.recompute_solves += 1
+                seg[t] = x
+            seg[e] = xT if e == self.steps else ckpt[e]
+            for t in range(e, s, -1):
+                lam, it, _ = self.solver(At, g, torch.zeros_like(g))
+                self.stats.iterations.append(it)
+                self.stats.backward_solves += 1
+                xt = seg[t].contiguous()
+                lam = lam.contiguous()
+                _lib.check(L.gbf_adjoint_face_grad_f64(
+                    topo.layout_ref, md.n_faces, md.owner_all32.data_ptr(), areas.data_ptr(),
+                    delta.data_ptr(), vols.data_ptr(), lam.data_ptr(), xt.data_ptr(), 1.0, 1,
+                    grad.data_ptr(), _lib.stream_ptr(dev)), "gbf_adjoint_face_grad_f64")
+                g = lam / self.dt
+                del seg[t]
+        return grad[: md.n_faces], g
+
+    # ------------------------------------------------------------------
+    def loss_and_grad(self, gamma: torch.Tensor, x0: torch.Tensor, target: torch.Tensor):
+        """Loss ||x_T - target||^2 and its gradient over all face
+        diffusivities, with timing and memory statistics in ``self.stats``."""
+        self.stats = GradStats()
+        dev = self.md.device
+        torch.cuda.synchronize(dev)
+        torch.cuda.reset_peak_memory_stats(dev)
+        base = torch.cuda.memory_allocated(dev)
+        t0 = time.perf_counter()
+        A = self.system(gamma)
+        xT, ckpt = self.forward_states(A, x0.to(dev, torch.float64))
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        diff = xT - target
+        loss = float(torch.dot(diff, diff))
+        grad, _ = self.backward_grad(A, ckpt, xT, 2.0 * diff)
+        torch.cuda.synchronize(dev)
+        t2 = time.perf_counter()
+        self.stats.forward_s = t1 - t0
+        self.stats.backward_s = t2 - t1
+        self.stats.peak_bytes = torch.cuda.max_memory_allocated(dev) - base
+        return loss, grad
+
+    def final_state(self, gamma: torch.Tensor, x0: torch.Tensor) -> torch.Tensor:
+        A = self.system(gamma)
+        x = x0.to(self.md.device, torch.float64)
+        for _ in range(self.steps):
+            x = self._step(A, x)
+        return x
+
+
+class UnrolledDiffusion(torch.autograd.Function):
+    """``x_T = UnrolledDiffusion.apply(gamma, x0, model)``: differentiable with
+    respect to the per-face diffusivity ``gamma`` and the initial state."""
+
+    @staticmethod
+    def forward(ctx, gamma, x0, model: UnrolledImplicitDiffusion):
+        A = model.system(gamma)
+        xT, ckpt = model.forward_states(A, x0.detach().to(model.md.device, torch.float64))
+        ctx.model, ctx.A, ctx.ckpt = model, A, ckpt
+        ctx.save_for_backward(xT)
+        return xT
+
+    @staticmethod
+    def backward(ctx, g):
+        (xT,) = ctx.saved_tensors
+        grad_gamma, grad_x0 = ctx.model.backward_grad(ctx.A, ctx.ckpt, xT, g.contiguous())
+        return grad_gamma, grad_x0, None

@@ -72,6 +72,8 @@ def mesh_from_arrays(d: dict, device="cpu", dtype=None):
         owner=t(d["owner"], torch.int64), neighbour=t(d["neighbour"], torch.int64),
         face_areas=t(d["face_areas"]), delta_coefficients=t(d["delta"]),
         cell_volumes=t(d["volumes"]), device=torch.device(device), dtype=dtype,
+        cell_centres=t(d["cell_centres"]) if "cell_centres" in d else None,
+        face_centres=t(d["face_centres"]) if "face_centres" in d else None,
     )
 
 
@@ -101,11 +103,42 @@ def jitter_case(N: int = 6, seed: int = 1, store: bool = True):
             n_cells=np.int64(m.n_cells), n_internal=np.int64(nint),
             owner=m.numpy("owner"), neighbour=m.numpy("neighbour"),
             face_areas=m.numpy("face_areas"), delta=m.numpy("delta_coefficients"),
-            volumes=m.numpy("cell_volumes"),
+            volumes=m.numpy("cell_volumes"), cell_centres=m.numpy("cell_centres"),
+            face_centres=m.numpy("face_centres"),
             gamma=rng.lognormal(0.0, 1.0, m.n_faces), phi=phi,
             b=rng.uniform(-1.0, 1.0, m.n_cells), w=rng.uniform(-1.0, 1.0, m.n_cells),
         )
         if store:
             np.savez_compressed(path, **d)
+    d["mesh"] = mesh_from_arrays(d)
+    return d
+
+
+def unroll_case(N: int = 10, dt: float = 1e-3, steps: int = 20, seed: int = 4) -> dict:
+    """Config-5 structure at a small size: uniform N^3 mesh (fixed value on
+    x0), per-face diffusivity gamma ~ LogNormal(0, 1), x0 ~ U[0, 1], and a
+    target produced by the same 20 implicit steps with a second draw gamma'
+    (computed here with the oracle restatement: fvm.laplacian + PCG)."""
+    from pyopenfoam_gb300.mesh import HexMesh
+
+    m = HexMesh(N)
+    rng = np.random.default_rng(seed)
+    gamma = rng.lognormal(0.0, 1.0, m.n_faces)
+    gamma2 = rng.lognormal(0.0, 1.0, m.n_faces)
+    x0 = rng.uniform(0.0, 1.0, m.n_cells)
+    d = dict(n_cells=np.int64(m.n_cells), n_internal=np.int64(m.n_internal_faces),
+             owner=m.numpy("owner"), neighbour=m.numpy("neighbour"),
+             face_areas=m.numpy("face_areas"), delta=m.numpy("delta_coefficients"),
+             volumes=m.numpy("cell_volumes"))
+    from oracle import oracle as O
+
+    nint = m.n_internal_faces
+    lo, up, dg = O.laplacian(m.n_cells, d["owner"], d["neighbour"], d["face_areas"], d["delta"],
+                             gamma2, d["volumes"])
+    x = x0.copy()
+    for _ in range(steps):
+        x = O.pcg(d["owner"][:nint], d["neighbour"], dg + 1.0 / dt, lo, up, x / dt, x, None, 0.0,
+                  1e-14, 5000).x
+    d.update(gamma=gamma, x0=x0, target=x, dt=dt, steps=steps)
     d["mesh"] = mesh_from_arrays(d)
     return d

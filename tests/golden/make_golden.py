@@ -27,7 +27,7 @@ sys.path.insert(0, ROOT)
 sys.dont_write_bytecode = True
 
 from tests.golden.cases import (  # noqa: E402
-    c1_poisson, jitter_case, random_ldu, sha,
+    c1_poisson, jitter_case, random_ldu, sha, unroll_case,
 )
 
 
@@ -97,6 +97,14 @@ def main(ref_root: str) -> None:
     for k, a in (("lap_lower", L.lower), ("lap_upper", L.upper), ("lap_diag", L.diag),
                  ("div_lower", Dv.lower), ("div_upper", Dv.upper), ("div_diag", Dv.diag)):
         out[f"j6_{k}"] = a.numpy().copy()
+    # per-cell diffusivity (linear interpolation to faces) and a scalar one
+    dcell = np.random.default_rng(7).lognormal(0.0, 1.0, mesh.n_cells)
+    Lc = fvm.laplacian(t(dcell), torch.zeros(mesh.n_cells, dtype=torch.float64), mesh=mesh)
+    Ls = fvm.laplacian(1.5, torch.zeros(mesh.n_cells, dtype=torch.float64), mesh=mesh)
+    out["j6_dcell"] = dcell
+    for k, a in (("lapc_lower", Lc.lower), ("lapc_upper", Lc.upper), ("lapc_diag", Lc.diag),
+                 ("laps_lower", Ls.lower), ("laps_upper", Ls.upper), ("laps_diag", Ls.diag)):
+        out[f"j6_{k}"] = a.numpy().copy()
     A = LduMatrix(mesh.n_cells, mesh.owner[: mesh.n_internal_faces], mesh.neighbour)
     A.diag, A.lower, A.upper = L.diag - Dv.diag, L.lower - Dv.lower, L.upper - Dv.upper
     b = t(jc["b"])
@@ -127,6 +135,32 @@ def main(ref_root: str) -> None:
     out["dls_grad_upper"] = upper.grad.numpy()
     out["dls_grad_b"] = bb.grad.numpy()
     print("dls done", flush=True)
+
+    # ---- 5. Unrolled implicit diffusion: 20 steps of (I/dt + L(gamma)) x' = x/dt
+    #         through fvm.laplacian (autograd) and DifferentiableLinearSolve
+    uc = unroll_case(10)
+    mesh10 = uc["mesh"]
+    gam = t(uc["gamma"]).clone().requires_grad_(True)
+    solver = PCGSolver(tolerance=0.0, rel_tol=1e-14, max_iter=5000, preconditioner="none")
+    own10 = mesh10.owner[: mesh10.n_internal_faces]
+
+    def run(gamma, x0):
+        lap = fvm.laplacian(gamma, torch.zeros(mesh10.n_cells, dtype=torch.float64), mesh=mesh10)
+        d = lap.diag + 1.0 / uc["dt"]
+        x = x0
+        for _ in range(uc["steps"]):
+            x = DifferentiableLinearSolve.apply(d, lap.lower, lap.upper, x / uc["dt"], solver,
+                                                own10, mesh10.neighbour, x, 0.0, 5000)
+        return x
+
+    xT = run(gam, t(uc["x0"]))
+    loss = ((xT - t(uc["target"])) ** 2).sum()
+    loss.backward()
+    out["unroll_target"] = uc["target"]
+    out["unroll_xT"] = xT.detach().numpy()
+    out["unroll_loss"] = np.float64(loss.item())
+    out["unroll_grad"] = gam.grad.numpy()
+    print("unroll done", float(loss), flush=True)
 
     path = os.path.join(HERE, "reference_outputs.npz")
     np.savez_compressed(path, **out)
