@@ -67,6 +67,12 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    p.add_argument("--workload", choices=["c3", "c1", "c2", "c4", "c5"], default="c3",
+                   help="c3 (default, the headline): 256^3 mixed vs FP64 PCG; c1: 32^3 "
+                        "PCG+DIC to 1e-6; c2: 128^3 jittered convection-diffusion with "
+                        "PBiCGStab+DILU; c5: adjoint gradient of 20 implicit steps at 96^3")
+    p.add_argument("--fd-faces", type=int, default=32, help="c5: faces checked by central "
+                                                            "differences")
     return p.parse_args()
 
 
@@ -426,11 +432,263 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def _line(args, world, metric, value, unit, hib, workload, extra, **kw):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+         "warmup": args.warmup, "ms_per_step": value * 1e3 if unit == "s" else None,
+         "higher_is_better": hib, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+         "data": "synthetic", "config": workload}
+    d.update(kw)
+    d["extra"] = extra
+    print(json.dumps(d), flush=True)
+
+
+def run_c1(args, rank, world, local):
+    """32^3 Poisson, PCG+DIC to 1e-6 relative (the reference's CPU case)."""
+    from oracle import oracle as O
+    from pyopenfoam_gb300 import PCGSolver
+    from pyopenfoam_gb300.mesh.poisson import hex_poisson
+
+    dev = torch.device("cuda", local)
+    sysd = hex_poisson(32, seed=0)
+    m = make_matrix(sysd, dev)
+    b = torch.as_tensor(sysd["b"]).to(dev)
+    x0 = torch.zeros_like(b)
+    s = PCGSolver(tolerance=0.0, rel_tol=1e-6, max_iter=1000, preconditioner="DIC")
+    ts = []
+    for i in range(args.warmup + args.steps):
+        m.invalidate_cache()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x, it, res = s(m, b, x0)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    gpu = max_over_ranks(statistics.median(ts), world)
+    cpu = None
+    if rank == 0:
+        own, nei = sysd["owner"], sysd["neighbour"]
+        t0 = time.perf_counter()
+        pd = O.dic_build(own, nei, sysd["diag"], sysd["upper"])
+        o = O.pcg(own, nei, sysd["diag"], sysd["lower"], sysd["upper"], sysd["b"],
+                  np.zeros(sysd["n"]), pd, 0.0, 1e-6, 1000, threads=len(os.sched_getaffinity(0)))
+        cpu = time.perf_counter() - t0
+        _line(args, world, "config 1: 32^3 Poisson PCG+DIC to 1e-6 relative residual, time",
+              gpu, "s", False,
+              {"workload": "32^3 Poisson (unit-cube hex, x0 fixed value), PCG+DIC to 1e-6",
+               "n_cells": sysd["n"]},
+              {"iterations": it, "oracle_iterations": o.iterations,
+               "x_rel_err_vs_oracle": float(np.abs(x.cpu().numpy() - o.x).max() /
+                                            np.abs(o.x).max())},
+              cpu_baseline={"value": cpu, "unit": "s", "cores": len(os.sched_getaffinity(0)),
+                            "kind": "port", "sample": "full solve"})
+
+
+def c2_system(N: int, dev):
+    """Config 2: N^3 hex mesh with +-20 % jitter (seed 1), face diffusivity
+    LogNormal(0, 1), upwind convection of u = (1, 0.5, 0.25) scaled to a cell
+    Peclet number of ~10, fixed value on x = 0.  The flux uses the nominal
+    (unjittered) face areas, so it is positive on every internal face and
+    divergence free; the outflow boundary faces add F_b/V_P to the diagonal
+    (what a zero-gradient outflow condition contributes to an upwind
+    convection matrix -- the reference's fvm.div itself skips boundary
+    faces, which leaves a closed box)."""
+    from pyopenfoam_gb300 import LduMatrix
+    from pyopenfoam_gb300.discretisation import fvm
+    from pyopenfoam_gb300.mesh import HexMesh
+
+    mesh = HexMesh(N, jitter=0.2, seed=1, device=dev)
+    nominal = HexMesh(N)
+    rng = np.random.default_rng(1)
+    gamma = rng.lognormal(0.0, 1.0, mesh.n_faces)
+    b = rng.uniform(-1.0, 1.0, mesh.n_cells)
+    u = np.array([1.0, 0.5, 0.25])
+    phi = (nominal.numpy("face_areas") * u).sum(axis=1) * (10.0 * N / np.linalg.norm(u))
+    nint = mesh.n_internal_faces
+    Lap = fvm.laplacian(torch.as_tensor(gamma), torch.zeros(1), mesh=mesh)
+    Dv = fvm.div(torch.as_tensor(phi), torch.zeros(1), "Gauss upwind", mesh=mesh)
+    own_b = mesh.numpy("owner")[nint:]
+    V = mesh.numpy("cell_volumes")
+    out_b = np.zeros(mesh.n_cells)
+    np.add.at(out_b, own_b, np.where(phi[nint:] > 0.0, phi[nint:], 0.0) / V[own_b])
+    A = LduMatrix(mesh.n_cells, Lap.owner, Lap.neighbour, device=dev)
+    A.diag = Lap.diag - Dv.diag + torch.as_tensor(out_b).to(dev)
+    A.lower = Lap.lower - Dv.lower
+    A.upper = Lap.upper - Dv.upper
+    return mesh, A, torch.as_tensor(b).to(dev)
+
+
+def run_c2(args, rank, world, local):
+    """128^3 jittered convection-diffusion, PBiCGStab+DILU to 1e-8."""
+    from oracle import oracle as O
+    from pyopenfoam_gb300 import PBiCGSTABSolver
+
+    dev = torch.device("cuda", local)
+    N = 128 if args.n == 256 else args.n
+    t0 = time.perf_counter()
+    mesh, A, b = c2_system(N, dev)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    res = {}
+    for omega in ("standard", "reference"):
+        s = PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000, omega=omega)
+        ts = []
+        for i in range(args.warmup + args.steps):
+            A.invalidate_cache()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            x, it, r = s(A, b, torch.zeros_like(b))
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                ts.append(time.perf_counter() - t0)
+        res[omega] = {"s": statistics.median(ts), "checks": it,
+                      "converged": s.last_info.converged,
+                      "true_rel_residual": true_rel_residual(A, x, b), "x": x}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        own = A.owner.cpu().numpy()
+        nei = A.neighbour.cpu().numpy()
+        d, lo, up = A.diag.cpu().numpy(), A.lower.cpu().numpy(), A.upper.cpu().numpy()
+        threads = len(os.sched_getaffinity(0))
+        t0 = time.perf_counter()
+        pd = O.dilu_build(own, nei, d, lo, up)
+        o = O.pbicgstab(own, nei, d, lo, up, b.cpu().numpy(), np.zeros(mesh.n_cells), pd, 0.0,
+                        1e-8, 4000, threads=threads, omega="standard")
+        t_cpu = time.perf_counter() - t0
+        xs = res["standard"]["x"].cpu().numpy()
+        cpu = {"value": t_cpu, "unit": "s", "cores": threads, "kind": "port",
+               "sample": "full solve (oracle PBiCGStab+DILU, standard omega)",
+               "checks": o.iterations, "converged": o.converged,
+               "x_rel_err_gpu_vs_oracle": float(np.abs(xs - o.x).max() / np.abs(o.x).max())}
+    for v in res.values():
+        v.pop("x")
+    if rank == 0:
+        _line(args, world, "config 2: 128^3 jittered convection-diffusion, PBiCGStab+DILU "
+              "(standard omega) to 1e-8 relative, time", res["standard"]["s"], "s", False,
+              {"workload": f"{N}^3 hex, +-20% jitter, log-normal gamma, upwind Pe~10, outflow "
+                           "boundary term", "n_cells": mesh.n_cells,
+               "n_faces": mesh.n_internal_faces},
+              {"omega_standard": res["standard"], "omega_reference": res["reference"],
+               "setup_s": t_setup}, cpu_baseline=cpu)
+
+
+def run_c4(args, rank, world, local):
+    """64 independent Poisson systems (sides U{16..96}, seed 3), mixed
+    FP32/FP64 refined PCG+DIC to 1e-8: one batched solve vs 64 sequential
+    single-system solves."""
+    from pyopenfoam_gb300 import MixedPrecisionPCGSolver
+    from pyopenfoam_gb300.mesh.batch import poisson_batch
+    from pyopenfoam_gb300.solvers.batched import BatchedPCGSolver
+
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    mats, rhs, sides = poisson_batch(64, 16, 96, sigma=0.5, seed=3, device=dev)
+    t_setup = time.perf_counter() - t0
+    n_total = sum(m.n_cells for m in mats)
+    bs = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000)
+    t0 = time.perf_counter()
+    bs.solve(mats, rhs)  # autotune (cached) + warm-up
+    torch.cuda.synchronize()
+    t_tune = time.perf_counter() - t0
+    for _ in range(max(args.warmup - 1, 0)):
+        bs.solve(mats, rhs)
+    ts = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = bs.solve(mats, rhs)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    t_batch = max_over_ranks(statistics.median(ts), world)
+    conv = sum(i.converged for i in bs.last_infos)
+    worst = max(true_rel_residual(m, x, b) for (x, _, _), m, b in zip(out, mats, rhs))
+    single = MixedPrecisionPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000)
+    for m, b in zip(mats[:4], rhs[:4]):
+        single(m, b, torch.zeros_like(b))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for m, b in zip(mats, rhs):
+        m.invalidate_cache()
+        single(m, b, torch.zeros_like(b))
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    if rank == 0:
+        _line(args, world, "config 4: 64 uneven Poisson systems, batched mixed PCG+DIC to 1e-8, "
+              "time", t_batch, "s", False,
+              {"workload": "64 uniform hex Poisson systems, sides U{16..96} (seed 3), gamma "
+                           "LogNormal(0,0.5), mixed FP32/FP64 refined to 1e-8",
+               "n_cells": n_total, "sides": sides},
+              {"sequential_s": t_seq, "speedup_vs_sequential": t_seq / t_batch,
+               "converged": conv, "worst_true_rel_residual": worst,
+               "iterations_min_max": [min(r.iterations for r in bs.last_results),
+                                      max(r.iterations for r in bs.last_results)],
+               "autotuned": {k: v for k, v in bs.last_config.items()},
+               "setup_s": t_setup, "first_solve_incl_autotune_s": t_tune})
+
+
+def run_c5(args, rank, world, local):
+    """Adjoint gradient through 20 implicit diffusion steps at 96^3."""
+    from pyopenfoam_gb300 import PCGSolver
+    from pyopenfoam_gb300.differentiable.unrolled import UnrolledImplicitDiffusion
+    from pyopenfoam_gb300.mesh import HexMesh
+
+    dev = torch.device("cuda", local)
+    N = 96 if args.n == 256 else args.n
+    mesh = HexMesh(N, device=dev)
+    rng = np.random.default_rng(4)
+    gamma = torch.as_tensor(rng.lognormal(0.0, 1.0, mesh.n_faces)).to(dev)
+    gamma2 = torch.as_tensor(rng.lognormal(0.0, 1.0, mesh.n_faces)).to(dev)
+    x0 = torch.as_tensor(rng.uniform(0.0, 1.0, mesh.n_cells)).to(dev)
+    solver = PCGSolver(tolerance=0.0, rel_tol=1e-14, max_iter=50000, preconditioner="DIC")
+    model = UnrolledImplicitDiffusion(mesh, dt=1e-3, steps=20, checkpoint_every=5, solver=solver)
+    target = model.final_state(gamma2, x0)
+    for _ in range(args.warmup):
+        model.loss_and_grad(gamma, x0, target)
+    fw, bw, peak = [], [], []
+    for _ in range(args.steps):
+        loss, grad = model.loss_and_grad(gamma, x0, target)
+        fw.append(model.stats.forward_s)
+        bw.append(model.stats.backward_s)
+        peak.append(model.stats.peak_bytes)
+    iters = model.stats.iterations
+    full = UnrolledImplicitDiffusion(mesh, dt=1e-3, steps=20, checkpoint_every=1, solver=solver)
+    full.loss_and_grad(gamma, x0, target)
+    peak_all = full.stats.peak_bytes
+    faces = rng.choice(mesh.n_faces, args.fd_faces, replace=False)
+    errs = []
+    t0 = time.perf_counter()
+    for f in faces:
+        fd = model.central_difference(gamma, x0, target, int(f), 1e-6)
+        g = float(grad[f])
+        errs.append(abs(fd - g) / max(abs(g), 1e-300))
+    t_fd = time.perf_counter() - t0
+    f_s, b_s = statistics.median(fw), statistics.median(bw)
+    if rank == 0:
+        _line(args, world, "config 5: adjoint gradient of 20 implicit steps (96^3), "
+              "forward + backward time", f_s + b_s, "s", False,
+              {"workload": f"{N}^3 uniform hex, dt=1e-3, 20 steps, gamma ~ LogNormal(0,1) "
+                           "per face, checkpoint every 5", "n_cells": mesh.n_cells,
+               "n_faces": mesh.n_faces},
+              {"forward_s": f_s, "backward_s": b_s, "backward_over_forward": b_s / f_s,
+               "peak_bytes_checkpointed": statistics.median(peak),
+               "peak_bytes_all_states": peak_all, "loss": loss,
+               "solver_iterations_per_solve": statistics.mean(iters),
+               "fd_faces": len(errs), "fd_h": 1e-6, "fd_max_rel_err": max(errs),
+               "fd_median_rel_err": statistics.median(errs), "fd_seconds": t_fd})
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "c1":
+        run_c1(args, rank, world, local)
+    elif args.workload == "c2":
+        run_c2(args, rank, world, local)
+    elif args.workload == "c4":
+        run_c4(args, rank, world, local)
+    elif args.workload == "c5":
+        run_c5(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

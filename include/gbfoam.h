@@ -303,6 +303,34 @@ int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double*
                         const gbf_solve_params* P, gbf_solve_result* R, void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/* ---- batching ---------------------------------------------------------------
+ * No reference counterpart.  Many independent systems solved together: the
+ * layout is their block-diagonal concatenation (each system's cells padded
+ * to a multiple of 32), cut into tiles -- contiguous cell ranges of one
+ * system, one CTA each.  Systems keep their own scalars, residual checks
+ * and convergence; finished systems' tiles return at once.  Same iteration
+ * as gbf_mixed_pcg_solve (FP32 inner, FP64 reliable updates); with
+ * use_graph a chunk of iterations is captured once in a CUDA graph and
+ * replayed.  R has n_systems entries.  block_size: 128, 256 or 512.        */
+typedef struct gbf_batch {
+  int32_t n_systems;
+  int32_t n_tiles;
+  const int32_t* tile_sys;   /* [n_tiles] system of each tile               */
+  const int32_t* tile_begin; /* [n_tiles] first cell                        */
+  const int32_t* tile_end;   /* [n_tiles] one past the last cell            */
+  const int32_t* sys_tile0;  /* [n_systems + 1] tiles of system s are
+                                sys_tile0[s] .. sys_tile0[s+1]-1            */
+} gbf_batch;
+
+size_t gbf_batched_mixed_pcg_workspace_bytes(int32_t n_cells, int32_t n_systems,
+                                             int32_t n_tiles);
+int gbf_batched_mixed_pcg_solve(const gbf_layout* L, const gbf_batch* B, const double* coef64,
+                                const double* diag64, const float* coef32,
+                                const double* precond_d, const double* b, double* x,
+                                double delta, const gbf_solve_params* P, int32_t block_size,
+                                int32_t use_graph, gbf_solve_result* R, void* workspace,
+                                size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,7 @@ __all__ = [
     "lib",
     "check",
     "Layout",
+    "Batch",
     "SolveParams",
     "SolveResult",
     "ptr",
@@ -81,6 +82,19 @@ class SolveResult(ctypes.Structure):
     ]
 
 
+class Batch(ctypes.Structure):
+    """``gbf_batch``: tile map of a block-diagonal batch (device pointers)."""
+
+    _fields_ = [
+        ("n_systems", _c_i32),
+        ("n_tiles", _c_i32),
+        ("tile_sys", _c_vp),
+        ("tile_begin", _c_vp),
+        ("tile_end", _c_vp),
+        ("sys_tile0", _c_vp),
+    ]
+
+
 _P = ctypes.POINTER
 _L = _P(Layout)
 
@@ -129,6 +143,10 @@ EXPORTED: dict[str, tuple] = {
     "gbf_mixed_pcg_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl,
                                            _c_vp, _c_i32, _P(SolveParams), _P(SolveResult),
                                            _c_vp, _c_size, _c_vp]),
+    "gbf_batched_mixed_pcg_workspace_bytes": (_c_size, [_c_i32, _c_i32, _c_i32]),
+    "gbf_batched_mixed_pcg_solve": (ctypes.c_int, [_L, _P(Batch), _c_vp, _c_vp, _c_vp, _c_vp,
+                                                   _c_vp, _c_vp, _c_dbl, _P(SolveParams), _c_i32,
+                                                   _c_i32, _c_vp, _c_vp, _c_size, _c_vp]),
     "gbf_pbicgstab_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_pbicgstab_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                                _P(SolveParams), _P(SolveResult), _c_vp, _c_size,

@@ -29,6 +29,7 @@ SOURCES = [
     "pbicgstab.cu",
     "mixed.cu",
     "assemble.cu",
+    "batched.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,5 +1,6 @@
 """GPU linear solvers with the reference's ``pyfoam.solvers`` interface."""
 
+from .batched import BatchedPCGSolver
 from .linear_solver import LinearSolverBase, create_solver, register_solver, solver_from_dict
 from .mixed import MixedPrecisionPCGSolver
 from .pbicgstab import PBiCGSTABSolver
@@ -10,5 +11,5 @@ from .residual import ConvergenceInfo, ResidualMonitor
 __all__ = [
     "LinearSolverBase", "create_solver", "solver_from_dict", "register_solver", "PCGSolver",
     "PBiCGSTABSolver", "MixedPrecisionPCGSolver", "DICPreconditioner", "DILUPreconditioner", "Preconditioner",
-    "ConvergenceInfo", "ResidualMonitor",
+    "ConvergenceInfo", "ResidualMonitor", "BatchedPCGSolver",
 ]
