@@ -12,19 +12,18 @@
 
 namespace gbf {
 
-// Sum over `cnt` slots starting at slot index i0 (stride 32) of
-// coef[slot] * x[col[slot]], skipping padding (col < 0).  Products are
-// rounded in T, sums in A.
+// Sum over `cnt` slots starting at slot k0 of cell c (slot index i0 =
+// base + 32*k0, compressed entry e0 + k0) of coef[slot] * x[col[slot]],
+// skipping padding (col < 0).  Products are rounded in T, sums in A.
 template <typename T, typename A>
-__device__ __forceinline__ A slot_sum(const int32_t* __restrict__ slot_col,
-                                      const T* __restrict__ coef, const T* __restrict__ x,
-                                      int i0, int cnt) {
+__device__ __forceinline__ A slot_sum(const gbf_layout& L, const T* __restrict__ coef,
+                                      const T* __restrict__ x, int c, int i0, int e0, int cnt) {
   A s = (A)0;
   if (cnt <= 4) {
     int col[4];
     T a[4], xv[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) col[k] = (k < cnt) ? __ldg(slot_col + i0 + 32 * k) : -1;
+    for (int k = 0; k < 4; ++k) col[k] = (k < cnt) ? slot_column(L, e0 + k, i0 + 32 * k, c) : -1;
 #pragma unroll
     for (int k = 0; k < 4; ++k) a[k] = (col[k] >= 0) ? __ldg(coef + i0 + 32 * k) : (T)0;
 #pragma unroll
@@ -35,7 +34,7 @@ __device__ __forceinline__ A slot_sum(const int32_t* __restrict__ slot_col,
   } else {
 #pragma unroll 4
     for (int k = 0; k < cnt; ++k) {
-      const int col = __ldg(slot_col + i0 + 32 * k);
+      const int col = slot_column(L, e0 + k, i0 + 32 * k, c);
       if (col >= 0) s = add_rn(s, (A)mul_rn(__ldg(coef + i0 + 32 * k), __ldg(x + col)));
     }
   }
@@ -50,8 +49,8 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
   A y = (A)mul_rn(__ldg(diag + c), xc);
   if (L.n_faces > 0) {
     const CellSlots cs = cell_slots(L, c);
-    const A so = slot_sum<T, A>(L.slot_col, coef, x, cs.base, cs.wo);
-    const A sn = slot_sum<T, A>(L.slot_col, coef, x, cs.base + 32 * cs.wo, cs.wn);
+    const A so = slot_sum<T, A>(L, coef, x, c, cs.base, cs.e0, cs.wo);
+    const A sn = slot_sum<T, A>(L, coef, x, c, cs.base + 32 * cs.wo, cs.e0 + cs.wo, cs.wn);
     if (NEI_FIRST) {
       y = add_rn(y, sn);
       y = add_rn(y, so);

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -41,6 +42,25 @@ constexpr int kBlock = 256;
 
 int check_layout(const gbf_layout* L);  // validates sizes / pointers
 
+// Resident blocks per SM of a kernel at block size `block` (cached per
+// kernel and device); 0 on error.
+int resident_blocks(const void* kernel, int block);
+
+// Grid of a grid-stride kernel: one full wave of resident blocks, no more
+// blocks than there are `block`-sized chunks of work, at most kMaxGrid.
+template <typename K>
+inline int wave_grid(K kernel, int block, long long work) {
+  int per_sm = resident_blocks(reinterpret_cast<const void*>(kernel), block);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long g = (long long)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  const long long need = (work + block - 1) / block;
+  if (g > need) g = need;
+  if (g > 4096) g = 4096;
+  return g < 1 ? 1 : (int)g;
+}
+
 // Kernel timing probes (gbf_timing_enable): timing_begin returns true when
 // an event was recorded; the caller then calls timing_end after the launch.
 constexpr int kNumProbes = 4;
@@ -57,16 +77,30 @@ struct CellSlots {
   int base;  // slot of k = 0 for this lane
   int wo;    // owner-side slot count of the slice
   int wn;    // neighbour-side slot count of the slice
+  int e0;    // compressed-offset entry of k = 0 (slice_off / 32)
 };
 
 __device__ __forceinline__ CellSlots cell_slots(const gbf_layout& L, int c) {
   const int s = c >> 5;
   const int w = __ldg(L.slice_w + s);
+  const int off = __ldg(L.slice_off + s);
   CellSlots r;
-  r.base = __ldg(L.slice_off + s) + (c & 31);
+  r.base = off + (c & 31);
   r.wo = w & 0xffff;
   r.wn = w >> 16;
+  r.e0 = off >> 5;
   return r;
+}
+
+// Column of slot k (absolute entry index e = e0 + k, slot index i) of cell
+// c: from the compressed offset when the slot is uniform across the slice,
+// else from slot_col.  -1 marks padding.
+__device__ __forceinline__ int slot_column(const gbf_layout& L, int e, int i, int c) {
+  if (L.slot_delta != nullptr) {
+    const int d = __ldg(L.slot_delta + e);
+    if (d != INT_MIN) return ((__ldg(L.slot_mask + e) >> (c & 31)) & 1u) ? c + d : -1;
+  }
+  return __ldg(L.slot_col + i);
 }
 
 // --------------------------------------------------------------------------

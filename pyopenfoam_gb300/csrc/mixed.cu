@@ -153,6 +153,9 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// Four cells per thread with 128-bit loads and stores of the FP32 vectors
+// (the workspace vectors are 256-byte aligned); the n % 4 tail cells are
+// handled one per thread.
 __global__ void __launch_bounds__(kBlock)
     mp_update_kernel(int n, double* __restrict__ x, MixedVecs v, double delta,
                      gbf_solve_params P) {
@@ -162,7 +165,51 @@ __global__ void __launch_bounds__(kBlock)
   const float alpha = (float)v.st->alpha;
   const bool fold = v.st->fold_pending != 0;
   DFAcc arr, arz;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += G * blockDim.x) {
+  const int n4 = n >> 2;
+  const int stride = G * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  float4* __restrict__ xlo4 = reinterpret_cast<float4*>(v.xlo);
+  float4* __restrict__ r4 = reinterpret_cast<float4*>(v.r);
+  float4* __restrict__ z4 = reinterpret_cast<float4*>(v.z);
+  const float4* __restrict__ p4 = reinterpret_cast<const float4*>(v.p);
+  const float4* __restrict__ ap4 = reinterpret_cast<const float4*>(v.Ap);
+  const float4* __restrict__ rd4 = reinterpret_cast<const float4*>(v.rD);
+  for (int q = tid; q < n4; q += stride) {
+    const float4 pp = p4[q], ap = ap4[q], rd = __ldg(rd4 + q);
+    float4 xl = xlo4[q], r = r4[q], z;
+    xl.x = fmaf(alpha, pp.x, xl.x);
+    xl.y = fmaf(alpha, pp.y, xl.y);
+    xl.z = fmaf(alpha, pp.z, xl.z);
+    xl.w = fmaf(alpha, pp.w, xl.w);
+    if (fold) {
+      const int c = 4 * q;
+      x[c] += (double)xl.x;
+      x[c + 1] += (double)xl.y;
+      x[c + 2] += (double)xl.z;
+      x[c + 3] += (double)xl.w;
+      xl = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    xlo4[q] = xl;
+    r.x = fmaf(-alpha, ap.x, r.x);
+    r.y = fmaf(-alpha, ap.y, r.y);
+    r.z = fmaf(-alpha, ap.z, r.z);
+    r.w = fmaf(-alpha, ap.w, r.w);
+    z.x = rd.x * r.x;
+    z.y = rd.y * r.y;
+    z.z = rd.z * r.z;
+    z.w = rd.w * r.w;
+    r4[q] = r;
+    z4[q] = z;
+    arr.add_prod(r.x, r.x);
+    arr.add_prod(r.y, r.y);
+    arr.add_prod(r.z, r.z);
+    arr.add_prod(r.w, r.w);
+    arz.add_prod(r.x, z.x);
+    arz.add_prod(r.y, z.y);
+    arz.add_prod(r.z, z.z);
+    arz.add_prod(r.w, z.w);
+  }
+  for (int c = 4 * n4 + tid; c < n; c += stride) {
     const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
     if (fold) {
       x[c] += (double)xl;
@@ -258,8 +305,21 @@ __global__ void __launch_bounds__(kBlock)
 __global__ void __launch_bounds__(kBlock) mp_p_kernel(int n, MixedVecs v) {
   if (v.st->status != GBF_RUNNING) return;
   const float beta = (float)v.st->beta;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-    v.p[c] = fmaf(beta, v.p[c], v.z[c]);
+  const int n4 = n >> 2;
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  float4* __restrict__ p4 = reinterpret_cast<float4*>(v.p);
+  const float4* __restrict__ z4 = reinterpret_cast<const float4*>(v.z);
+  for (int q = tid; q < n4; q += stride) {
+    float4 p = p4[q];
+    const float4 z = z4[q];
+    p.x = fmaf(beta, p.x, z.x);
+    p.y = fmaf(beta, p.y, z.y);
+    p.z = fmaf(beta, p.z, z.z);
+    p.w = fmaf(beta, p.w, z.w);
+    p4[q] = p;
+  }
+  for (int c = 4 * n4 + tid; c < n; c += stride) v.p[c] = fmaf(beta, v.p[c], v.z[c]);
 }
 
 // Folds any remaining FP32 correction into x (breakdown / iteration limit;
@@ -316,11 +376,15 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   v.partials = reinterpret_cast<double*>(w + 7 * vb);
   v.st = reinterpret_cast<MixedState*>(w + 7 * vb + a256(sizeof(double) * 2 * kMaxGrid));
 
-  int G = reduction_grid();
-  const int need = (n + kBlock - 1) / kBlock;
-  if (G > need) G = need;
+  // one full wave of resident blocks per kernel (each reduces its own partials)
+  const int Gi = wave_grid(mp_init_kernel, kBlock, n);
+  const int Ga = wave_grid(mp_ap_kernel, kBlock, n);
+  const int Gu = wave_grid(mp_update_kernel, kBlock, (n + 3) / 4);
+  const int Gt = wave_grid(mp_true_kernel, kBlock, n);
+  const int Gp = wave_grid(mp_p_kernel, kBlock, (n + 3) / 4);
+  const int G = wave_grid(mp_fold_kernel, kBlock, n);
   GBF_CHECK_CUDA(cudaMemsetAsync(v.st, 0, sizeof(MixedState), s));
-  mp_init_kernel<<<G, kBlock, 0, s>>>(*L, coef64, diag64, pd, b, x, v, hist, *P);
+  mp_init_kernel<<<Gi, kBlock, 0, s>>>(*L, coef64, diag64, pd, b, x, v, hist, *P);
   GBF_CHECK_LAUNCH();
   const int chunk = P->check_every > 0 ? P->check_every : 32;
   MixedState hs;
@@ -333,11 +397,11 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   while (hs.status == GBF_RUNNING && launched < limit) {
     for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
       const bool tb = timing_begin(kProbeMixedAp, s);
-      mp_ap_kernel<<<G, kBlock, 0, s>>>(*L, coef32, v);
+      mp_ap_kernel<<<Ga, kBlock, 0, s>>>(*L, coef32, v);
       if (tb) timing_end(kProbeMixedAp, s);
-      mp_update_kernel<<<G, kBlock, 0, s>>>(n, x, v, delta, *P);
-      mp_true_kernel<<<G, kBlock, 0, s>>>(*L, coef64, diag64, b, x, v, hist, hist_cap, *P);
-      mp_p_kernel<<<G, kBlock, 0, s>>>(n, v);
+      mp_update_kernel<<<Gu, kBlock, 0, s>>>(n, x, v, delta, *P);
+      mp_true_kernel<<<Gt, kBlock, 0, s>>>(*L, coef64, diag64, b, x, v, hist, hist_cap, *P);
+      mp_p_kernel<<<Gp, kBlock, 0, s>>>(n, v);
     }
     GBF_CHECK_LAUNCH();
     GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));

@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
 #include <vector>
 
 #include "gbfoam.h"
@@ -275,5 +276,55 @@ extern "C" int gbf_sweep_schedule(int32_t n, int32_t nf, const int32_t* own, con
   *n_levels = nl;
   *max_level_size = mx;
   (void)used;
+  return GBF_OK;
+}
+
+// Offset compression of the slot columns.  For every (slice, slot) the 32
+// lanes' columns are stored as one offset `delta` (column = cell + delta)
+// plus a 32-bit mask of the lanes that hold a face, whenever all those
+// lanes share the same offset -- the common case on meshes whose cells are
+// numbered along a structured direction (a hex mesh has offsets +-1, +-nx,
+// +-nx*ny).  Otherwise delta = INT32_MIN and the kernels read slot_col.
+// Entry (s, k) lives at slice_off[s] / 32 + k, so both arrays hold
+// n_slots / 32 entries: 8 bytes per 32 slots instead of 128.
+extern "C" int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off,
+                                   const int32_t* slice_w, const int32_t* slot_col,
+                                   int32_t* slot_delta, uint32_t* slot_mask,
+                                   int64_t* n_uniform) {
+  if (n_slices < 0 || !slice_off || !slice_w || !slot_col || !slot_delta || !slot_mask) {
+    gbf::set_error("layout_compress: bad arguments");
+    return GBF_ERR_ARG;
+  }
+  int64_t uni = 0;
+  for (int32_t s = 0; s < n_slices; ++s) {
+    const int32_t w = (slice_w[s] & 0xffff) + (slice_w[s] >> 16);
+    const int64_t e0 = slice_off[s] / 32;
+    for (int32_t k = 0; k < w; ++k) {
+      const int64_t base = (int64_t)slice_off[s] + 32 * (int64_t)k;
+      uint32_t mask = 0;
+      bool uniform = true, have = false;
+      int64_t d = 0;
+      for (int32_t l = 0; l < 32; ++l) {
+        const int32_t col = slot_col[base + l];
+        if (col < 0) continue;
+        const int64_t dl = (int64_t)col - ((int64_t)s * 32 + l);
+        if (!have) {
+          d = dl;
+          have = true;
+        } else if (dl != d) {
+          uniform = false;
+        }
+        mask |= 1u << l;
+      }
+      if (uniform && have && d > INT32_MIN && d <= INT32_MAX) {
+        slot_delta[e0 + k] = (int32_t)d;
+        ++uni;
+      } else {
+        slot_delta[e0 + k] = INT32_MIN;
+      }
+      slot_mask[e0 + k] = mask;
+    }
+  }
+  if (n_uniform) *n_uniform = uni;
   return GBF_OK;
 }

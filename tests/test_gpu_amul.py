@@ -139,3 +139,24 @@ def test_full_size_bitwise_against_oracle(N):
     y = m.Ax(torch.as_tensor(x)).cpu().numpy()
     ref = O.amul(own, nei, diag, lower, upper, x)
     assert (bits(y) == bits(ref)).all()
+
+
+def test_offset_compression_gives_identical_bits():
+    from pyopenfoam_gb300 import _lib
+
+    for perm in (False, True):
+        c = random_ldu(20, 13, perm)
+        m = mat(c["n"], c["owner"], c["neighbour"], c["diag"], c["lower"], c["upper"])
+        topo = m.topology()
+        x = torch.as_tensor(c["x"]).cuda()
+        y1 = m.Ax(x)
+        plain = topo.uncompressed_layout()
+        y2 = torch.empty_like(y1)
+        import ctypes
+
+        _lib.check(_lib.lib().gbf_amul_f64(ctypes.byref(plain), m.packed().data_ptr(),
+                                           m.diag.data_ptr(), x.data_ptr(), y2.data_ptr(), 0,
+                                           torch.cuda.current_stream().cuda_stream))
+        assert (bits(y1.cpu().numpy()) == bits(y2.cpu().numpy())).all()
+        if not perm:
+            assert topo.n_uniform_entries > 0.9 * topo.n_slots // 32
