@@ -81,23 +81,89 @@ void bucket_by_level(int32_t n_items, const std::vector<int32_t>& level, int32_t
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Slot assignment of one slice side (owner- or neighbour-side faces of its
+// 32 cells).  Each lane's faces, in ascending face order, carry the column
+// offset d = column - cell.  The slots of the slice form one sequence of
+// offsets M, built so that every lane's offset sequence is a subsequence of
+// M (greedy merge); a lane's faces then go to the slots where their offsets
+// sit in M, in order, and the other slots of that lane are holes.  Every
+// cell still visits its faces in ascending face order (the reference's
+// summation order), and every slot holds one offset for the whole slice,
+// which the offset compression below stores once.  If merging would widen
+// the side by more than 4 slots over the densest lane, the side falls back
+// to the dense assignment (k-th face in slot k).
+// ---------------------------------------------------------------------------
+struct SideLists {
+  std::vector<int64_t> ptr;    // per cell, into face
+  std::vector<int32_t> face;   // ascending face order per cell
+};
+
+static void side_lists(int32_t n, int32_t nf, const int32_t* key, SideLists& L) {
+  L.ptr.assign((size_t)n + 1, 0);
+  for (int32_t f = 0; f < nf; ++f) L.ptr[(size_t)key[f] + 1]++;
+  for (int32_t c = 0; c < n; ++c) L.ptr[c + 1] += L.ptr[c];
+  L.face.resize((size_t)nf);
+  std::vector<int64_t> cur(L.ptr.begin(), L.ptr.end() - 1);
+  for (int32_t f = 0; f < nf; ++f) L.face[cur[key[f]]++] = f;
+}
+
+// Slots of the faces of slice s on one side: slot_of[k] for the k-th face
+// (in cell-major, ascending-face order) of the slice; returns the width.
+static int32_t assign_side(int32_t s, int32_t n, const SideLists& L, const int32_t* other,
+                           std::vector<int32_t>& slot_of) {
+  const int32_t c0 = s * 32, c1 = std::min(n, c0 + 32);
+  int32_t dense = 0;
+  for (int32_t c = c0; c < c1; ++c) dense = std::max<int32_t>(dense, (int32_t)(L.ptr[c + 1] - L.ptr[c]));
+  std::vector<int64_t> M;
+  for (int32_t c = c0; c < c1; ++c) {
+    size_t pos = 0;
+    for (int64_t k = L.ptr[c]; k < L.ptr[c + 1]; ++k) {
+      const int64_t d = (int64_t)other[L.face[k]] - c;
+      size_t j = pos;
+      while (j < M.size() && M[j] != d) ++j;
+      if (j == M.size()) {
+        M.insert(M.begin() + (long)pos, d);
+        j = pos;
+      }
+      pos = j + 1;
+    }
+  }
+  slot_of.clear();
+  if ((int32_t)M.size() > dense + 4) {  // irregular slice: dense slots
+    for (int32_t c = c0; c < c1; ++c)
+      for (int64_t k = L.ptr[c]; k < L.ptr[c + 1]; ++k) slot_of.push_back((int32_t)(k - L.ptr[c]));
+    return dense;
+  }
+  for (int32_t c = c0; c < c1; ++c) {
+    size_t pos = 0;
+    for (int64_t k = L.ptr[c]; k < L.ptr[c + 1]; ++k) {
+      const int64_t d = (int64_t)other[L.face[k]] - c;
+      size_t j = pos;
+      while (M[j] != d) ++j;  // an embedding exists by construction
+      slot_of.push_back((int32_t)j);
+      pos = j + 1;
+    }
+  }
+  return (int32_t)M.size();
+}
+
 extern "C" int gbf_layout_plan(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
                                int32_t* n_slices, int64_t* n_slots, int32_t* max_width) {
   int rc = check_faces(n, nf, own, nei);
   if (rc) return rc;
-  std::vector<int32_t> co, cn;
-  face_counts(n, nf, own, nei, co, cn);
+  SideLists lo, ln;
+  side_lists(n, nf, own, lo);
+  side_lists(n, nf, nei, ln);
   const int32_t ns = (n + 31) / 32;
   int64_t slots = 0;
   int32_t mw = 0;
+  std::vector<int32_t> tmp;
   for (int32_t s = 0; s < ns; ++s) {
-    int32_t wo = 0, wn = 0;
-    for (int32_t c = s * 32; c < std::min(n, s * 32 + 32); ++c) {
-      wo = std::max(wo, co[c]);
-      wn = std::max(wn, cn[c]);
-    }
+    const int32_t wo = assign_side(s, n, lo, nei, tmp);
+    const int32_t wn = assign_side(s, n, ln, own, tmp);
     if (wo > 0xffff || wn > 0x7fff) {
-      gbf::set_error("a cell has more than 32767 faces");
+      gbf::set_error("a slice needs more than 32767 slots");
       return GBF_ERR_ARG;
     }
     slots += 32 * (int64_t)(wo + wn);
@@ -118,47 +184,41 @@ extern "C" int gbf_layout_fill(int32_t n, int32_t nf, const int32_t* own, const 
                                int32_t* slot_face) {
   int rc = check_faces(n, nf, own, nei);
   if (rc) return rc;
-  std::vector<int32_t> co, cn;
-  face_counts(n, nf, own, nei, co, cn);
+  SideLists lo, ln;
+  side_lists(n, nf, own, lo);
+  side_lists(n, nf, nei, ln);
   const int32_t ns = (n + 31) / 32;
   int64_t off = 0;
+  std::vector<int32_t> so, sn;
   for (int32_t s = 0; s < ns; ++s) {
-    int32_t wo = 0, wn = 0;
-    for (int32_t c = s * 32; c < std::min(n, s * 32 + 32); ++c) {
-      wo = std::max(wo, co[c]);
-      wn = std::max(wn, cn[c]);
-    }
+    const int32_t wo = assign_side(s, n, lo, nei, so);
+    const int32_t wn = assign_side(s, n, ln, own, sn);
     slice_off[s] = (int32_t)off;
     slice_w[s] = wo | (wn << 16);
+    for (int64_t i = off; i < off + 32 * (int64_t)(wo + wn); ++i) {
+      slot_col[i] = -1;
+      slot_face[i] = -1;
+    }
+    const int32_t c0 = s * 32, c1 = std::min(n, c0 + 32);
+    size_t qo = 0, qn = 0;
+    for (int32_t c = c0; c < c1; ++c) {
+      const int32_t lane = c & 31;
+      for (int64_t k = lo.ptr[c]; k < lo.ptr[c + 1]; ++k) {
+        const int32_t f = lo.face[k];
+        const int64_t slot = off + 32 * (int64_t)so[qo++] + lane;
+        slot_col[slot] = nei[f];
+        slot_face[slot] = f;
+      }
+      for (int64_t k = ln.ptr[c]; k < ln.ptr[c + 1]; ++k) {
+        const int32_t f = ln.face[k];
+        const int64_t slot = off + 32 * (int64_t)(wo + sn[qn++]) + lane;
+        slot_col[slot] = own[f];
+        slot_face[slot] = f;
+      }
+    }
     off += 32 * (int64_t)(wo + wn);
   }
   slice_off[ns] = (int32_t)off;
-  for (int64_t i = 0; i < off; ++i) {
-    slot_col[i] = -1;
-    slot_face[i] = -1;
-  }
-  // faces visited in ascending order: the k-th owner-side (neighbour-side)
-  // face of a cell goes to its k-th owner (neighbour) slot
-  std::vector<int32_t> ko((size_t)n, 0), kn((size_t)n, 0);
-  for (int32_t f = 0; f < nf; ++f) {
-    {
-      const int32_t c = own[f];
-      const int32_t s = c >> 5;
-      const int64_t slot = (int64_t)slice_off[s] + 32 * (int64_t)ko[c] + (c & 31);
-      ko[c]++;
-      slot_col[slot] = nei[f];
-      slot_face[slot] = f;
-    }
-    {
-      const int32_t c = nei[f];
-      const int32_t s = c >> 5;
-      const int32_t wo = slice_w[s] & 0xffff;
-      const int64_t slot = (int64_t)slice_off[s] + 32 * (int64_t)(wo + kn[c]) + (c & 31);
-      kn[c]++;
-      slot_col[slot] = own[f];
-      slot_face[slot] = f;
-    }
-  }
   return GBF_OK;
 }
 
