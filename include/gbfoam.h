@@ -63,9 +63,9 @@ typedef struct gbf_layout {
   const int32_t* slot_face;/* [n_slots]   face of the slot, -1 = padding       */
   const int32_t* owner;    /* [n_faces]   face-order owner (int32)             */
   const int32_t* neighbour;/* [n_faces]   face-order neighbour (int32)         */
-  /* optional offset compression (gbf_layout_compress); NULL = use slot_col */
-  const int32_t* slot_delta; /* [n_slots/32] column - cell, or INT32_MIN   */
-  const uint32_t* slot_mask; /* [n_slots/32] lanes that hold a face        */
+  /* optional offset compression (gbf_layout_compress); NULL = use slot_col:
+   * per (slice, slot) {column - cell or INT32_MIN, mask of lanes with a face} */
+  const int32_t* slot_dm;    /* [2 * n_slots/32]                            */
 } gbf_layout;
 
 /* ---- library ----------------------------------------------------------- */
@@ -97,10 +97,10 @@ int gbf_layout_fill(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
  * a lane mask when all lanes share the offset (INT32_MIN otherwise);
  * entry (s, k) at slice_off[s]/32 + k.  Kernels give identical results with
  * or without it; it removes most of the index traffic on structured
- * numberings.  n_uniform_h receives the number of compressed entries.      */
+ * numberings.  slot_dm_h holds 2 * n_slots/32 int32: {delta, mask} per
+ * entry.  n_uniform_h receives the number of compressed entries.           */
 int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off_h, const int32_t* slice_w_h,
-                        const int32_t* slot_col_h, int32_t* slot_delta_h, uint32_t* slot_mask_h,
-                        int64_t* n_uniform_h);
+                        const int32_t* slot_col_h, int32_t* slot_dm_h, int64_t* n_uniform_h);
 /* DIC wavefront: level(c) = 1 + max level of the cells j < c that c reads in
  * the reference's cell-ordered factorisation (preconditioners.py:124-128).
  * level_ptr_h has room for n_cells + 1 entries, level_cells_h for n_cells. */

@@ -55,8 +55,7 @@ class Layout(ctypes.Structure):
         ("slot_face", _c_vp),
         ("owner", _c_vp),
         ("neighbour", _c_vp),
-        ("slot_delta", _c_vp),
-        ("slot_mask", _c_vp),
+        ("slot_dm", _c_vp),
     ]
 
 
@@ -109,8 +108,7 @@ EXPORTED: dict[str, tuple] = {
     "gbf_timing_read": (ctypes.c_int, [_c_i32, _P(_c_i32), _P(_c_dbl)]),
     "gbf_layout_plan": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _P(_c_i32), _P(_c_i64), _P(_c_i32)]),
     "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
-    "gbf_layout_compress": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
-                                           _P(_c_i64)]),
+    "gbf_layout_compress": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i64)]),
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_sweep_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,

@@ -87,21 +87,18 @@ class Topology:
         self.neighbour32 = to(self._nei_h) if self.n_faces else torch.zeros(1, dtype=torch.int32, device=dev)
         # offset compression of the columns (identical results, less index traffic)
         nent = max(self.n_slots // 32, 1)
-        sd = np.empty(nent, np.int32)
-        sm = np.empty(nent, np.uint32)
+        dm = np.empty(2 * nent, np.int32)
         nu = ctypes.c_int64()
         check(L.gbf_layout_compress(self.n_slices, off.ctypes.data, w.ctypes.data,
-                                    col.ctypes.data, sd.ctypes.data, sm.ctypes.data,
-                                    ctypes.byref(nu)), "gbf_layout_compress")
+                                    col.ctypes.data, dm.ctypes.data, ctypes.byref(nu)),
+              "gbf_layout_compress")
         self.n_uniform_entries = nu.value
-        self.slot_delta = to(sd)
-        self.slot_mask = to(sm.view(np.int32))
+        self.slot_dm = to(dm)
         self.layout = Layout(
             self.n_cells, self.n_faces, self.n_slices, self.max_width, self.n_slots,
             self.slice_off.data_ptr(), self.slice_w.data_ptr(), self.slot_col.data_ptr(),
             self.slot_face.data_ptr(), self.owner32.data_ptr(), self.neighbour32.data_ptr(),
-            self.slot_delta.data_ptr() if self.compress else None,
-            self.slot_mask.data_ptr() if self.compress else None,
+            self.slot_dm.data_ptr() if self.compress else None,
         )
         self._dic: Schedule | None = None
         self._dilu: Schedule | None = None
@@ -115,8 +112,7 @@ class Topology:
         """The same layout without the offset compression (slot_col only)."""
         L = Layout()
         ctypes.pointer(L)[0] = self.layout
-        L.slot_delta = None
-        L.slot_mask = None
+        L.slot_dm = None
         return L
 
     def dic_schedule(self) -> Schedule:

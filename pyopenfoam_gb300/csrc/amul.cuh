@@ -24,8 +24,10 @@ __device__ __forceinline__ A slot_sum(const gbf_layout& L, const T* __restrict__
     T a[4], xv[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) col[k] = (k < cnt) ? slot_column(L, e0 + k, i0 + 32 * k, c) : -1;
+    // coefficients do not wait for the columns: every slot k < cnt exists
+    // (holes hold 0), so the loads are issued together with the columns'
 #pragma unroll
-    for (int k = 0; k < 4; ++k) a[k] = (col[k] >= 0) ? __ldg(coef + i0 + 32 * k) : (T)0;
+    for (int k = 0; k < 4; ++k) a[k] = (k < cnt) ? __ldg(coef + i0 + 32 * k) : (T)0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
 #pragma unroll
@@ -49,8 +51,35 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
   A y = (A)mul_rn(__ldg(diag + c), xc);
   if (L.n_faces > 0) {
     const CellSlots cs = cell_slots(L, c);
-    const A so = slot_sum<T, A>(L, coef, x, c, cs.base, cs.e0, cs.wo);
-    const A sn = slot_sum<T, A>(L, coef, x, c, cs.base + 32 * cs.wo, cs.e0 + cs.wo, cs.wn);
+    A so = (A)0, sn = (A)0;
+    if (cs.wo <= 4 && cs.wn <= 4) {
+      // both sides in one predicated block: every column, coefficient and x
+      // load of the cell is in flight at once
+      int col[8];
+      T a[8], xv[8];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        col[k] = (k < cs.wo) ? slot_column(L, cs.e0 + k, cs.base + 32 * k, c) : -1;
+        col[4 + k] = (k < cs.wn) ? slot_column(L, cs.e0 + cs.wo + k,
+                                               cs.base + 32 * (cs.wo + k), c) : -1;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        a[k] = (k < cs.wo) ? __ldg(coef + cs.base + 32 * k) : (T)0;
+        a[4 + k] = (k < cs.wn) ? __ldg(coef + cs.base + 32 * (cs.wo + k)) : (T)0;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (col[k] >= 0) so = add_rn(so, (A)mul_rn(a[k], xv[k]));
+#pragma unroll
+      for (int k = 4; k < 8; ++k)
+        if (col[k] >= 0) sn = add_rn(sn, (A)mul_rn(a[k], xv[k]));
+    } else {
+      so = slot_sum<T, A>(L, coef, x, c, cs.base, cs.e0, cs.wo);
+      sn = slot_sum<T, A>(L, coef, x, c, cs.base + 32 * cs.wo, cs.e0 + cs.wo, cs.wn);
+    }
     if (NEI_FIRST) {
       y = add_rn(y, sn);
       y = add_rn(y, so);

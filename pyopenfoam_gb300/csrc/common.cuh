@@ -96,9 +96,9 @@ __device__ __forceinline__ CellSlots cell_slots(const gbf_layout& L, int c) {
 // c: from the compressed offset when the slot is uniform across the slice,
 // else from slot_col.  -1 marks padding.
 __device__ __forceinline__ int slot_column(const gbf_layout& L, int e, int i, int c) {
-  if (L.slot_delta != nullptr) {
-    const int d = __ldg(L.slot_delta + e);
-    if (d != INT_MIN) return ((__ldg(L.slot_mask + e) >> (c & 31)) & 1u) ? c + d : -1;
+  if (L.slot_dm != nullptr) {
+    const int2 dm = __ldg(reinterpret_cast<const int2*>(L.slot_dm) + e);
+    if (dm.x != INT_MIN) return (((unsigned)dm.y >> (c & 31)) & 1u) ? c + dm.x : -1;
   }
   return __ldg(L.slot_col + i);
 }

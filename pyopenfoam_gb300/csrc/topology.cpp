@@ -345,13 +345,12 @@ extern "C" int gbf_sweep_schedule(int32_t n, int32_t nf, const int32_t* own, con
 // lanes share the same offset -- the common case on meshes whose cells are
 // numbered along a structured direction (a hex mesh has offsets +-1, +-nx,
 // +-nx*ny).  Otherwise delta = INT32_MIN and the kernels read slot_col.
-// Entry (s, k) lives at slice_off[s] / 32 + k, so both arrays hold
-// n_slots / 32 entries: 8 bytes per 32 slots instead of 128.
+// Entry (s, k) lives at slice_off[s] / 32 + k as the int32 pair
+// {delta, mask}: 8 bytes per 32 slots instead of 128.
 extern "C" int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off,
                                    const int32_t* slice_w, const int32_t* slot_col,
-                                   int32_t* slot_delta, uint32_t* slot_mask,
-                                   int64_t* n_uniform) {
-  if (n_slices < 0 || !slice_off || !slice_w || !slot_col || !slot_delta || !slot_mask) {
+                                   int32_t* slot_dm, int64_t* n_uniform) {
+  if (n_slices < 0 || !slice_off || !slice_w || !slot_col || !slot_dm) {
     gbf::set_error("layout_compress: bad arguments");
     return GBF_ERR_ARG;
   }
@@ -377,12 +376,12 @@ extern "C" int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off,
         mask |= 1u << l;
       }
       if (uniform && have && d > INT32_MIN && d <= INT32_MAX) {
-        slot_delta[e0 + k] = (int32_t)d;
+        slot_dm[2 * (e0 + k)] = (int32_t)d;
         ++uni;
       } else {
-        slot_delta[e0 + k] = INT32_MIN;
+        slot_dm[2 * (e0 + k)] = INT32_MIN;
       }
-      slot_mask[e0 + k] = mask;
+      slot_dm[2 * (e0 + k) + 1] = (int32_t)mask;
     }
   }
   if (n_uniform) *n_uniform = uni;

@@ -184,11 +184,11 @@ def test_layout_offset_compression_reproduces_columns(perm):
     off, w, col, face, mw = _layout(n, own, nei)
     ns = off.shape[0] - 1
     ne = max(col.shape[0] // 32, 1)
-    sd = np.empty(ne, np.int32)
-    sm = np.empty(ne, np.uint32)
+    dm = np.empty(2 * ne, np.int32)
     nu = ctypes.c_int64()
     _lib.check(_lib.lib().gbf_layout_compress(ns, off.ctypes.data, w.ctypes.data, col.ctypes.data,
-                                              sd.ctypes.data, sm.ctypes.data, ctypes.byref(nu)))
+                                              dm.ctypes.data, ctypes.byref(nu)))
+    sd, sm = dm[0::2], dm[1::2].view(np.uint32)
     for s in range(ns):
         width = (w[s] & 0xFFFF) + (w[s] >> 16)
         for k in range(width):
