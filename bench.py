@@ -216,6 +216,7 @@ def time_amul(m, dev, reps=20):
     import ctypes
 
     plain = topo.uncompressed_layout()
+    var = topo.variable_width_layout()
     fns = {
         "f64": lambda: L.gbf_amul_f64(topo.layout_ref, coef64.data_ptr(), m.diag.data_ptr(),
                                       x.data_ptr(), y64.data_ptr(), 0, st.cuda_stream),
@@ -224,6 +225,9 @@ def time_amul(m, dev, reps=20):
         "f32_explicit_columns": lambda: L.gbf_amul_f32(ctypes.byref(plain), coef32.data_ptr(),
                                                        d32.data_ptr(), x32.data_ptr(),
                                                        y32.data_ptr(), 0, st.cuda_stream),
+        "f32_variable_width": lambda: L.gbf_amul_f32(ctypes.byref(var), coef32.data_ptr(),
+                                                     d32.data_ptr(), x32.data_ptr(),
+                                                     y32.data_ptr(), 0, st.cuda_stream),
     }
     for name, fn in fns.items():
         s = 8 if name == "f64" else 4

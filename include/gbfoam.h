@@ -56,6 +56,9 @@ typedef struct gbf_layout {
   int32_t n_faces;         /* internal faces                                   */
   int32_t n_slices;        /* ceil(n_cells / 32)                               */
   int32_t max_width;       /* max over slices of wo + wn                       */
+  int32_t uniform_wo;      /* > 0: every slice has wo = uniform_wo and
+                              wn = uniform_wn, slice_off[s] = 32*s*(wo+wn)  */
+  int32_t uniform_wn;
   int64_t n_slots;         /* total slots incl. padding                        */
   const int32_t* slice_off;/* [n_slices + 1]                                   */
   const int32_t* slice_w;  /* [n_slices]  wo | (wn << 16)                      */
@@ -87,12 +90,16 @@ int gbf_timing_read(int32_t probe, int32_t* launches, double* total_ms);
  * Replace the reference's per-call Python loops over faces
  * (solvers/preconditioners.py:116-122, :254-268) and CSR caching
  * (core/ldu_matrix.py:101-102, :336-343) with one O(n + F) host pass. */
+/* uniform_pad_pct >= 0: pad every slice to the widest slice's (wo, wn) when
+ * that adds at most uniform_pad_pct percent slots (then *uniform = 1 and
+ * the kernels compute slot addresses without reading slice_off/slice_w);
+ * < 0 never.  plan and fill must get the same value.                       */
 int gbf_layout_plan(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
-                    const int32_t* neighbour_h, int32_t* n_slices, int64_t* n_slots,
-                    int32_t* max_width);
+                    const int32_t* neighbour_h, int32_t uniform_pad_pct, int32_t* n_slices,
+                    int64_t* n_slots, int32_t* max_width, int32_t* uniform);
 int gbf_layout_fill(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
-                    const int32_t* neighbour_h, int32_t* slice_off_h, int32_t* slice_w_h,
-                    int32_t* slot_col_h, int32_t* slot_face_h);
+                    const int32_t* neighbour_h, int32_t uniform_pad_pct, int32_t* slice_off_h,
+                    int32_t* slice_w_h, int32_t* slot_col_h, int32_t* slot_face_h);
 /* Offset compression of slot_col: per (slice, slot) one column offset and
  * a lane mask when all lanes share the offset (INT32_MIN otherwise);
  * entry (s, k) at slice_off[s]/32 + k.  Kernels give identical results with

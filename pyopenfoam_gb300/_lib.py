@@ -48,6 +48,8 @@ class Layout(ctypes.Structure):
         ("n_faces", _c_i32),
         ("n_slices", _c_i32),
         ("max_width", _c_i32),
+        ("uniform_wo", _c_i32),
+        ("uniform_wn", _c_i32),
         ("n_slots", _c_i64),
         ("slice_off", _c_vp),
         ("slice_w", _c_vp),
@@ -106,8 +108,10 @@ EXPORTED: dict[str, tuple] = {
     "gbf_device_sm_count": (ctypes.c_int, [_P(_c_i32)]),
     "gbf_timing_enable": (ctypes.c_int, [_c_i32, _c_i32]),
     "gbf_timing_read": (ctypes.c_int, [_c_i32, _P(_c_i32), _P(_c_dbl)]),
-    "gbf_layout_plan": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _P(_c_i32), _P(_c_i64), _P(_c_i32)]),
-    "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_layout_plan": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _P(_c_i32),
+                                       _P(_c_i64), _P(_c_i32), _P(_c_i32)]),
+    "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp, _c_vp,
+                                       _c_vp]),
     "gbf_layout_compress": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i64)]),
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),

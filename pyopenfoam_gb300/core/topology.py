@@ -45,6 +45,9 @@ class Topology:
 
     #: use the per-slice column-offset compression in the gather kernels
     compress = True
+    #: pad all slices to one width when that costs at most this many percent
+    #: more slots (-1: never)
+    uniform_pad_pct = 5
 
     def __init__(self, n_cells: int, owner: torch.Tensor, neighbour: torch.Tensor) -> None:
         if n_cells < 0 or n_cells >= 2**31:
@@ -60,13 +63,14 @@ class Topology:
         self._own_h = _i32_host(owner, n_cells, "owner")
         self._nei_h = _i32_host(neighbour, n_cells, "neighbour")
         L = lib()
-        ns, nslots, mw = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        ns, nslots, mw, uni = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()
         check(
             L.gbf_layout_plan(self.n_cells, self.n_faces, self._own_h.ctypes.data,
-                              self._nei_h.ctypes.data, ctypes.byref(ns), ctypes.byref(nslots),
-                              ctypes.byref(mw)),
+                              self._nei_h.ctypes.data, self.uniform_pad_pct, ctypes.byref(ns),
+                              ctypes.byref(nslots), ctypes.byref(mw), ctypes.byref(uni)),
             "gbf_layout_plan",
         )
+        self.uniform = bool(uni.value)
         self.n_slices, self.n_slots, self.max_width = ns.value, nslots.value, mw.value
         off = np.empty(self.n_slices + 1, np.int32)
         w = np.empty(max(self.n_slices, 1), np.int32)
@@ -74,8 +78,8 @@ class Topology:
         face = np.empty(max(self.n_slots, 1), np.int32)
         check(
             L.gbf_layout_fill(self.n_cells, self.n_faces, self._own_h.ctypes.data,
-                              self._nei_h.ctypes.data, off.ctypes.data, w.ctypes.data,
-                              col.ctypes.data, face.ctypes.data),
+                              self._nei_h.ctypes.data, self.uniform_pad_pct, off.ctypes.data,
+                              w.ctypes.data, col.ctypes.data, face.ctypes.data),
             "gbf_layout_fill",
         )
         to = lambda a: torch.from_numpy(a).to(dev)  # noqa: E731
@@ -94,8 +98,10 @@ class Topology:
               "gbf_layout_compress")
         self.n_uniform_entries = nu.value
         self.slot_dm = to(dm)
+        uwo = int(w[0] & 0xFFFF) if self.uniform and self.n_slices else 0
+        uwn = int(w[0] >> 16) if self.uniform and self.n_slices else 0
         self.layout = Layout(
-            self.n_cells, self.n_faces, self.n_slices, self.max_width, self.n_slots,
+            self.n_cells, self.n_faces, self.n_slices, self.max_width, uwo, uwn, self.n_slots,
             self.slice_off.data_ptr(), self.slice_w.data_ptr(), self.slot_col.data_ptr(),
             self.slot_face.data_ptr(), self.owner32.data_ptr(), self.neighbour32.data_ptr(),
             self.slot_dm.data_ptr() if self.compress else None,
@@ -113,6 +119,15 @@ class Topology:
         L = Layout()
         ctypes.pointer(L)[0] = self.layout
         L.slot_dm = None
+        return L
+
+    def variable_width_layout(self) -> Layout:
+        """The same layout read through slice_off/slice_w (no fixed-width
+        address arithmetic)."""
+        L = Layout()
+        ctypes.pointer(L)[0] = self.layout
+        L.uniform_wo = 0
+        L.uniform_wn = 0
         return L
 
     def dic_schedule(self) -> Schedule:

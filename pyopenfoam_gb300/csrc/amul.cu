@@ -28,9 +28,8 @@ template <typename T, typename A, bool NEI_FIRST>
 __global__ void __launch_bounds__(kBlock)
     amul_kernel(gbf_layout L, const T* __restrict__ coef, const T* __restrict__ diag,
                 const T* __restrict__ x, A* __restrict__ y) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= L.n_cells) return;
-  y[c] = cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, __ldg(x + c));
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += gridDim.x * blockDim.x)
+    y[c] = cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, __ldg(x + c));
 }
 
 int check_layout(const gbf_layout* L) {
@@ -62,11 +61,13 @@ static int amul(const gbf_layout* L, const T* coef, const T* diag, const T* x, A
   if (rc) return rc;
   if (L->n_cells == 0) return GBF_OK;
   GBF_REQUIRE(diag && x && y && (L->n_faces == 0 || coef), "amul: NULL pointer");
-  const int grid = (L->n_cells + kBlock - 1) / kBlock;
-  if (nei_first)
+  if (nei_first) {
+    const int grid = wave_grid(amul_kernel<T, A, true>, kBlock, L->n_cells);
     amul_kernel<T, A, true><<<grid, kBlock, 0, as_stream(stream)>>>(*L, coef, diag, x, y);
-  else
+  } else {
+    const int grid = wave_grid(amul_kernel<T, A, false>, kBlock, L->n_cells);
     amul_kernel<T, A, false><<<grid, kBlock, 0, as_stream(stream)>>>(*L, coef, diag, x, y);
+  }
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }

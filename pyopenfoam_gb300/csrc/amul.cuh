@@ -92,3 +92,4 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
 }
 
 }  // namespace gbf
+

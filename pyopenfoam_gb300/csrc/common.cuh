@@ -82,9 +82,17 @@ struct CellSlots {
 
 __device__ __forceinline__ CellSlots cell_slots(const gbf_layout& L, int c) {
   const int s = c >> 5;
+  CellSlots r;
+  if (L.uniform_wo > 0 || L.uniform_wn > 0) {  // fixed widths: no metadata loads
+    const int w = L.uniform_wo + L.uniform_wn;
+    r.base = 32 * s * w + (c & 31);
+    r.wo = L.uniform_wo;
+    r.wn = L.uniform_wn;
+    r.e0 = s * w;
+    return r;
+  }
   const int w = __ldg(L.slice_w + s);
   const int off = __ldg(L.slice_off + s);
-  CellSlots r;
   r.base = off + (c & 31);
   r.wo = w & 0xffff;
   r.wn = w >> 16;

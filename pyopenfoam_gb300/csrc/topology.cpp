@@ -148,26 +148,59 @@ static int32_t assign_side(int32_t s, int32_t n, const SideLists& L, const int32
   return (int32_t)M.size();
 }
 
+// Widths of every slice side; decides uniform padding.
+static int plan_widths(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                       const SideLists& lo, const SideLists& ln, int32_t pad_pct,
+                       std::vector<int32_t>& wo, std::vector<int32_t>& wn, int32_t& uni_o,
+                       int32_t& uni_n) {
+  const int32_t ns = (n + 31) / 32;
+  wo.resize((size_t)ns);
+  wn.resize((size_t)ns);
+  std::vector<int32_t> tmp;
+  int64_t slots = 0;
+  int32_t mo = 0, mn = 0;
+  for (int32_t s = 0; s < ns; ++s) {
+    wo[s] = assign_side(s, n, lo, nei, tmp);
+    wn[s] = assign_side(s, n, ln, own, tmp);
+    if (wo[s] > 0xffff || wn[s] > 0x7fff) {
+      gbf::set_error("a slice needs more than 32767 slots");
+      return GBF_ERR_ARG;
+    }
+    slots += 32 * (int64_t)(wo[s] + wn[s]);
+    mo = std::max(mo, wo[s]);
+    mn = std::max(mn, wn[s]);
+  }
+  uni_o = uni_n = 0;
+  const int64_t uni_slots = 32 * (int64_t)ns * (mo + mn);
+  if (pad_pct >= 0 && ns > 0 && uni_slots * 100 <= slots * (100 + (int64_t)pad_pct)) {
+    uni_o = mo;
+    uni_n = mn;
+    for (int32_t s = 0; s < ns; ++s) {
+      wo[s] = mo;
+      wn[s] = mn;
+    }
+  }
+  return GBF_OK;
+}
+
 extern "C" int gbf_layout_plan(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
-                               int32_t* n_slices, int64_t* n_slots, int32_t* max_width) {
+                               int32_t pad_pct, int32_t* n_slices, int64_t* n_slots,
+                               int32_t* max_width, int32_t* uniform) {
   int rc = check_faces(n, nf, own, nei);
   if (rc) return rc;
   SideLists lo, ln;
   side_lists(n, nf, own, lo);
   side_lists(n, nf, nei, ln);
+  std::vector<int32_t> wo, wn;
+  int32_t uo, un;
+  rc = plan_widths(n, nf, own, nei, lo, ln, pad_pct, wo, wn, uo, un);
+  if (rc) return rc;
   const int32_t ns = (n + 31) / 32;
   int64_t slots = 0;
   int32_t mw = 0;
-  std::vector<int32_t> tmp;
   for (int32_t s = 0; s < ns; ++s) {
-    const int32_t wo = assign_side(s, n, lo, nei, tmp);
-    const int32_t wn = assign_side(s, n, ln, own, tmp);
-    if (wo > 0xffff || wn > 0x7fff) {
-      gbf::set_error("a slice needs more than 32767 slots");
-      return GBF_ERR_ARG;
-    }
-    slots += 32 * (int64_t)(wo + wn);
-    mw = std::max(mw, wo + wn);
+    slots += 32 * (int64_t)(wo[s] + wn[s]);
+    mw = std::max(mw, wo[s] + wn[s]);
   }
   if (slots >= ((int64_t)1 << 31)) {
     gbf::set_error("matrix needs %lld slots; the layout holds < 2^31", (long long)slots);
@@ -176,23 +209,29 @@ extern "C" int gbf_layout_plan(int32_t n, int32_t nf, const int32_t* own, const 
   *n_slices = ns;
   *n_slots = slots;
   *max_width = mw;
+  if (uniform) *uniform = uo > 0 || un > 0 ? 1 : 0;
   return GBF_OK;
 }
 
 extern "C" int gbf_layout_fill(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
-                               int32_t* slice_off, int32_t* slice_w, int32_t* slot_col,
-                               int32_t* slot_face) {
+                               int32_t pad_pct, int32_t* slice_off, int32_t* slice_w,
+                               int32_t* slot_col, int32_t* slot_face) {
   int rc = check_faces(n, nf, own, nei);
   if (rc) return rc;
   SideLists lo, ln;
   side_lists(n, nf, own, lo);
   side_lists(n, nf, nei, ln);
+  std::vector<int32_t> wos, wns;
+  int32_t uo, un;
+  rc = plan_widths(n, nf, own, nei, lo, ln, pad_pct, wos, wns, uo, un);
+  if (rc) return rc;
   const int32_t ns = (n + 31) / 32;
   int64_t off = 0;
   std::vector<int32_t> so, sn;
   for (int32_t s = 0; s < ns; ++s) {
-    const int32_t wo = assign_side(s, n, lo, nei, so);
-    const int32_t wn = assign_side(s, n, ln, own, sn);
+    assign_side(s, n, lo, nei, so);
+    assign_side(s, n, ln, own, sn);
+    const int32_t wo = wos[s], wn = wns[s];
     slice_off[s] = (int32_t)off;
     slice_w[s] = wo | (wn << 16);
     for (int64_t i = off; i < off + 32 * (int64_t)(wo + wn); ++i) {

@@ -158,5 +158,12 @@ def test_offset_compression_gives_identical_bits():
                                            m.diag.data_ptr(), x.data_ptr(), y2.data_ptr(), 0,
                                            torch.cuda.current_stream().cuda_stream))
         assert (bits(y1.cpu().numpy()) == bits(y2.cpu().numpy())).all()
+        # and through slice_off / slice_w instead of the fixed-width arithmetic
+        var = topo.variable_width_layout()
+        y3 = torch.empty_like(y1)
+        _lib.check(_lib.lib().gbf_amul_f64(ctypes.byref(var), m.packed().data_ptr(),
+                                           m.diag.data_ptr(), x.data_ptr(), y3.data_ptr(), 0,
+                                           torch.cuda.current_stream().cuda_stream))
+        assert (bits(y1.cpu().numpy()) == bits(y3.cpu().numpy())).all()
         if not perm:
-            assert topo.n_uniform_entries > 0.9 * topo.n_slots // 32
+            assert topo.uniform and topo.n_uniform_entries == topo.n_slots // 32

@@ -37,27 +37,32 @@ def test_library_exports_every_declared_symbol():
     assert L.gbf_version() >= 1
 
 
-def _layout(n, own, nei):
+def _layout(n, own, nei, pad=-1):
     L = _lib.lib()
     o = np.ascontiguousarray(own, np.int32)
     q = np.ascontiguousarray(nei, np.int32)
-    ns, nsl, mw = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
-    _lib.check(L.gbf_layout_plan(n, o.shape[0], o.ctypes.data, q.ctypes.data, ctypes.byref(ns),
-                                 ctypes.byref(nsl), ctypes.byref(mw)))
+    ns, nsl, mw, uni = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()
+    _lib.check(L.gbf_layout_plan(n, o.shape[0], o.ctypes.data, q.ctypes.data, pad,
+                                 ctypes.byref(ns), ctypes.byref(nsl), ctypes.byref(mw),
+                                 ctypes.byref(uni)))
     off = np.empty(ns.value + 1, np.int32)
     w = np.empty(max(ns.value, 1), np.int32)
     col = np.empty(max(nsl.value, 1), np.int32)
     face = np.empty(max(nsl.value, 1), np.int32)
-    _lib.check(L.gbf_layout_fill(n, o.shape[0], o.ctypes.data, q.ctypes.data, off.ctypes.data,
-                                 w.ctypes.data, col.ctypes.data, face.ctypes.data))
+    _lib.check(L.gbf_layout_fill(n, o.shape[0], o.ctypes.data, q.ctypes.data, pad,
+                                 off.ctypes.data, w.ctypes.data, col.ctypes.data,
+                                 face.ctypes.data))
     return off, w, col[: nsl.value], face[: nsl.value], mw.value
 
 
-@pytest.mark.parametrize("perm", [False, True])
-def test_layout_slots_follow_reference_face_order(perm):
+@pytest.mark.parametrize("perm,pad", [(False, -1), (True, -1), (False, 50), (True, 50)])
+def test_layout_slots_follow_reference_face_order(perm, pad):
     c = random_ldu(7, seed=3, permute_faces=perm)
     n, own, nei = c["n"], c["owner"], c["neighbour"]
-    off, w, col, face, mw = _layout(n, own, nei)
+    off, w, col, face, mw = _layout(n, own, nei, pad)
+    if pad >= 0 and not perm:
+        assert len(set(w.tolist())) == 1  # uniform widths
+        assert all(off[s] == 32 * s * ((w[0] & 0xFFFF) + (w[0] >> 16)) for s in range(len(w)))
     seen_own = np.zeros(own.shape[0], int)
     seen_nei = np.zeros(own.shape[0], int)
     for cell in range(n):
@@ -137,12 +142,12 @@ def test_topology_rejects_bad_addressing():
     o = np.array([0, 5], np.int32)
     q = np.array([1, 2], np.int32)
     a, b, c_ = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
-    rc = L.gbf_layout_plan(3, 2, o.ctypes.data, q.ctypes.data, ctypes.byref(a), ctypes.byref(b),
-                           ctypes.byref(c_))
+    rc = L.gbf_layout_plan(3, 2, o.ctypes.data, q.ctypes.data, 5, ctypes.byref(a),
+                           ctypes.byref(b), ctypes.byref(c_), None)
     assert rc == 4 and b"outside" in L.gbf_last_error()
     o = np.array([1], np.int32)
-    rc = L.gbf_layout_plan(3, 1, o.ctypes.data, o.ctypes.data, ctypes.byref(a), ctypes.byref(b),
-                           ctypes.byref(c_))
+    rc = L.gbf_layout_plan(3, 1, o.ctypes.data, o.ctypes.data, 5, ctypes.byref(a),
+                           ctypes.byref(b), ctypes.byref(c_), None)
     assert rc == 4 and b"owner == neighbour" in L.gbf_last_error()
 
 
