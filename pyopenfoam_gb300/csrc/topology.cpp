@@ -414,7 +414,10 @@ extern "C" int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off,
         }
         mask |= 1u << l;
       }
-      if (uniform && have && d > INT32_MIN && d <= INT32_MAX) {
+      if (!have) {  // a slot that is a hole in every lane
+        slot_dm[2 * (e0 + k)] = 0;
+        ++uni;
+      } else if (uniform && d > INT32_MIN && d <= INT32_MAX) {
         slot_dm[2 * (e0 + k)] = (int32_t)d;
         ++uni;
       } else {
