@@ -59,6 +59,8 @@ typedef struct gbf_layout {
   int32_t uniform_wo;      /* > 0: every slice has wo = uniform_wo and
                               wn = uniform_wn, slice_off[s] = 32*s*(wo+wn)  */
   int32_t uniform_wn;
+  int32_t all_uniform;     /* 1: slot_dm set and no entry is INT32_MIN      */
+  int32_t reserved;
   int64_t n_slots;         /* total slots incl. padding                        */
   const int32_t* slice_off;/* [n_slices + 1]                                   */
   const int32_t* slice_w;  /* [n_slices]  wo | (wn << 16)                      */

@@ -50,6 +50,8 @@ class Layout(ctypes.Structure):
         ("max_width", _c_i32),
         ("uniform_wo", _c_i32),
         ("uniform_wn", _c_i32),
+        ("all_uniform", _c_i32),
+        ("reserved", _c_i32),
         ("n_slots", _c_i64),
         ("slice_off", _c_vp),
         ("slice_w", _c_vp),

@@ -100,8 +100,10 @@ class Topology:
         self.slot_dm = to(dm)
         uwo = int(w[0] & 0xFFFF) if self.uniform and self.n_slices else 0
         uwn = int(w[0] >> 16) if self.uniform and self.n_slices else 0
+        all_uni = int(self.compress and self.n_uniform_entries == self.n_slots // 32)
         self.layout = Layout(
-            self.n_cells, self.n_faces, self.n_slices, self.max_width, uwo, uwn, self.n_slots,
+            self.n_cells, self.n_faces, self.n_slices, self.max_width, uwo, uwn, all_uni, 0,
+            self.n_slots,
             self.slice_off.data_ptr(), self.slice_w.data_ptr(), self.slot_col.data_ptr(),
             self.slot_face.data_ptr(), self.owner32.data_ptr(), self.neighbour32.data_ptr(),
             self.slot_dm.data_ptr() if self.compress else None,
@@ -119,6 +121,7 @@ class Topology:
         L = Layout()
         ctypes.pointer(L)[0] = self.layout
         L.slot_dm = None
+        L.all_uniform = 0
         return L
 
     def variable_width_layout(self) -> Layout:
@@ -128,6 +131,7 @@ class Topology:
         ctypes.pointer(L)[0] = self.layout
         L.uniform_wo = 0
         L.uniform_wn = 0
+        L.all_uniform = 0
         return L
 
     def dic_schedule(self) -> Schedule:

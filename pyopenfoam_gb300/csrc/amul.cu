@@ -24,12 +24,19 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
-template <typename T, typename A, bool NEI_FIRST>
+template <int KIND, typename T, typename A, bool NEI_FIRST>
 __global__ void __launch_bounds__(kBlock)
     amul_kernel(gbf_layout L, const T* __restrict__ coef, const T* __restrict__ diag,
                 const T* __restrict__ x, A* __restrict__ y) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += gridDim.x * blockDim.x)
-    y[c] = cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, __ldg(x + c));
+    y[c] = cell_amul_k<KIND, T, A, NEI_FIRST>(L, coef, diag, x, c, __ldg(x + c));
+}
+
+template <int KIND, typename T, typename A, bool NEI_FIRST>
+static void launch_amul(const gbf_layout* L, const T* coef, const T* diag, const T* x, A* y,
+                        cudaStream_t s) {
+  const int grid = wave_grid(amul_kernel<KIND, T, A, NEI_FIRST>, kBlock, L->n_cells);
+  amul_kernel<KIND, T, A, NEI_FIRST><<<grid, kBlock, 0, s>>>(*L, coef, diag, x, y);
 }
 
 int check_layout(const gbf_layout* L) {
@@ -61,12 +68,18 @@ static int amul(const gbf_layout* L, const T* coef, const T* diag, const T* x, A
   if (rc) return rc;
   if (L->n_cells == 0) return GBF_OK;
   GBF_REQUIRE(diag && x && y && (L->n_faces == 0 || coef), "amul: NULL pointer");
+  cudaStream_t s = as_stream(stream);
+  const bool hex = layout_kind(*L) == kLayoutHex33;
   if (nei_first) {
-    const int grid = wave_grid(amul_kernel<T, A, true>, kBlock, L->n_cells);
-    amul_kernel<T, A, true><<<grid, kBlock, 0, as_stream(stream)>>>(*L, coef, diag, x, y);
+    if (hex)
+      launch_amul<kLayoutHex33, T, A, true>(L, coef, diag, x, y, s);
+    else
+      launch_amul<kLayoutGeneric, T, A, true>(L, coef, diag, x, y, s);
   } else {
-    const int grid = wave_grid(amul_kernel<T, A, false>, kBlock, L->n_cells);
-    amul_kernel<T, A, false><<<grid, kBlock, 0, as_stream(stream)>>>(*L, coef, diag, x, y);
+    if (hex)
+      launch_amul<kLayoutHex33, T, A, false>(L, coef, diag, x, y, s);
+    else
+      launch_amul<kLayoutGeneric, T, A, false>(L, coef, diag, x, y, s);
   }
   GBF_CHECK_LAUNCH();
   return GBF_OK;

@@ -91,5 +91,91 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
   return y;
 }
 
-}  // namespace gbf
+// ---------------------------------------------------------------------------
+// Fixed-width gather for layouts whose slices all have WO owner-side and WN
+// neighbour-side slots, every slot offset-uniform (all_uniform): the slot
+// addresses are arithmetic, the slice's {delta, mask} entries come in W/2
+// 128-bit loads, and no slot needs a width predicate or a slot_col
+// fallback.  Same products and summation order as cell_amul.
+// ---------------------------------------------------------------------------
+template <typename T, typename A, bool NEI_FIRST, int WO, int WN>
+__device__ __forceinline__ A cell_amul_fixed(const gbf_layout& L, const T* __restrict__ coef,
+                                             const T* __restrict__ diag,
+                                             const T* __restrict__ x, int c, T xc) {
+  constexpr int W = WO + WN;
+  static_assert(W % 2 == 0, "fixed-width gather loads entry pairs");
+  const int s = c >> 5, lane = c & 31;
+  const int base = 32 * W * s + lane;
+  const int4* __restrict__ dm4 = reinterpret_cast<const int4*>(L.slot_dm) + (W / 2) * s;
+  int d[W];
+  unsigned m[W];
+#pragma unroll
+  for (int q = 0; q < W / 2; ++q) {
+    const int4 v = __ldg(dm4 + q);
+    d[2 * q] = v.x;
+    m[2 * q] = (unsigned)v.y;
+    d[2 * q + 1] = v.z;
+    m[2 * q + 1] = (unsigned)v.w;
+  }
+  T a[W], xv[W];
+  bool on[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) a[k] = __ldg(coef + base + 32 * k);
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    on[k] = (m[k] >> lane) & 1u;
+    xv[k] = on[k] ? __ldg(x + c + d[k]) : (T)0;
+  }
+  A so = (A)0, sn = (A)0;
+#pragma unroll
+  for (int k = 0; k < WO; ++k)
+    if (on[k]) so = add_rn(so, (A)mul_rn(a[k], xv[k]));
+#pragma unroll
+  for (int k = WO; k < W; ++k)
+    if (on[k]) sn = add_rn(sn, (A)mul_rn(a[k], xv[k]));
+  A y = (A)mul_rn(__ldg(diag + c), xc);
+  if (NEI_FIRST) {
+    y = add_rn(y, sn);
+    y = add_rn(y, so);
+  } else {
+    y = add_rn(y, so);
+    y = add_rn(y, sn);
+  }
+  return y;
+}
 
+// Layout kinds with a fixed-width kernel instantiation.
+enum { kLayoutGeneric = 0, kLayoutHex33 = 33 };
+
+// The fixed-width gather reads slot_dm as int4, so it needs a 16-byte
+// aligned table.
+inline int layout_kind(const gbf_layout& L) {
+  if (L.n_faces > 0 && L.all_uniform && L.slot_dm && L.uniform_wo == 3 && L.uniform_wn == 3 &&
+      (reinterpret_cast<uintptr_t>(L.slot_dm) & 15u) == 0)
+    return kLayoutHex33;
+  return kLayoutGeneric;
+}
+
+// Runs the statement list with the compile-time constant KIND set to the
+// layout's kind, so a kernel templated on it is launched in its fixed-width
+// form where one exists.
+#define GBF_LAYOUT_DISPATCH(layout, KIND, ...)      \
+  do {                                              \
+    if (::gbf::layout_kind(layout) == ::gbf::kLayoutHex33) { \
+      constexpr int KIND = ::gbf::kLayoutHex33;     \
+      __VA_ARGS__;                                  \
+    } else {                                        \
+      constexpr int KIND = ::gbf::kLayoutGeneric;   \
+      __VA_ARGS__;                                  \
+    }                                               \
+  } while (0)
+
+template <int KIND, typename T, typename A, bool NEI_FIRST>
+__device__ __forceinline__ A cell_amul_k(const gbf_layout& L, const T* __restrict__ coef,
+                                         const T* __restrict__ diag, const T* __restrict__ x,
+                                         int c, T xc) {
+  if (KIND == kLayoutHex33) return cell_amul_fixed<T, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, xc);
+  return cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, xc);
+}
+
+}  // namespace gbf

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(BS)
   }
 }
 
-template <int BS>
+template <int BS, int KIND>
 __global__ void __launch_bounds__(BS)
     bmp_ap_kernel(gbf_layout L, BTiles T, const float* __restrict__ coef32, BVecs v) {
   const int tile = blockIdx.x;
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(BS)
   BDFAcc a;
   for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < __ldg(T.tile_end + tile); c += BS) {
     const float pc = __ldg(v.p + c);
-    const float y = cell_amul<float, float, false>(L, coef32, v.d32, v.p, c, pc);
+    const float y = cell_amul_k<KIND, float, float, false>(L, coef32, v.d32, v.p, c, pc);
     v.Ap[c] = y;
     a.add_prod(pc, y);
   }
@@ -299,7 +299,7 @@ static int launch_iteration(cudaStream_t s, int nt, const gbf_layout& L, const B
                             const double* coef64, const double* diag64, const float* coef32,
                             const double* b, double* x, const BVecs& v, double delta,
                             const gbf_solve_params& P) {
-  bmp_ap_kernel<BS><<<nt, BS, 0, s>>>(L, T, coef32, v);
+  GBF_LAYOUT_DISPATCH(L, K, bmp_ap_kernel<BS, K><<<nt, BS, 0, s>>>(L, T, coef32, v));
   bmp_update_kernel<BS><<<nt, BS, 0, s>>>(T, x, v, delta, P);
   bmp_true_kernel<BS><<<nt, BS, 0, s>>>(L, T, coef64, diag64, b, x, v, P);
   bmp_p_kernel<BS><<<nt, BS, 0, s>>>(T, v);

@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+template <int KIND>
 __global__ void __launch_bounds__(kBlock)
     mp_ap_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v) {
   if (v.st->status != GBF_RUNNING) return;
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(kBlock)
   DFAcc a;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
     const float pc = __ldg(v.p + c);
-    const float y = cell_amul<float, float, false>(L, coef32, v.d32, v.p, c, pc);
+    const float y = cell_amul_k<KIND, float, float, false>(L, coef32, v.d32, v.p, c, pc);
     v.Ap[c] = y;
     a.add_prod(pc, y);
   }
@@ -378,7 +379,9 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
 
   // one full wave of resident blocks per kernel (each reduces its own partials)
   const int Gi = wave_grid(mp_init_kernel, kBlock, n);
-  const int Ga = wave_grid(mp_ap_kernel, kBlock, n);
+  const bool hex = layout_kind(*L) == kLayoutHex33;
+  const int Ga = hex ? wave_grid(mp_ap_kernel<kLayoutHex33>, kBlock, n)
+                     : wave_grid(mp_ap_kernel<kLayoutGeneric>, kBlock, n);
   const int Gu = wave_grid(mp_update_kernel, kBlock, (n + 3) / 4);
   const int Gt = wave_grid(mp_true_kernel, kBlock, n);
   const int Gp = wave_grid(mp_p_kernel, kBlock, (n + 3) / 4);
@@ -397,7 +400,10 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   while (hs.status == GBF_RUNNING && launched < limit) {
     for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
       const bool tb = timing_begin(kProbeMixedAp, s);
-      mp_ap_kernel<<<Ga, kBlock, 0, s>>>(*L, coef32, v);
+      if (hex)
+        mp_ap_kernel<kLayoutHex33><<<Ga, kBlock, 0, s>>>(*L, coef32, v);
+      else
+        mp_ap_kernel<kLayoutGeneric><<<Ga, kBlock, 0, s>>>(*L, coef32, v);
       if (tb) timing_end(kProbeMixedAp, s);
       mp_update_kernel<<<Gu, kBlock, 0, s>>>(n, x, v, delta, *P);
       mp_true_kernel<<<Gt, kBlock, 0, s>>>(*L, coef64, diag64, b, x, v, hist, hist_cap, *P);

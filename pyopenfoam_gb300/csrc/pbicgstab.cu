@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+template <int KIND>
 __global__ void __launch_bounds__(kBlock)
     bicg_v_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
                   BicgVecs v) {
@@ -91,7 +92,8 @@ __global__ void __launch_bounds__(kBlock)
   const int G = gridDim.x;
   double acc = 0.0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
-    const double yv = cell_amul<double, double, false>(L, coef, diag, v.y, c, __ldg(v.y + c));
+    const double yv =
+        cell_amul_k<KIND, double, double, false>(L, coef, diag, v.y, c, __ldg(v.y + c));
     v.v[c] = yv;
     acc = fma(__ldg(v.rt + c), yv, acc);
   }
@@ -142,6 +144,7 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+template <int KIND>
 __global__ void __launch_bounds__(kBlock)
     bicg_t_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
                   BicgVecs v, int standard_omega) {
@@ -151,7 +154,7 @@ __global__ void __launch_bounds__(kBlock)
   double tt = 0.0, tz = 0.0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
     const double zc = __ldg(v.z + c);
-    const double tc = cell_amul<double, double, false>(L, coef, diag, v.z, c, zc);
+    const double tc = cell_amul_k<KIND, double, double, false>(L, coef, diag, v.z, c, zc);
     v.t[c] = tc;
     tt = fma(tc, tc, tt);
     // reference: omega = (t.z)/(t.t); standard BiCGStab: (t.s)/(t.t)
@@ -315,13 +318,15 @@ extern "C" int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* coef,
   while (hs.status == GBF_RUNNING && launched < P->max_iter) {
     for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
       const bool tb = timing_begin(kProbeBicgAmul, s);
-      bicg_v_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      GBF_LAYOUT_DISPATCH(*L, K, bicg_v_kernel<K><<<G, kBlock, 0, s>>>(*L, coef, diag, v));
       if (tb) timing_end(kProbeBicgAmul, s);
       if (pd)
         bicg_s_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
       else
         bicg_s_kernel<false><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
-      bicg_t_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v, P->variant == 1);
+      GBF_LAYOUT_DISPATCH(*L, K,
+                          bicg_t_kernel<K><<<G, kBlock, 0, s>>>(*L, coef, diag, v,
+                                                                P->variant == 1));
       bicg_r_kernel<<<G, kBlock, 0, s>>>(n, x, v, hist, *P);
       if (pd)
         bicg_p_kernel<true><<<G, kBlock, 0, s>>>(n, pd, v);

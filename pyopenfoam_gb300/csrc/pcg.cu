@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+template <int KIND>
 __global__ void __launch_bounds__(kBlock)
     pcg_ap_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
                   PcgVecs v) {
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kBlock)
   double acc = 0.0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += G * blockDim.x) {
     const double pc = __ldg(p + c);
-    const double y = cell_amul<double, double, false>(L, coef, diag, p, c, pc);
+    const double y = cell_amul_k<KIND, double, double, false>(L, coef, diag, p, c, pc);
     v.Ap[c] = y;
     acc = fma(pc, y, acc);
   }
@@ -233,7 +234,10 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
   while (hs.status == GBF_RUNNING && launched < P->max_iter) {
     for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
       const bool tb = timing_begin(kProbePcgAp, s);
-      pcg_ap_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      if (layout_kind(*L) == kLayoutHex33)
+        pcg_ap_kernel<kLayoutHex33><<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      else
+        pcg_ap_kernel<kLayoutGeneric><<<G, kBlock, 0, s>>>(*L, coef, diag, v);
       if (tb) timing_end(kProbePcgAp, s);
       if (pd)
         pcg_update_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
@@ -371,7 +375,7 @@ extern "C" int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* coef
   int launched = 0;
   while (hs.status == GBF_RUNNING && launched < P->max_iter) {
     for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
-      pcg_ap_kernel<<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      pcg_ap_kernel<kLayoutGeneric><<<G, kBlock, 0, s>>>(*L, coef, diag, v);
       if (pd)
         pcg_update_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
       else

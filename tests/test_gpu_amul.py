@@ -166,4 +166,10 @@ def test_offset_compression_gives_identical_bits():
                                            torch.cuda.current_stream().cuda_stream))
         assert (bits(y1.cpu().numpy()) == bits(y3.cpu().numpy())).all()
         if not perm:
+            # y1 came through the fixed-width (3 + 3 slot) hex gather, y2 and
+            # y3 through the generic one
             assert topo.uniform and topo.n_uniform_entries == topo.n_slots // 32
+            assert topo.layout.all_uniform == 1
+            assert (topo.layout.uniform_wo, topo.layout.uniform_wn) == (3, 3)
+        else:
+            assert topo.layout.all_uniform == 0
