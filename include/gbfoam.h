@@ -305,6 +305,41 @@ int gbf_adjoint_face_grad_f64(const gbf_layout* L, int32_t n_faces_total,
                               const double* x, double scale, int32_t accumulate,
                               double* g_gamma, void* stream);
 
+/* assemble_pressure_equation, solvers/pressure_equation.py:49-148: the
+ * Laplacian of 1/A_p (1/max(|A_p|,1e-30) per cell, linearly interpolated with
+ * face_weights[n_faces_total]) without a boundary diagonal term, and the
+ * source -div(phiHbyA)/V over internal then boundary faces.  Bitwise the
+ * reference's coefficients and source.                                     */
+int gbf_pressure_assemble_f64(const gbf_layout* L, int32_t n_faces_total, const int32_t* bnd_ptr,
+                              const int32_t* bnd_face, const double* face_areas,
+                              const double* delta, const double* face_weights, const double* A_p,
+                              const double* volumes, const double* phiHbyA, double* lower,
+                              double* upper, double* diag, double* source, void* stream);
+
+/* DifferentiableLaplacian.forward, differentiable/operators.py:421-522: the
+ * explicit Laplacian out = div(D grad phi) per unit volume, with the
+ * reference's face flux ((D_f (phi_N - phi_P)) |S_f|) delta_f, its per-cell
+ * summation order and the boundary term ((D_b |S_b|) delta_b) phi_P.  D as in
+ * gbf_laplacian_assemble_f64.  Called with phi := grad_output it is the
+ * phi-gradient of backward (:542-567).  Bitwise the reference's results.   */
+int gbf_explicit_laplacian_f64(const gbf_layout* L, int32_t n_faces_total,
+                               const int32_t* bnd_ptr, const int32_t* bnd_face,
+                               const double* face_areas, const double* delta, int32_t d_mode,
+                               double d_value, const double* d_face, const double* d_cell,
+                               const double* weights, const double* volumes, const double* phi,
+                               double* out, void* stream);
+/* DifferentiableLaplacian.backward D-gradient, operators.py:570-625:
+ * g_face[n_faces_total] per face; if g_cell != NULL also the per-cell
+ * mapping (half of each internal face to each side, boundary faces to the
+ * owner); if g_sum != NULL the sum over all faces (a 0-d D) in a fixed order.
+ * g_face and g_cell are bitwise the reference's; g_sum agrees to rounding. */
+int gbf_explicit_laplacian_grad_d_f64(const gbf_layout* L, int32_t n_faces_total,
+                                      const int32_t* owner_all, const int32_t* bnd_ptr,
+                                      const int32_t* bnd_face, const double* face_areas,
+                                      const double* delta, const double* volumes,
+                                      const double* phi, const double* g, double* g_face,
+                                      double* g_cell, double* g_sum, void* stream);
+
 /* ---- mixed precision -------------------------------------------------------
  * No reference counterpart (the north-star's precision pattern): PCG whose
  * Krylov recurrence, Amul (coef32 = FP32 packing of the FP64 matrix) and

@@ -490,6 +490,144 @@ void orc_dls_grads_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
   }
 }
 
+/* assemble_pressure_equation: solvers/pressure_equation.py:49-148          */
+/* inv = 1/max(|A_p|,1e-30); inv_f = w*inv_P + (1-w)*inv_N;                   */
+/* fc = (inv_f*|S|)*delta; lower = -fc/V_P; upper = -fc/V_N;                 */
+/* diag = (0 + sum_own fc/V_P) + sum_nei fc/V_N;                             */
+/* source = (((0 + sum_own -phi) + sum_nei phi) [+ sum_bnd -phi]) / V        */
+/* ------------------------------------------------------------------------ */
+static double inv_abs(double a) {
+  double v = fabs(a);
+  return 1.0 / (v < 1e-30 ? 1e-30 : v);
+}
+
+void orc_pressure_assemble_f64(idx_t n, idx_t nint, idx_t nfaces, const idx_t* own,
+                               const idx_t* nei, const double* areas, const double* delta,
+                               const double* w, const double* Ap, const double* V,
+                               const double* phi, double* lower, double* upper, double* diag,
+                               double* source, double* work /* 3n */) {
+  double *s1 = work, *s2 = work + n, *s3 = work + 2 * n;
+  for (idx_t c = 0; c < n; ++c) { s1[c] = 0.0; s2[c] = 0.0; s3[c] = 0.0; }
+  for (idx_t f = 0; f < nint; ++f) {
+    double inv_f = w[f] * inv_abs(Ap[own[f]]) + (1.0 - w[f]) * inv_abs(Ap[nei[f]]);
+    double fc = inv_f * smag3(areas + 3 * f);
+    fc = fc * delta[f];
+    lower[f] = (-fc) / V[own[f]];
+    upper[f] = (-fc) / V[nei[f]];
+    s1[own[f]] = s1[own[f]] + fc / V[own[f]];
+    s2[nei[f]] = s2[nei[f]] + fc / V[nei[f]];
+  }
+  for (idx_t c = 0; c < n; ++c) diag[c] = (0.0 + s1[c]) + s2[c];
+  for (idx_t c = 0; c < n; ++c) { s1[c] = 0.0; s2[c] = 0.0; }
+  for (idx_t f = 0; f < nint; ++f) s1[own[f]] = s1[own[f]] + (-phi[f]);
+  for (idx_t f = 0; f < nint; ++f) s2[nei[f]] = s2[nei[f]] + phi[f];
+  for (idx_t c = 0; c < n; ++c) source[c] = (0.0 + s1[c]) + s2[c];
+  if (nfaces > nint) {
+    for (idx_t f = nint; f < nfaces; ++f) s3[own[f]] = s3[own[f]] + (-phi[f]);
+    for (idx_t c = 0; c < n; ++c) source[c] = source[c] + s3[c];
+  }
+  for (idx_t c = 0; c < n; ++c) source[c] = source[c] / V[c];
+}
+
+/* Linear-interpolation weights: discretisation/weights.py:21-85            */
+/* w_f = |f_c - C_N| / (|f_c - C_P| + |f_c - C_N|) on internal faces (the    */
+/* denominator replaced by 1 when it is not > 1e-30), 1 on boundary faces.   */
+/* ------------------------------------------------------------------------ */
+void orc_centre_weights_f64(idx_t nint, idx_t nfaces, const idx_t* own, const idx_t* nei,
+                            const double* cc, const double* fc, double* w) {
+  for (idx_t f = 0; f < nfaces; ++f) w[f] = 1.0;
+  for (idx_t f = 0; f < nint; ++f) {
+    double a[3], b[3];
+    for (int k = 0; k < 3; ++k) {
+      a[k] = fc[3 * f + k] - cc[3 * own[f] + k];
+      b[k] = fc[3 * f + k] - cc[3 * nei[f] + k];
+    }
+    double dp = smag3(a), dn = smag3(b);
+    double den = dp + dn;
+    w[f] = dn / (den > 1e-30 ? den : 1.0);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* DifferentiableLaplacian (differentiable/operators.py:409-643)             */
+/* forward (:421-522): flux_f = ((D_f*(phi_N - phi_P))*|S_f|)*delta_f;       */
+/*   lap = ((0 + sum_own flux) + sum_nei (-flux)) [+ sum_bnd               */
+/*         ((D_b*|S_b|)*delta_b)*phi_P]  / max(V, 1e-30)                      */
+/* D is given per face (the caller resolves scalars / cell values to faces). */
+/* The same routine is the phi-gradient of backward (:542-567) with phi := g. */
+/* ------------------------------------------------------------------------ */
+static double clampv(double v) { return v < 1e-30 ? 1e-30 : v; }
+
+void orc_explicit_laplacian_f64(idx_t n, idx_t nint, idx_t nfaces, const idx_t* own /* nfaces */,
+                                const idx_t* nei /* nint */, const double* areas,
+                                const double* delta, const double* D, const double* V,
+                                const double* phi, double* out, double* work /* 3n */) {
+  double *s1 = work, *s2 = work + n, *s3 = work + 2 * n;
+  for (idx_t c = 0; c < n; ++c) { s1[c] = 0.0; s2[c] = 0.0; s3[c] = 0.0; }
+  for (idx_t f = 0; f < nint; ++f) {
+    double fl = D[f] * (phi[nei[f]] - phi[own[f]]);
+    fl = fl * smag3(areas + 3 * f);
+    fl = fl * delta[f];
+    s1[own[f]] = s1[own[f]] + fl;
+  }
+  for (idx_t f = 0; f < nint; ++f) {
+    double fl = D[f] * (phi[nei[f]] - phi[own[f]]);
+    fl = fl * smag3(areas + 3 * f);
+    fl = fl * delta[f];
+    s2[nei[f]] = s2[nei[f]] + (-fl);
+  }
+  for (idx_t c = 0; c < n; ++c) out[c] = 0.0 + s1[c];
+  for (idx_t c = 0; c < n; ++c) out[c] = out[c] + s2[c];
+  if (nfaces > nint) {
+    for (idx_t f = nint; f < nfaces; ++f) {
+      double cb = D[f] * smag3(areas + 3 * f);
+      cb = cb * delta[f];
+      s3[own[f]] = s3[own[f]] + cb * phi[own[f]];
+    }
+    for (idx_t c = 0; c < n; ++c) out[c] = out[c] + s3[c];
+  }
+  for (idx_t c = 0; c < n; ++c) out[c] = out[c] / clampv(V[c]);
+}
+
+/* backward, D-gradient per face (:570-600):                                 */
+/*   internal: (((g_P/V_P - g_N/V_N)*(phi_N - phi_P))*|S|)*delta             */
+/*   boundary: (((g_P/V_P)*phi_P)*|S|)*delta                                 */
+void orc_explicit_laplacian_grad_d_f64(idx_t nint, idx_t nfaces, const idx_t* own,
+                                       const idx_t* nei, const double* areas,
+                                       const double* delta, const double* V, const double* phi,
+                                       const double* g, double* gface) {
+  for (idx_t f = 0; f < nint; ++f) {
+    idx_t p = own[f], q = nei[f];
+    double a = g[p] / clampv(V[p]) - g[q] / clampv(V[q]);
+    a = a * (phi[q] - phi[p]);
+    a = a * smag3(areas + 3 * f);
+    gface[f] = a * delta[f];
+  }
+  for (idx_t f = nint; f < nfaces; ++f) {
+    idx_t p = own[f];
+    double a = (g[p] / clampv(V[p])) * phi[p];
+    a = a * smag3(areas + 3 * f);
+    gface[f] = a * delta[f];
+  }
+}
+
+/* per-cell D (:608-625): ((0 + sum_own 0.5*gf) + sum_nei 0.5*gf)           */
+/*                        [+ sum_bnd gf]                                     */
+void orc_face_grad_to_cells_f64(idx_t n, idx_t nint, idx_t nfaces, const idx_t* own,
+                                const idx_t* nei, const double* gface, double* gcell,
+                                double* work /* 3n */) {
+  double *s1 = work, *s2 = work + n, *s3 = work + 2 * n;
+  for (idx_t c = 0; c < n; ++c) { s1[c] = 0.0; s2[c] = 0.0; s3[c] = 0.0; }
+  for (idx_t f = 0; f < nint; ++f) s1[own[f]] = s1[own[f]] + gface[f] * 0.5;
+  for (idx_t f = 0; f < nint; ++f) s2[nei[f]] = s2[nei[f]] + gface[f] * 0.5;
+  for (idx_t c = 0; c < n; ++c) gcell[c] = 0.0 + s1[c];
+  for (idx_t c = 0; c < n; ++c) gcell[c] = gcell[c] + s2[c];
+  if (nfaces > nint) {
+    for (idx_t f = nint; f < nfaces; ++f) s3[own[f]] = s3[own[f]] + gface[f];
+    for (idx_t c = 0; c < n; ++c) gcell[c] = gcell[c] + s3[c];
+  }
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -12,6 +12,11 @@ Routines (reference citations are in ``ldu_oracle.c``):
 * ``pcg`` / ``pbicgstab``         -- the solvers with ``ResidualMonitor`` rules
 * ``laplacian`` / ``div_upwind``  -- ``fvm.laplacian`` / ``fvm.div`` assembly
 * ``dls_grads``                   -- ``DifferentiableLinearSolve.backward``
+* ``pressure_assemble``           -- ``assemble_pressure_equation``
+* ``centre_weights``              -- linear-interpolation weights
+* ``explicit_laplacian`` / ``explicit_laplacian_grad_d`` /
+  ``face_grad_to_cells``          -- ``DifferentiableLaplacian`` forward and
+  backward
 """
 
 from __future__ import annotations
@@ -205,6 +210,78 @@ def dls_grads(owner, neighbour, lam, x):
     lib().orc_dls_grads_f64(ctypes.c_int64(n), ctypes.c_int64(nf), _p(own), _p(nei), _p(la),
                             _p(xx), _p(gd), _p(gl), _p(gu))
     return gd, gl, gu
+
+
+def pressure_assemble(n_cells, owner_all, neighbour, face_areas, delta, weights, A_p, volumes,
+                      phiHbyA):
+    """``assemble_pressure_equation``: (lower, upper, diag, source)."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    fa, dl, w, ap, V, ph = (_f(face_areas).reshape(-1, 3), _f(delta), _f(weights), _f(A_p),
+                            _f(volumes), _f(phiHbyA))
+    nint, nfaces = nei.shape[0], own.shape[0]
+    lo, up, dg, src = np.empty(nint), np.empty(nint), np.empty(n_cells), np.empty(n_cells)
+    wk = np.empty(3 * n_cells + 1)
+    lib().orc_pressure_assemble_f64(ctypes.c_int64(n_cells), ctypes.c_int64(nint),
+                                    ctypes.c_int64(nfaces), _p(own), _p(nei), _p(fa), _p(dl),
+                                    _p(w), _p(ap), _p(V), _p(ph), _p(lo), _p(up), _p(dg), _p(src),
+                                    _p(wk))
+    return lo, up, dg, src
+
+
+def centre_weights(owner_all, neighbour, cell_centres, face_centres):
+    own, nei = _i64(owner_all), _i64(neighbour)
+    cc, fc = _f(cell_centres).reshape(-1, 3), _f(face_centres).reshape(-1, 3)
+    w = np.empty(own.shape[0])
+    lib().orc_centre_weights_f64(ctypes.c_int64(nei.shape[0]), ctypes.c_int64(own.shape[0]),
+                                 _p(own), _p(nei), _p(cc), _p(fc), _p(w))
+    return w
+
+
+def face_values(owner_all, neighbour, D_cell, weights):
+    """``LinearInterpolation.interpolate`` (interpolation.py:101-145):
+    w*D_P + (1 - w)*D_N on internal faces, D_P on boundary faces."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    D, w = _f(D_cell), _f(weights)
+    nint = nei.shape[0]
+    out = D[own].copy()
+    wi = w[:nint]
+    out[:nint] = wi * D[own[:nint]] + (1.0 - wi) * D[nei]
+    return out
+
+
+def explicit_laplacian(n_cells, owner_all, neighbour, face_areas, delta, D_face, volumes, phi):
+    """``DifferentiableLaplacian.forward`` for a per-face D (and the
+    phi-gradient of its backward, with phi := grad_output)."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    fa, dl, D, V, ph = (_f(face_areas).reshape(-1, 3), _f(delta), _f(D_face), _f(volumes),
+                        _f(phi))
+    out = np.empty(n_cells)
+    w = np.empty(3 * n_cells + 1)
+    lib().orc_explicit_laplacian_f64(ctypes.c_int64(n_cells), ctypes.c_int64(nei.shape[0]),
+                                     ctypes.c_int64(own.shape[0]), _p(own), _p(nei), _p(fa),
+                                     _p(dl), _p(D), _p(V), _p(ph), _p(out), _p(w))
+    return out
+
+
+def explicit_laplacian_grad_d(owner_all, neighbour, face_areas, delta, volumes, phi, g):
+    own, nei = _i64(owner_all), _i64(neighbour)
+    fa, dl, V, ph, gg = (_f(face_areas).reshape(-1, 3), _f(delta), _f(volumes), _f(phi), _f(g))
+    out = np.empty(own.shape[0])
+    lib().orc_explicit_laplacian_grad_d_f64(ctypes.c_int64(nei.shape[0]),
+                                            ctypes.c_int64(own.shape[0]), _p(own), _p(nei),
+                                            _p(fa), _p(dl), _p(V), _p(ph), _p(gg), _p(out))
+    return out
+
+
+def face_grad_to_cells(n_cells, owner_all, neighbour, g_face):
+    own, nei = _i64(owner_all), _i64(neighbour)
+    gf = _f(g_face)
+    out = np.empty(n_cells)
+    w = np.empty(3 * n_cells + 1)
+    lib().orc_face_grad_to_cells_f64(ctypes.c_int64(n_cells), ctypes.c_int64(nei.shape[0]),
+                                     ctypes.c_int64(own.shape[0]), _p(own), _p(nei), _p(gf),
+                                     _p(out), _p(w))
+    return out
 
 
 def num_threads() -> int:

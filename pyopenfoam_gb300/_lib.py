@@ -133,6 +133,15 @@ EXPORTED: dict[str, tuple] = {
     "gbf_dls_grads_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_adjoint_face_grad_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                                  _c_vp, _c_dbl, _c_i32, _c_vp, _c_vp]),
+    "gbf_pressure_assemble_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                 _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                 _c_vp, _c_vp]),
+    "gbf_explicit_laplacian_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32,
+                                                  _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                  _c_vp, _c_vp]),
+    "gbf_explicit_laplacian_grad_d_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                         _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                         _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f64_to_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),

@@ -23,21 +23,31 @@ __device__ __forceinline__ double face_smag(const double* __restrict__ a) {
 // Face diffusivity: constant, per face, or linearly interpolated from cells
 // (LinearInterpolation.interpolate, interpolation.py:101-145:
 //  w*phi_P + (1 - w)*phi_N on internal faces, phi_P on boundary faces).
+// Mode 3 is the pressure equation's 1/A_p: the per-cell values are
+// 1 / max(|A_p|, 1e-30) (pressure_equation.py:103-104), then interpolated
+// like mode 2.
 struct DiffSpec {
-  int mode;            // 0 constant, 1 per face, 2 per cell
+  int mode;            // 0 constant, 1 per face, 2 per cell, 3 per-cell 1/|A_p|
   double value;        // mode 0
   const double* face;  // mode 1: [n_faces]
-  const double* cell;  // mode 2: [n_cells]
-  const double* w;     // mode 2: [n_faces] interpolation weights
+  const double* cell;  // modes 2, 3: [n_cells]
+  const double* w;     // modes 2, 3: [n_faces] interpolation weights
 };
+
+__device__ __forceinline__ double cell_D(const DiffSpec& D, int c) {
+  const double v = __ldg(D.cell + c);
+  if (D.mode != 3) return v;
+  const double a = fabs(v);
+  return __ddiv_rn(1.0, a < 1e-30 ? 1e-30 : a);  // clamp(min) keeps NaN
+}
 
 __device__ __forceinline__ double face_D(const DiffSpec& D, int f, int p, int q, bool internal) {
   if (D.mode == 0) return D.value;
   if (D.mode == 1) return __ldg(D.face + f);
-  const double dp = __ldg(D.cell + p);
+  const double dp = cell_D(D, p);
   if (!internal) return dp;
   const double w = __ldg(D.w + f);
-  return __dadd_rn(__dmul_rn(w, dp), __dmul_rn(__dsub_rn(1.0, w), __ldg(D.cell + q)));
+  return __dadd_rn(__dmul_rn(w, dp), __dmul_rn(__dsub_rn(1.0, w), cell_D(D, q)));
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -364,6 +374,279 @@ extern "C" int gbf_adjoint_face_grad_f64(const gbf_layout* L, int32_t n_faces_to
                              as_stream(stream)>>>(L->n_faces, n_faces_total, owner_all,
                                                   L->neighbour, face_areas, delta, volumes, lam, x,
                                                   scale, accumulate, g_gamma);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// DifferentiableLaplacian (differentiable/operators.py:409-643): the
+// explicit Laplacian of a cell field and its backward.
+//
+// forward (:421-522), per cell c, faces in ascending order on each side:
+//   flux_f = ((D_f * (phi_N - phi_P)) * |S_f|) * delta_f
+//   lap = (0 + sum_own flux) + sum_nei (-flux)
+//         [+ sum_bnd ((D_b * |S_b|) * delta_b) * phi_c]      (if boundary faces)
+//   lap /= max(V_c, 1e-30)
+// The phi-gradient of backward (:542-567) is the same operator applied to
+// grad_output.  Each face flux is recomputed by both of its cells (same
+// operands, same roundings), so the cell gather needs no scatter and no
+// atomics.
+// ---------------------------------------------------------------------------
+namespace gbf {
+
+__device__ __forceinline__ double clamp_volume(double v) { return v < 1e-30 ? 1e-30 : v; }
+
+__global__ void __launch_bounds__(kBlock)
+    explicit_lap_kernel(gbf_layout L, const int32_t* __restrict__ bnd_ptr,
+                        const int32_t* __restrict__ bnd_face, const double* __restrict__ areas,
+                        const double* __restrict__ delta, DiffSpec D,
+                        const double* __restrict__ V, const double* __restrict__ phi,
+                        int has_bnd, double* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.n_cells) return;
+  const double pc = __ldg(phi + c);
+  double so = 0.0, sn = 0.0;
+  if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    for (int k = 0; k < cs.wo; ++k) {
+      const int i = cs.base + 32 * k;
+      const int f = __ldg(L.slot_face + i);
+      if (f < 0) continue;
+      const int q = __ldg(L.slot_col + i);
+      double fl = __dmul_rn(face_D(D, f, c, q, true), __dsub_rn(__ldg(phi + q), pc));
+      fl = __dmul_rn(fl, face_smag(areas + 3 * (size_t)f));
+      fl = __dmul_rn(fl, __ldg(delta + f));
+      so = __dadd_rn(so, fl);
+    }
+    for (int k = 0; k < cs.wn; ++k) {
+      const int i = cs.base + 32 * (cs.wo + k);
+      const int f = __ldg(L.slot_face + i);
+      if (f < 0) continue;
+      const int p = __ldg(L.slot_col + i);
+      double fl = __dmul_rn(face_D(D, f, p, c, true), __dsub_rn(pc, __ldg(phi + p)));
+      fl = __dmul_rn(fl, face_smag(areas + 3 * (size_t)f));
+      fl = __dmul_rn(fl, __ldg(delta + f));
+      sn = __dadd_rn(sn, -fl);
+    }
+  }
+  double y = __dadd_rn(0.0, so);
+  y = __dadd_rn(y, sn);
+  if (has_bnd) {
+    double sb = 0.0;
+    for (int k = __ldg(bnd_ptr + c); k < __ldg(bnd_ptr + c + 1); ++k) {
+      const int f = __ldg(bnd_face + k);
+      double cb = __dmul_rn(face_D(D, f, c, c, false), face_smag(areas + 3 * (size_t)f));
+      cb = __dmul_rn(cb, __ldg(delta + f));
+      sb = __dadd_rn(sb, __dmul_rn(cb, pc));
+    }
+    y = __dadd_rn(y, sb);
+  }
+  out[c] = __ddiv_rn(y, clamp_volume(__ldg(V + c)));
+}
+
+// D-gradient per face (:570-600):
+//   internal: (((g_P/V_P - g_N/V_N) * (phi_N - phi_P)) * |S|) * delta
+//   boundary: (((g_P/V_P) * phi_P) * |S|) * delta
+__global__ void __launch_bounds__(kBlock)
+    explicit_lap_grad_d_kernel(int nint, int nfaces, const int32_t* __restrict__ own_all,
+                               const int32_t* __restrict__ nei, const double* __restrict__ areas,
+                               const double* __restrict__ delta, const double* __restrict__ V,
+                               const double* __restrict__ phi, const double* __restrict__ g,
+                               double* __restrict__ gface) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nfaces) return;
+  const int p = __ldg(own_all + f);
+  const double gp = __ddiv_rn(__ldg(g + p), clamp_volume(__ldg(V + p)));
+  double a;
+  if (f < nint) {
+    const int q = __ldg(nei + f);
+    const double gq = __ddiv_rn(__ldg(g + q), clamp_volume(__ldg(V + q)));
+    a = __dmul_rn(__dsub_rn(gp, gq), __dsub_rn(__ldg(phi + q), __ldg(phi + p)));
+  } else {
+    a = __dmul_rn(gp, __ldg(phi + p));
+  }
+  a = __dmul_rn(a, face_smag(areas + 3 * (size_t)f));
+  gface[f] = __dmul_rn(a, __ldg(delta + f));
+}
+
+// Per-cell D (:608-625): ((0 + sum_own gf*0.5) + sum_nei gf*0.5) [+ sum_bnd gf].
+__global__ void __launch_bounds__(kBlock)
+    face_grad_to_cells_kernel(gbf_layout L, const int32_t* __restrict__ bnd_ptr,
+                              const int32_t* __restrict__ bnd_face,
+                              const double* __restrict__ gface, int has_bnd,
+                              double* __restrict__ gcell) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.n_cells) return;
+  double so = 0.0, sn = 0.0;
+  if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    for (int k = 0; k < cs.wo; ++k) {
+      const int f = __ldg(L.slot_face + cs.base + 32 * k);
+      if (f >= 0) so = __dadd_rn(so, __dmul_rn(__ldg(gface + f), 0.5));
+    }
+    for (int k = 0; k < cs.wn; ++k) {
+      const int f = __ldg(L.slot_face + cs.base + 32 * (cs.wo + k));
+      if (f >= 0) sn = __dadd_rn(sn, __dmul_rn(__ldg(gface + f), 0.5));
+    }
+  }
+  double y = __dadd_rn(0.0, so);
+  y = __dadd_rn(y, sn);
+  if (has_bnd) {
+    double sb = 0.0;
+    for (int k = __ldg(bnd_ptr + c); k < __ldg(bnd_ptr + c + 1); ++k)
+      sb = __dadd_rn(sb, __ldg(gface + __ldg(bnd_face + k)));
+    y = __dadd_rn(y, sb);
+  }
+  gcell[c] = y;
+}
+
+// Scalar D: the sum of the face gradients in one 1024-thread block, in a
+// fixed order (strided per-thread sums, then the warp / block tree), so the
+// result is reproducible run to run.
+constexpr int kSumBlock = 1024;
+__global__ void __launch_bounds__(kSumBlock)
+    fixed_order_sum_kernel(int n, const double* __restrict__ a, double* __restrict__ out) {
+  __shared__ double sh[kSumBlock / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += kSumBlock) s = __dadd_rn(s, __ldg(a + i));
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = s;
+}
+
+}  // namespace gbf
+
+extern "C" int gbf_explicit_laplacian_f64(const gbf_layout* L, int32_t n_faces_total,
+                                          const int32_t* bnd_ptr, const int32_t* bnd_face,
+                                          const double* face_areas, const double* delta,
+                                          int32_t d_mode, double d_value, const double* d_face,
+                                          const double* d_cell, const double* weights,
+                                          const double* volumes, const double* phi, double* out,
+                                          void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int n = L->n_cells, nint = L->n_faces;
+  GBF_REQUIRE(n_faces_total >= nint, "explicit_laplacian: n_faces_total < n_internal_faces");
+  GBF_REQUIRE(d_mode >= 0 && d_mode <= 2, "explicit_laplacian: bad diffusivity mode %d", d_mode);
+  GBF_REQUIRE(d_mode != 1 || d_face, "explicit_laplacian: per-face diffusivity is NULL");
+  GBF_REQUIRE(d_mode != 2 || (d_cell && (nint == 0 || weights)),
+              "explicit_laplacian: per-cell diffusivity is NULL");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(volumes && phi && out && (n_faces_total == 0 || (face_areas && delta)),
+              "explicit_laplacian: NULL pointer");
+  const bool has_bnd = n_faces_total > nint;
+  GBF_REQUIRE(!has_bnd || (bnd_ptr && bnd_face), "explicit_laplacian: NULL boundary lists");
+  const DiffSpec D = make_spec(d_mode, d_value, d_face, d_cell, weights);
+  explicit_lap_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(
+      *L, bnd_ptr, bnd_face, face_areas, delta, D, volumes, phi, has_bnd ? 1 : 0, out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_explicit_laplacian_grad_d_f64(const gbf_layout* L, int32_t n_faces_total,
+                                                 const int32_t* owner_all,
+                                                 const int32_t* bnd_ptr, const int32_t* bnd_face,
+                                                 const double* face_areas, const double* delta,
+                                                 const double* volumes, const double* phi,
+                                                 const double* g, double* g_face, double* g_cell,
+                                                 double* g_sum, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int nint = L->n_faces;
+  GBF_REQUIRE(n_faces_total >= nint, "explicit_laplacian_grad_d: n_faces_total < n_internal");
+  cudaStream_t s = as_stream(stream);
+  if (n_faces_total > 0) {
+    GBF_REQUIRE(owner_all && face_areas && delta && volumes && phi && g && g_face &&
+                    (nint == 0 || L->neighbour),
+                "explicit_laplacian_grad_d: NULL pointer");
+    explicit_lap_grad_d_kernel<<<(n_faces_total + kBlock - 1) / kBlock, kBlock, 0, s>>>(
+        nint, n_faces_total, owner_all, L->neighbour, face_areas, delta, volumes, phi, g, g_face);
+    GBF_CHECK_LAUNCH();
+  }
+  const bool has_bnd = n_faces_total > nint;
+  if (g_cell && L->n_cells > 0) {
+    GBF_REQUIRE(!has_bnd || (bnd_ptr && bnd_face),
+                "explicit_laplacian_grad_d: NULL boundary lists");
+    face_grad_to_cells_kernel<<<(L->n_cells + kBlock - 1) / kBlock, kBlock, 0, s>>>(
+        *L, bnd_ptr, bnd_face, g_face, has_bnd ? 1 : 0, g_cell);
+    GBF_CHECK_LAUNCH();
+  }
+  if (g_sum) {
+    fixed_order_sum_kernel<<<1, kSumBlock, 0, s>>>(n_faces_total, g_face, g_sum);
+    GBF_CHECK_LAUNCH();
+  }
+  return GBF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pressure equation (solvers/pressure_equation.py:49-148):
+//   face_coeff = ((1/A_p)_f |S_f|) delta_f with (1/A_p)_f linearly
+//   interpolated from 1/max(|A_p|, 1e-30) with the given face weights;
+//   lower = -fc/V_P, upper = -fc/V_N; diag = (0 + sum_own fc/V_P) + sum_nei fc/V_N
+//   (no boundary term); source = (((0 + sum_own -phi_f) + sum_nei phi_f)
+//   [+ sum_bnd -phi_b]) / V.
+// ---------------------------------------------------------------------------
+namespace gbf {
+__global__ void __launch_bounds__(kBlock)
+    pressure_source_kernel(gbf_layout L, const int32_t* __restrict__ bnd_ptr,
+                           const int32_t* __restrict__ bnd_face, const double* __restrict__ phi,
+                           const double* __restrict__ V, int has_bnd, double* __restrict__ src) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.n_cells) return;
+  double so = 0.0, sn = 0.0;
+  if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    for (int k = 0; k < cs.wo; ++k) {
+      const int f = __ldg(L.slot_face + cs.base + 32 * k);
+      if (f >= 0) so = __dadd_rn(so, -__ldg(phi + f));
+    }
+    for (int k = 0; k < cs.wn; ++k) {
+      const int f = __ldg(L.slot_face + cs.base + 32 * (cs.wo + k));
+      if (f >= 0) sn = __dadd_rn(sn, __ldg(phi + f));
+    }
+  }
+  double y = __dadd_rn(0.0, so);
+  y = __dadd_rn(y, sn);
+  if (has_bnd) {
+    double sb = 0.0;
+    for (int k = __ldg(bnd_ptr + c); k < __ldg(bnd_ptr + c + 1); ++k)
+      sb = __dadd_rn(sb, -__ldg(phi + __ldg(bnd_face + k)));
+    y = __dadd_rn(y, sb);
+  }
+  src[c] = __ddiv_rn(y, __ldg(V + c));
+}
+}  // namespace gbf
+
+extern "C" int gbf_pressure_assemble_f64(const gbf_layout* L, int32_t n_faces_total,
+                                         const int32_t* bnd_ptr, const int32_t* bnd_face,
+                                         const double* face_areas, const double* delta,
+                                         const double* face_weights, const double* A_p,
+                                         const double* volumes, const double* phiHbyA,
+                                         double* lower, double* upper, double* diag,
+                                         double* source, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int n = L->n_cells, nint = L->n_faces;
+  GBF_REQUIRE(n_faces_total >= nint, "pressure_assemble: n_faces_total < n_internal_faces");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(A_p && volumes && diag && source && (n_faces_total == 0 || phiHbyA),
+              "pressure_assemble: NULL pointer");
+  const bool has_bnd = n_faces_total > nint;
+  GBF_REQUIRE(!has_bnd || (bnd_ptr && bnd_face), "pressure_assemble: NULL boundary lists");
+  const DiffSpec D = make_spec(3, 0.0, nullptr, A_p, face_weights);
+  cudaStream_t s = as_stream(stream);
+  if (nint > 0) {
+    GBF_REQUIRE(lower && upper && face_areas && delta && face_weights && L->owner &&
+                    L->neighbour,
+                "pressure_assemble: NULL pointer");
+    lap_face_kernel<<<(nint + kBlock - 1) / kBlock, kBlock, 0, s>>>(
+        nint, L->owner, L->neighbour, face_areas, delta, D, volumes, lower, upper);
+    GBF_CHECK_LAUNCH();
+  }
+  lap_diag_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(
+      *L, lower, upper, nullptr, nullptr, face_areas, delta, D, volumes, 0, diag);
+  GBF_CHECK_LAUNCH();
+  pressure_source_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(
+      *L, bnd_ptr, bnd_face, phiHbyA, volumes, has_bnd ? 1 : 0, source);
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }

@@ -51,7 +51,7 @@ int reduction_grid() {
 
 extern "C" const char* gbf_last_error(void) { return gbf::g_err; }
 
-extern "C" int gbf_version(void) { return 1; }
+extern "C" int gbf_version(void) { return 2; }
 
 extern "C" int gbf_device_sm_count(int32_t* n_sm) {
   int dev = 0, sms = 0;

@@ -1,5 +1,7 @@
-"""Differentiation through the linear solve and the Laplacian assembly."""
+"""Differentiation through the linear solve, the Laplacian assembly and the
+explicit Laplacian."""
 
 from .linear_solver import DifferentiableLinearSolve, dls_grads
+from .operators import DifferentiableLaplacian
 
-__all__ = ["DifferentiableLinearSolve", "dls_grads"]
+__all__ = ["DifferentiableLaplacian", "DifferentiableLinearSolve", "dls_grads"]

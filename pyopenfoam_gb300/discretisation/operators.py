@@ -27,6 +27,7 @@ import torch
 from .. import _lib
 from ..core.device import resolve_device
 from ..core.fv_matrix import FvMatrix
+from ..core.topology import get_topology
 
 __all__ = ["fvm", "MeshData", "mesh_data"]
 
@@ -63,6 +64,11 @@ class MeshData:
     def field(self, name: str) -> torch.Tensor:
         t = getattr(self._mesh, name)
         return t.to(device=self.device, dtype=torch.float64).contiguous()
+
+    def topology(self):
+        """Slot layout of the internal-face addressing (shared through the
+        topology cache with every LduMatrix on the same tensors)."""
+        return get_topology(self.n_cells, self.owner, self.neighbour)
 
     def weights(self, topo) -> torch.Tensor:
         if self._weights is None:

@@ -6,10 +6,12 @@ from .mixed import MixedPrecisionPCGSolver
 from .pbicgstab import PBiCGSTABSolver
 from .pcg import PCGSolver
 from .preconditioners import DICPreconditioner, DILUPreconditioner, Preconditioner
+from .pressure_equation import assemble_pressure_equation, solve_pressure_equation
 from .residual import ConvergenceInfo, ResidualMonitor
 
 __all__ = [
     "LinearSolverBase", "create_solver", "solver_from_dict", "register_solver", "PCGSolver",
     "PBiCGSTABSolver", "MixedPrecisionPCGSolver", "DICPreconditioner", "DILUPreconditioner", "Preconditioner",
-    "ConvergenceInfo", "ResidualMonitor", "BatchedPCGSolver",
+    "ConvergenceInfo", "ResidualMonitor", "BatchedPCGSolver", "assemble_pressure_equation",
+    "solve_pressure_equation",
 ]

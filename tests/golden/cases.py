@@ -142,3 +142,35 @@ def unroll_case(N: int = 10, dt: float = 1e-3, steps: int = 20, seed: int = 4) -
     d.update(gamma=gamma, x0=x0, target=x, dt=dt, steps=steps)
     d["mesh"] = mesh_from_arrays(d)
     return d
+
+
+DLAP_FIXTURE = os.path.join(HERE, "reference_dlap.npz")
+DLAP_CASES = ("j6_face", "j6_cell", "j6_scalar", "j6_float", "two_float", "two_scalar",
+              "two_face")
+
+
+def dlap_case(tag: str) -> dict:
+    """Inputs of one DifferentiableLaplacian golden (make_golden.py --dlap):
+    the mesh arrays, phi, the loss weights g (grad_output) and D as
+    ``(kind, value)`` with kind in face / cell / scalar (0-d tensor) /
+    float."""
+    z = np.load(DLAP_FIXTURE)
+    kind = tag.split("_", 1)[1]
+    if tag.startswith("j6"):
+        jc = jitter_case(6, seed=1)
+        d = {k: jc[k] for k in ("owner", "neighbour", "face_areas", "delta", "volumes",
+                                "cell_centres", "face_centres")}
+        d["n_cells"], d["n_internal"] = int(jc["n_cells"]), int(jc["n_internal"])
+        d["phi"], d["g"] = z["j6_phi"], jc["w"]
+        D = {"face": jc["gamma"], "cell": np.random.default_rng(7).lognormal(0.0, 1.0, d["n_cells"]),
+             "scalar": 1.5, "float": 2.0}[kind]
+    else:
+        d = {k: z[f"two_{k}"] for k in ("owner", "neighbour", "face_areas", "delta", "volumes",
+                                          "cell_centres", "face_centres")}
+        d["n_cells"], d["n_internal"] = 2, int(z["two_n_internal"])
+        d["phi"], d["g"] = np.array([1.0, 2.0]), np.ones(2)
+        nf = d["owner"].shape[0]
+        D = {"face": np.linspace(0.5, 1.5, nf), "scalar": 1.5, "float": 1.0}[kind]
+    d["kind"], d["D"] = kind, D
+    d["expect"] = {k[len(tag) + 1:]: z[k] for k in z.files if k.startswith(tag + "_")}
+    return d

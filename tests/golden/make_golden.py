@@ -3,6 +3,7 @@
 Run in a checkout that has the reference project next to it:
 
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --dlap
 
 It imports the reference's own classes (``pyfoam.core.ldu_matrix``,
 ``pyfoam.solvers.*``, ``pyfoam.discretisation.operators.fvm``,
@@ -167,5 +168,115 @@ def main(ref_root: str) -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+# 2-cell stacked-cube mesh of the reference's differentiable-operator unit
+# tests (tests/unit/differentiable/test_operators.py:26-72): points, faces,
+# owner / neighbour and patches as given there.
+_TWO_CELL_POINTS = [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1],
+                    [0, 1, 1], [0, 0, 2], [1, 0, 2], [1, 1, 2], [0, 1, 2]]
+_TWO_CELL_FACES = [[4, 5, 6, 7], [0, 3, 2, 1], [0, 1, 5, 4], [3, 7, 6, 2], [0, 4, 7, 3],
+                   [1, 2, 6, 5], [8, 9, 10, 11], [4, 5, 9, 8], [7, 11, 10, 6], [4, 8, 11, 7],
+                   [5, 6, 10, 9]]
+_TWO_CELL_OWNER = [0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1]
+
+
+def dlap(ref_root: str) -> None:
+    """DifferentiableLaplacian forward / backward goldens
+    (differentiable/operators.py:409-643) and the pressure-equation caller
+    (solvers/pressure_equation.py:49-184) -> reference_dlap.npz."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import torch
+    from pyfoam.core.dtype import INDEX_DTYPE
+    from pyfoam.differentiable.operators import DifferentiableLaplacian
+    from pyfoam.mesh.fv_mesh import FvMesh
+
+    torch.set_num_threads(8)
+    t = torch.from_numpy
+    out = {}
+
+    def run(tag, mesh, phi, D, g):
+        ph = t(phi).clone().requires_grad_(True)
+        Dt = D
+        if isinstance(D, np.ndarray):
+            Dt = t(D).clone().requires_grad_(True)
+        elif isinstance(D, torch.Tensor):
+            Dt = D.clone().requires_grad_(True)
+        lap = DifferentiableLaplacian.apply(ph, Dt, mesh)
+        (lap * t(g)).sum().backward()
+        out[f"{tag}_lap"] = lap.detach().numpy().copy()
+        out[f"{tag}_grad_phi"] = ph.grad.numpy().copy()
+        if isinstance(Dt, torch.Tensor):
+            out[f"{tag}_grad_D"] = Dt.grad.numpy().copy()
+
+    # jittered 6^3 mesh: per-face, per-cell, 0-d tensor and float D
+    jc = jitter_case(6, seed=1)
+    mesh = jc["mesh"]
+    rng = np.random.default_rng(8)
+    phi = rng.uniform(-1.0, 1.0, mesh.n_cells)
+    out["j6_phi"] = phi
+    dcell = np.random.default_rng(7).lognormal(0.0, 1.0, mesh.n_cells)
+    run("j6_face", mesh, phi, jc["gamma"], jc["w"])
+    run("j6_cell", mesh, phi, dcell, jc["w"])
+    run("j6_scalar", mesh, phi, torch.tensor(1.5, dtype=torch.float64), jc["w"])
+    run("j6_float", mesh, phi, 2.0, jc["w"])
+
+    # the reference unit-test mesh
+    m2 = FvMesh(points=torch.tensor(_TWO_CELL_POINTS, dtype=torch.float64),
+                faces=[torch.tensor(f, dtype=INDEX_DTYPE) for f in _TWO_CELL_FACES],
+                owner=torch.tensor(_TWO_CELL_OWNER, dtype=INDEX_DTYPE),
+                neighbour=torch.tensor([1], dtype=INDEX_DTYPE),
+                boundary=[{"name": "bottom", "type": "wall", "startFace": 1, "nFaces": 5},
+                          {"name": "top", "type": "wall", "startFace": 6, "nFaces": 5}])
+    m2.compute_geometry()
+    for k, a in (("owner", m2.owner), ("neighbour", m2.neighbour), ("face_areas", m2.face_areas),
+                 ("delta", m2.delta_coefficients), ("volumes", m2.cell_volumes),
+                 ("cell_centres", m2.cell_centres), ("face_centres", m2.face_centres)):
+        out[f"two_{k}"] = a.numpy().copy()
+    out["two_n_internal"] = np.int64(m2.n_internal_faces)
+    ones = np.ones(2)
+    run("two_float", m2, np.array([1.0, 2.0]), 1.0, ones)
+    run("two_scalar", m2, np.array([1.0, 2.0]), torch.tensor(1.5, dtype=torch.float64), ones)
+    run("two_face", m2, np.array([1.0, 2.0]), np.linspace(0.5, 1.5, m2.n_faces), ones)
+
+    # assemble_pressure_equation / solve_pressure_equation on the jittered
+    # 6^3 mesh (solvers/pressure_equation.py:49-184)
+    from pyfoam.discretisation.weights import compute_centre_weights
+    from pyfoam.solvers.pcg import PCGSolver
+    from pyfoam.solvers.pressure_equation import (assemble_pressure_equation,
+                                                  solve_pressure_equation)
+
+    prng = np.random.default_rng(9)
+    A_p = prng.uniform(0.5, 3.0, mesh.n_cells) * np.where(prng.random(mesh.n_cells) < 0.2, -1, 1)
+    A_p[3] = 0.0  # clamp to 1e-30
+    phiH = prng.uniform(-1.0, 1.0, mesh.n_faces)
+    wts = compute_centre_weights(mesh.cell_centres, mesh.face_centres, mesh.owner,
+                                 mesh.neighbour, mesh.n_internal_faces, mesh.n_faces,
+                                 dtype=torch.float64)
+    peq = assemble_pressure_equation(t(phiH), t(A_p), mesh, face_weights=wts)
+    out["p_A_p"], out["p_phiHbyA"] = A_p, phiH
+    for k in ("lower", "upper", "diag", "source"):
+        out[f"p_{k}"] = getattr(peq, k).numpy().copy()
+    # a well-posed solve: A_p > 0, pinned reference cell
+    A_s = prng.uniform(0.5, 3.0, mesh.n_cells)
+    out["p_A_s"] = A_s
+    peq = assemble_pressure_equation(t(phiH), t(A_s), mesh, face_weights=wts)
+    psol = PCGSolver(tolerance=0.0, rel_tol=1e-6, max_iter=2000, preconditioner="DIC")
+    p_new, p_it, p_res = solve_pressure_equation(peq, torch.zeros(mesh.n_cells,
+                                                                  dtype=torch.float64),
+                                                 psol, tolerance=0.0, max_iter=2000,
+                                                 reference_cell=5)
+    out["p_x"], out["p_iterations"], out["p_residual"] = (p_new.numpy().copy(), np.int64(p_it),
+                                                          np.float64(p_res))
+    print("pressure", p_it, p_res, flush=True)
+
+    path = os.path.join(HERE, "reference_dlap.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYFOAM_REFERENCE", ""))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else os.environ.get("PYFOAM_REFERENCE", "")
+    if "--dlap" in sys.argv:
+        dlap(root)
+    else:
+        main(root)

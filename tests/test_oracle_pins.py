@@ -6,7 +6,9 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.golden.cases import FIXTURE, c1_poisson, jitter_case, random_ldu, sha
+from tests.golden.cases import (
+    DLAP_CASES, DLAP_FIXTURE, FIXTURE, c1_poisson, dlap_case, jitter_case, random_ldu, sha,
+)
 
 G = np.load(FIXTURE)
 
@@ -133,3 +135,62 @@ def test_oracle_dls_gradients_against_reference():
                      (gu, "dls_grad_upper")):
         ref = G[key]
         assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max(), key
+
+
+@pytest.mark.parametrize("tag", DLAP_CASES)
+def test_oracle_differentiable_laplacian_against_reference(tag):
+    """DifferentiableLaplacian forward, phi-gradient and D-gradient
+    (differentiable/operators.py:421-643) on the jittered 6^3 mesh and the
+    reference's own 2-cell unit-test mesh: bitwise, except the 0-d D
+    gradient (torch's sum order) to 1e-13 relative."""
+    d = dlap_case(tag)
+    own, nei, nf = d["owner"], d["neighbour"], d["owner"].shape[0]
+    if d["kind"] == "face":
+        Df = d["D"]
+    elif d["kind"] == "cell":
+        w = O.centre_weights(own, nei, d["cell_centres"], d["face_centres"])
+        Df = O.face_values(own, nei, d["D"], w)
+    else:
+        Df = np.full(nf, float(d["D"]))
+    args = (d["n_cells"], own, nei, d["face_areas"], d["delta"], Df, d["volumes"])
+    e = d["expect"]
+    assert (O.explicit_laplacian(*args, d["phi"]).view(np.int64) == e["lap"].view(np.int64)).all()
+    assert (O.explicit_laplacian(*args, d["g"]).view(np.int64)
+            == e["grad_phi"].view(np.int64)).all()
+    if "grad_D" in e:
+        gf = O.explicit_laplacian_grad_d(own, nei, d["face_areas"], d["delta"], d["volumes"],
+                                         d["phi"], d["g"])
+        if d["kind"] == "face":
+            assert (gf.view(np.int64) == e["grad_D"].view(np.int64)).all()
+        elif d["kind"] == "cell":
+            gc = O.face_grad_to_cells(d["n_cells"], own, nei, gf)
+            assert (gc.view(np.int64) == e["grad_D"].view(np.int64)).all()
+        else:
+            np.testing.assert_allclose(gf.sum(), e["grad_D"], rtol=1e-13, atol=0)
+    else:
+        assert d["kind"] == "float"
+
+
+def test_oracle_pressure_equation_against_reference():
+    """assemble_pressure_equation (bitwise, including a negative and a zero
+    A_p) and solve_pressure_equation (pinned cell, PCG+DIC) on the jittered
+    6^3 mesh, solvers/pressure_equation.py:49-184."""
+    z = np.load(DLAP_FIXTURE)
+    jc = jitter_case(6, seed=1)
+    own, nei, n = jc["owner"], jc["neighbour"], int(jc["n_cells"])
+    w = O.centre_weights(own, nei, jc["cell_centres"], jc["face_centres"])
+    args = (n, own, nei, jc["face_areas"], jc["delta"], w)
+    lo, up, dg, src = O.pressure_assemble(*args, z["p_A_p"], jc["volumes"], z["p_phiHbyA"])
+    for k, a in (("lower", lo), ("upper", up), ("diag", dg), ("source", src)):
+        assert (a.view(np.int64) == z[f"p_{k}"].view(np.int64)).all(), k
+    lo, up, dg, src = O.pressure_assemble(*args, z["p_A_s"], jc["volumes"], z["p_phiHbyA"])
+    large = max(abs(dg[5]), 1.0) * 1e10  # FvMatrix.set_reference, core/fv_matrix.py:241-259
+    dg[5] += large
+    src[5] += large * 0.0
+    nint = nei.shape[0]
+    pd = O.dic_build(own[:nint], nei, dg, up)
+    r = O.pcg(own[:nint], nei, dg, lo, up, src, np.zeros(n), pd, tolerance=0.0, rel_tol=1e-6,
+              max_iter=2000)
+    assert r.iterations == int(z["p_iterations"])
+    np.testing.assert_allclose(r.final_residual, z["p_residual"], rtol=1e-9)
+    np.testing.assert_allclose(r.x, z["p_x"], rtol=0, atol=1e-9 * np.abs(z["p_x"]).max())
