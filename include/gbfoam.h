@@ -39,6 +39,7 @@ extern "C" {
 #define GBF_CONVERGED 1
 #define GBF_BREAKDOWN 2
 #define GBF_MAX_ITER 3
+#define GBF_DEVICE_TIMEOUT 4 /* a bounded wait inside a kernel ran out; results invalid */
 
 /* Cell-sliced LDU addressing (built once per mesh topology).
  *
@@ -75,6 +76,10 @@ typedef struct gbf_layout {
 
 /* ---- library ----------------------------------------------------------- */
 const char* gbf_last_error(void);
+/* Reads and clears the fault flag of the stand-alone staged Amul kernels
+ * (set when a bounded wait on a bulk copy ran out; their output is then
+ * invalid).  No reference counterpart.                                     */
+int gbf_stream_fault(int32_t* fault);
 int gbf_version(void);
 /* Number of SMs of the current device (grid sizing of the reductions).     */
 int gbf_device_sm_count(int32_t* n_sm);

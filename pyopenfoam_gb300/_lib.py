@@ -29,9 +29,10 @@ __all__ = [
     "GBF_CONVERGED",
     "GBF_BREAKDOWN",
     "GBF_MAX_ITER",
+    "GBF_DEVICE_TIMEOUT",
 ]
 
-GBF_RUNNING, GBF_CONVERGED, GBF_BREAKDOWN, GBF_MAX_ITER = 0, 1, 2, 3
+GBF_RUNNING, GBF_CONVERGED, GBF_BREAKDOWN, GBF_MAX_ITER, GBF_DEVICE_TIMEOUT = 0, 1, 2, 3, 4
 
 _c_i32 = ctypes.c_int32
 _c_i64 = ctypes.c_int64
@@ -142,6 +143,7 @@ EXPORTED: dict[str, tuple] = {
     "gbf_explicit_laplacian_grad_d_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp,
                                                          _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                                          _c_vp, _c_vp, _c_vp]),
+    "gbf_stream_fault": (ctypes.c_int, [_c_vp]),
     "gbf_pack_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pack_f64_to_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp]),

@@ -1,7 +1,12 @@
 // Coefficient packing and the stand-alone Amul entry points.
-#include "amul.cuh"
+#include <type_traits>
+
+#include "bulk.cuh"
 
 namespace gbf {
+
+// Set by a staged Amul block whose bounded wait ran out (gbf_stream_fault).
+static __device__ unsigned int g_stream_fault;
 
 // One thread per lane of every slice (padding lanes of the last slice
 // included, so that all slots are written).
@@ -30,6 +35,34 @@ __global__ void __launch_bounds__(kBlock)
                 const T* __restrict__ x, A* __restrict__ y) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += gridDim.x * blockDim.x)
     y[c] = cell_amul_k<KIND, T, A, NEI_FIRST>(L, coef, diag, x, c, __ldg(x + c));
+}
+
+// FP32 Amul of a hex 3+3 layout with the coefficient / x / diagonal stream
+// staged through shared memory by bulk asynchronous copies; the cells of the
+// last, partial tile are computed from global memory by one block.
+template <typename A, bool NEI_FIRST>
+__global__ void __launch_bounds__(kTileCells, 8)
+    amul_stream_kernel(gbf_layout L, const float* __restrict__ coef,
+                       const float* __restrict__ diag, const float* __restrict__ x,
+                       A* __restrict__ y, int n_tiles) {
+  __shared__ HexRing ring;
+  const bool ok = hex_stream_tiles<A, NEI_FIRST>(ring, n_tiles, coef, x, diag, L.slot_dm,
+                                                 [&](int c, A v, float) { y[c] = v; });
+  if (blockIdx.x == n_tiles % gridDim.x) {
+    const int c = n_tiles * kTileCells + threadIdx.x;
+    if (c < L.n_cells)
+      y[c] = cell_amul_fixed<float, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, __ldg(x + c));
+  }
+  if (!ok && threadIdx.x == 0) atomicExch(&g_stream_fault, 1u);
+}
+
+template <typename A, bool NEI_FIRST>
+static void launch_amul_stream(const gbf_layout* L, const float* coef, const float* diag,
+                               const float* x, A* y, cudaStream_t s) {
+  const int n_tiles = L->n_cells / kTileCells;
+  const int grid = wave_grid(amul_stream_kernel<A, NEI_FIRST>, kTileCells,
+                             (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells);
+  amul_stream_kernel<A, NEI_FIRST><<<grid, kTileCells, 0, s>>>(*L, coef, diag, x, y, n_tiles);
 }
 
 template <int KIND, typename T, typename A, bool NEI_FIRST>
@@ -70,6 +103,16 @@ static int amul(const gbf_layout* L, const T* coef, const T* diag, const T* x, A
   GBF_REQUIRE(diag && x && y && (L->n_faces == 0 || coef), "amul: NULL pointer");
   cudaStream_t s = as_stream(stream);
   const bool hex = layout_kind(*L) == kLayoutHex33;
+  if constexpr (std::is_same<T, float>::value) {
+    if (hex && hex_stream_aligned(coef, x, diag, L->slot_dm)) {
+      if (nei_first)
+        launch_amul_stream<A, true>(L, coef, diag, x, y, s);
+      else
+        launch_amul_stream<A, false>(L, coef, diag, x, y, s);
+      GBF_CHECK_LAUNCH();
+      return GBF_OK;
+    }
+  }
   if (nei_first) {
     if (hex)
       launch_amul<kLayoutHex33, T, A, true>(L, coef, diag, x, y, s);
@@ -86,6 +129,15 @@ static int amul(const gbf_layout* L, const T* coef, const T* diag, const T* x, A
 }
 
 }  // namespace gbf
+
+extern "C" int gbf_stream_fault(int32_t* fault) {
+  GBF_REQUIRE(fault, "stream_fault: NULL pointer");
+  unsigned int v = 0, zero = 0;
+  GBF_CHECK_CUDA(cudaMemcpyFromSymbol(&v, gbf::g_stream_fault, sizeof(v)));
+  GBF_CHECK_CUDA(cudaMemcpyToSymbol(gbf::g_stream_fault, &zero, sizeof(zero)));
+  *fault = (int32_t)v;
+  return GBF_OK;
+}
 
 extern "C" int gbf_pack_f64(const gbf_layout* L, const double* own_src, const double* nei_src,
                             double* slot_coef, void* stream) {

@@ -1,0 +1,197 @@
+// Shared-memory staging of the FP32 Amul stream with bulk asynchronous
+// copies (cp.async.bulk, completion counted on an mbarrier).
+//
+// For a layout whose slices all have 3 owner-side and 3 neighbour-side slots,
+// every slot offset-uniform (layout_kind == kLayoutHex33), the bytes a block
+// of 256 cells streams from HBM are contiguous per 8-slice tile:
+//   coefficients 8*6*32 floats (6144 B), x 256 floats (1024 B),
+//   diagonal 256 floats (1024 B), {delta, mask} entries 8*6 int2 (384 B).
+// One thread of the block issues the four copies of a tile into a ring of
+// kStages stage buffers; all threads wait on the stage's mbarrier, compute
+// their cell from shared memory (the neighbour x values are gathered from
+// global memory through L1/L2) and release the stage with a block barrier,
+// after which the issuing thread refills it with the tile kStages ahead.
+// The HBM stream therefore stays in flight independently of the registers
+// the gather needs.
+//
+// Every wait is bounded: after kWaitPolls unsuccessful polls the block
+// records a fault, drains (again bounded) the copies it has in flight and
+// stops streaming; the host turns the fault into GBF_DEVICE_TIMEOUT.
+#pragma once
+
+#include "amul.cuh"
+
+namespace gbf {
+
+constexpr int kTileCells = 256;
+constexpr int kTileSlices = kTileCells / 32;
+constexpr int kHexW = 6;
+constexpr int kStages = 3;
+constexpr int kWaitPolls = 1 << 20;
+
+struct __align__(128) HexStage {
+  float coef[kTileSlices * kHexW * 32];
+  float x[kTileCells];
+  float d[kTileCells];
+  int2 dm[kTileSlices * kHexW];
+};
+constexpr unsigned kStageBytes = sizeof(float) * (kTileSlices * kHexW * 32 + 2 * kTileCells) +
+                                 sizeof(int2) * kTileSlices * kHexW;
+static_assert(kStageBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+
+struct HexRing {
+  HexStage stage[kStages];
+  unsigned long long bar[kStages];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+// Makes initialised barriers visible to the asynchronous proxy.
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (int i = 0; i < kWaitPolls; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// dst and src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Issues the four copies of tile t into stage s (one thread).
+__device__ __forceinline__ void hex_issue(HexRing& R, int s, int t, const float* coef,
+                                          const float* x, const float* d, const int* slot_dm) {
+  HexStage& S = R.stage[s];
+  mbar_arrive_expect_tx(&R.bar[s], kStageBytes);
+  bulk_g2s(S.coef, coef + (size_t)t * (kTileSlices * kHexW * 32), sizeof(S.coef), &R.bar[s]);
+  bulk_g2s(S.x, x + (size_t)t * kTileCells, sizeof(S.x), &R.bar[s]);
+  bulk_g2s(S.d, d + (size_t)t * kTileCells, sizeof(S.d), &R.bar[s]);
+  bulk_g2s(S.dm, slot_dm + (size_t)t * (2 * kTileSlices * kHexW), sizeof(S.dm), &R.bar[s]);
+}
+
+// (A x)[c] of thread `tid` of the tile in stage S: the products and the
+// summation order of cell_amul_fixed<float, A, NEI_FIRST, 3, 3>.
+template <typename A, bool NEI_FIRST>
+__device__ __forceinline__ A hex_cell_from_stage(const HexStage& S, int tid,
+                                                 const float* __restrict__ x, int c) {
+  const int sl = tid >> 5, lane = tid & 31;
+  float a[kHexW], xv[kHexW];
+  bool on[kHexW];
+#pragma unroll
+  for (int k = 0; k < kHexW; ++k) a[k] = S.coef[(sl * kHexW + k) * 32 + lane];
+#pragma unroll
+  for (int k = 0; k < kHexW; ++k) {
+    const int2 e = S.dm[sl * kHexW + k];
+    on[k] = ((unsigned)e.y >> lane) & 1u;
+    xv[k] = on[k] ? __ldg(x + c + e.x) : 0.0f;
+  }
+  A so = (A)0, sn = (A)0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (on[k]) so = add_rn(so, (A)__fmul_rn(a[k], xv[k]));
+#pragma unroll
+  for (int k = 3; k < kHexW; ++k)
+    if (on[k]) sn = add_rn(sn, (A)__fmul_rn(a[k], xv[k]));
+  A y = (A)__fmul_rn(S.d[tid], S.x[tid]);
+  if (NEI_FIRST) {
+    y = add_rn(y, sn);
+    return add_rn(y, so);
+  }
+  y = add_rn(y, so);
+  return add_rn(y, sn);
+}
+
+// True when the pointers the staged path streams from are 16-byte aligned.
+inline bool hex_stream_aligned(const void* coef, const void* x, const void* d,
+                               const void* slot_dm) {
+  return ((reinterpret_cast<uintptr_t>(coef) | reinterpret_cast<uintptr_t>(x) |
+           reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(slot_dm)) &
+          15u) == 0;
+}
+
+// Runs f(c, y, xc) for every cell of the full tiles assigned to this block
+// (tiles blockIdx.x, blockIdx.x + gridDim.x, ...).  Returns false if a wait
+// ran out (the block then stops streaming after draining its copies).
+template <typename A, bool NEI_FIRST, typename F>
+__device__ __forceinline__ bool hex_stream_tiles(HexRing& R, int n_tiles, const float* coef,
+                                                 const float* x, const float* d,
+                                                 const int* slot_dm, F&& f) {
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&R.bar[s], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  int issued = 0;  // tiles issued by thread 0 (valid in thread 0)
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      const int t = blockIdx.x + s * gridDim.x;
+      if (t >= n_tiles) break;
+      hex_issue(R, s, t, coef, x, d, slot_dm);
+      ++issued;
+    }
+  }
+  bool ok = true;
+  int k = 0;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
+    const int s = k % kStages;
+    const unsigned parity = (unsigned)(k / kStages) & 1u;
+    const bool got = mbar_wait(&R.bar[s], parity);
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    const int c = t * kTileCells + tid;
+    f(c, hex_cell_from_stage<A, NEI_FIRST>(R.stage[s], tid, x, c), R.stage[s].x[tid]);
+    __syncthreads();  // every thread is done with stage s
+    if (tid == 0) {
+      const int tn = t + kStages * gridDim.x;
+      if (tn < n_tiles) {
+        hex_issue(R, s, tn, coef, x, d, slot_dm);
+        ++issued;
+      }
+    }
+  }
+  if (!ok && tid == 0) {
+    // drain: wait (bounded) for every issued stage not yet consumed
+    for (int j = k; j < issued; ++j) mbar_wait(&R.bar[j % kStages], (unsigned)(j / kStages) & 1u);
+  }
+  __syncthreads();
+  return ok;
+}
+
+}  // namespace gbf

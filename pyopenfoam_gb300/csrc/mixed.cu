@@ -30,7 +30,7 @@
 #include <math.h>
 #include <string.h>
 
-#include "amul.cuh"
+#include "bulk.cuh"
 
 namespace gbf {
 
@@ -38,7 +38,7 @@ enum { MP_NORMAL = 0, MP_TRUE_RESIDUAL = 1 };
 
 struct MixedState {
   double rz, alpha, beta, res0, res, rmax, target, pAp;
-  int inner, status, n_hist, phase, fold_pending, updates, pad0, pad1;
+  int inner, status, n_hist, phase, fold_pending, updates, fault, pad1;
   unsigned int ticket[8];
 };
 
@@ -147,6 +147,51 @@ __global__ void __launch_bounds__(kBlock)
       MixedState* st = v.st;
       st->pAp = pAp;
       if (fabs(pAp) < 1e-30)
+        st->status = GBF_BREAKDOWN;
+      else
+        st->alpha = st->rz / pAp;
+    }
+  }
+}
+
+// K_ap for a hex 3+3 layout: the coefficient / p / diagonal stream of each
+// 256-cell tile is staged in shared memory by bulk asynchronous copies
+// (bulk.cuh); the cells of the last, partial tile come from global memory.
+// A wait that runs out records st->fault, which the last block turns into
+// GBF_DEVICE_TIMEOUT once every block has arrived.
+__global__ void __launch_bounds__(kTileCells, 8)
+    mp_ap_stream_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v,
+                        int n_tiles) {
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ HexRing ring;
+  __shared__ double sh[kTileCells / 32];
+  const int G = gridDim.x;
+  DFAcc a;
+  const bool ok = hex_stream_tiles<float, false>(ring, n_tiles, coef32, v.p, v.d32, L.slot_dm,
+                                                 [&](int c, float y, float pc) {
+                                                   v.Ap[c] = y;
+                                                   a.add_prod(pc, y);
+                                                 });
+  if (blockIdx.x == n_tiles % G) {
+    const int c = n_tiles * kTileCells + threadIdx.x;
+    if (c < L.n_cells) {
+      const float pc = __ldg(v.p + c);
+      const float y = cell_amul_fixed<float, float, false, 3, 3>(L, coef32, v.d32, v.p, c, pc);
+      v.Ap[c] = y;
+      a.add_prod(pc, y);
+    }
+  }
+  if (!ok && threadIdx.x == 0) atomicExch(&v.st->fault, 1);
+  const double acc = block_sum(a.value(), sh);
+  if (threadIdx.x == 0) v.partials[blockIdx.x] = acc;
+  if (last_block_done(&v.st->ticket[1])) {
+    const double pAp = reduce_partials(v.partials, G, sh);
+    if (threadIdx.x == 0) {
+      MixedState* st = v.st;
+      st->pAp = pAp;
+      if (__ldcg(&st->fault))
+        st->status = GBF_DEVICE_TIMEOUT;
+      else if (fabs(pAp) < 1e-30)
         st->status = GBF_BREAKDOWN;
       else
         st->alpha = st->rz / pAp;
@@ -380,8 +425,15 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   // one full wave of resident blocks per kernel (each reduces its own partials)
   const int Gi = wave_grid(mp_init_kernel, kBlock, n);
   const bool hex = layout_kind(*L) == kLayoutHex33;
-  const int Ga = hex ? wave_grid(mp_ap_kernel<kLayoutHex33>, kBlock, n)
-                     : wave_grid(mp_ap_kernel<kLayoutGeneric>, kBlock, n);
+  // staged K_ap: hex layout, 16-byte aligned coefficient / vector streams
+  // (the workspace vectors are 256-byte aligned)
+  const bool staged = hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
+  const int n_tiles = n / kTileCells;
+  const int Ga = staged ? wave_grid(mp_ap_stream_kernel, kTileCells,
+                                    (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells)
+                 : hex  ? wave_grid(mp_ap_kernel<kLayoutHex33>, kBlock, n)
+                        : wave_grid(mp_ap_kernel<kLayoutGeneric>, kBlock, n);
+  const int Ba = staged ? kTileCells : kBlock;
   const int Gu = wave_grid(mp_update_kernel, kBlock, (n + 3) / 4);
   const int Gt = wave_grid(mp_true_kernel, kBlock, n);
   const int Gp = wave_grid(mp_p_kernel, kBlock, (n + 3) / 4);
@@ -400,10 +452,12 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   while (hs.status == GBF_RUNNING && launched < limit) {
     for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
       const bool tb = timing_begin(kProbeMixedAp, s);
-      if (hex)
-        mp_ap_kernel<kLayoutHex33><<<Ga, kBlock, 0, s>>>(*L, coef32, v);
+      if (staged)
+        mp_ap_stream_kernel<<<Ga, Ba, 0, s>>>(*L, coef32, v, n_tiles);
+      else if (hex)
+        mp_ap_kernel<kLayoutHex33><<<Ga, Ba, 0, s>>>(*L, coef32, v);
       else
-        mp_ap_kernel<kLayoutGeneric><<<Ga, kBlock, 0, s>>>(*L, coef32, v);
+        mp_ap_kernel<kLayoutGeneric><<<Ga, Ba, 0, s>>>(*L, coef32, v);
       if (tb) timing_end(kProbeMixedAp, s);
       mp_update_kernel<<<Gu, kBlock, 0, s>>>(n, x, v, delta, *P);
       mp_true_kernel<<<Gt, kBlock, 0, s>>>(*L, coef64, diag64, b, x, v, hist, hist_cap, *P);

@@ -90,6 +90,9 @@ class MixedPrecisionPCGSolver(LinearSolverBase):
             "gbf_mixed_pcg_solve",
         )
         self.last_result = R
+        if R.status == _lib.GBF_DEVICE_TIMEOUT:
+            raise RuntimeError("gbf_mixed_pcg_solve: a bounded wait on a staged copy ran out "
+                               "inside the Amul kernel; the result is invalid")
         nh = min(R.outer_updates + 1, cap) if n > 0 else 1
         monitor.record(hist[:nh].tolist() if n > 0 else [0.0])
         info = monitor.build_info(converged=(R.status == _lib.GBF_CONVERGED))

@@ -173,3 +173,46 @@ def test_offset_compression_gives_identical_bits():
             assert (topo.layout.uniform_wo, topo.layout.uniform_wn) == (3, 3)
         else:
             assert topo.layout.all_uniform == 0
+
+
+@pytest.mark.parametrize("N", [20, 64])
+def test_staged_float32_amul_matches_generic_gather(N):
+    """The FP32 hex Amul with bulk-copy staging (N^3 = 8000 cells leaves a
+    partial 64-cell tile, 64^3 is whole tiles) gives the same bits as the
+    generic per-slot gather and as the float oracle, forward and transposed,
+    float and float64 accumulation; no bounded wait ran out."""
+    import ctypes
+
+    from pyopenfoam_gb300 import _lib
+
+    c = random_ldu(N, 17, False)
+    m = mat(c["n"], c["owner"], c["neighbour"], c["diag"], c["lower"], c["upper"])
+    topo = m.topology()
+    assert topo.layout.all_uniform == 1
+    L = _lib.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    d32 = m.diag.float().contiguous()
+    x32 = torch.as_tensor(c["x"]).float().cuda()
+    var = topo.variable_width_layout()
+    for transposed in (False, True):
+        coef32 = m.packed(transposed=transposed, dtype=torch.float32)
+        for fn, dt in ((L.gbf_amul_f32, torch.float32), (L.gbf_amul_f32_f64out, torch.float64)):
+            y1 = torch.empty(c["n"], device=DEV, dtype=dt)
+            y2 = torch.empty_like(y1)
+            _lib.check(fn(topo.layout_ref, coef32.data_ptr(), d32.data_ptr(), x32.data_ptr(),
+                          y1.data_ptr(), int(transposed), st))
+            _lib.check(fn(ctypes.byref(var), coef32.data_ptr(), d32.data_ptr(), x32.data_ptr(),
+                          y2.data_ptr(), int(transposed), st))
+            a, b = y1.cpu().numpy(), y2.cpu().numpy()
+            assert (a.view(np.uint8) == b.view(np.uint8)).all()
+        if not transposed:
+            ref = O.amul(c["owner"], c["neighbour"], c["diag"].astype(np.float32),
+                         c["lower"].astype(np.float32), c["upper"].astype(np.float32),
+                         c["x"].astype(np.float32), float_accumulate=True)
+            y = torch.empty(c["n"], device=DEV, dtype=torch.float32)
+            _lib.check(L.gbf_amul_f32(topo.layout_ref, coef32.data_ptr(), d32.data_ptr(),
+                                      x32.data_ptr(), y.data_ptr(), 0, st))
+            np.testing.assert_array_equal(y.cpu().numpy(), ref)
+    fault = ctypes.c_int32(-1)
+    _lib.check(L.gbf_stream_fault(ctypes.byref(fault)))
+    assert fault.value == 0
