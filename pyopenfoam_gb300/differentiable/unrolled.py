@@ -20,6 +20,7 @@ explicit one used by the benchmark.
 
 from __future__ import annotations
 
+import math
 import time
 from dataclasses import dataclass, field
 
@@ -88,6 +89,22 @@ class UnrolledImplicitDiffusion:
         At.diag, At.lower, At.upper = A.diag, A.upper, A.lower
         return At
 
+    def _solve_normalised(self, A: LduMatrix, b: torch.Tensor, x0: torch.Tensor):
+        """Solve A x = b with b and x0 scaled by the power of two that brings
+        max|b| into [0.5, 1), and the solution scaled back.  Power-of-two
+        scaling is exact, so the iterates are those of the unscaled solve
+        multiplied by 2^k -- except that the solver's absolute thresholds
+        (the 1e-30 breakdown test on p.Ap) no longer stop a solve whose
+        right-hand side is tiny (adjoint and difference systems) before it
+        reaches its relative tolerance."""
+        m = float(b.abs().max()) if b.numel() else 0.0
+        if m == 0.0 or not math.isfinite(m):
+            return self.solver(A, b, x0)
+        k = -math.frexp(m)[1]
+        s, inv = math.ldexp(1.0, k), math.ldexp(1.0, -k)
+        x, it, res = self.solver(A, b * s, x0 * s)
+        return x * inv, it, res * inv
+
     def _step(self, A: LduMatrix, x: torch.Tensor) -> torch.Tensor:
         # warm start from the previous state
         xn, it, _ = self.solver(A, x / self.dt, x)
@@ -129,7 +146,7 @@ class UnrolledImplicitDiffusion:
                 seg[t] = x
             seg[e] = xT if e == self.steps else ckpt[e]
             for t in range(e, s, -1):
-                lam, it, _ = self.solver(At, g, torch.zeros_like(g))
+                lam, it, _ = self._solve_normalised(At, g, torch.zeros_like(g))
                 self.stats.iterations.append(it)
                 self.stats.backward_solves += 1
                 xt = seg[t].contiguous()
@@ -176,7 +193,11 @@ class UnrolledImplicitDiffusion:
         differ by a factor << 2, so their differences are exact by
         Sterbenz's lemma).  Solving for d instead of subtracting x+ from x-
         keeps the quotient accurate to the solver tolerance relative to |d|
-        rather than |x|; L+ - L- = sum d (x+ + x- - 2 target)."""
+        rather than |x|; L+ - L- = sum d (x+ + x- - 2 target).  The
+        difference systems are solved with power-of-two normalisation
+        (``_solve_normalised``): |d| is ~2h |dx/dgamma|, small enough that
+        the solver's absolute breakdown threshold would otherwise end the
+        solves early."""
         gp, gm = gamma.clone(), gamma.clone()
         gp[face] += h
         gm[face] -= h
@@ -189,7 +210,7 @@ class UnrolledImplicitDiffusion:
         for _ in range(self.steps):
             xm_next, _, _ = self.solver(Am, xm / self.dt, xm)
             rhs = d / self.dt - dA.Ax(xm_next)
-            d, _, _ = self.solver(Ap, rhs, d)
+            d, _, _ = self._solve_normalised(Ap, rhs, d)
             xm = xm_next
         xp = xm + d
         two_h = float(gp[face] - gm[face])  # the perturbation actually applied (exact)
