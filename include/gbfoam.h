@@ -72,6 +72,11 @@ typedef struct gbf_layout {
   /* optional offset compression (gbf_layout_compress); NULL = use slot_col:
    * per (slice, slot) {column - cell or INT32_MIN, mask of lanes with a face} */
   const int32_t* slot_dm;    /* [2 * n_slots/32]                            */
+  /* optional mirror table for symmetric matrices (gbf_layout_mirror); NULL =
+   * none.  Entry (s, k) of a NEIGHBOUR-side slot k >= wo: the owner-side slot
+   * j that holds the same face in the slice of its owner cell, the same j for
+   * every lane of the slice; -1 on owner-side and hole-only entries.        */
+  const int8_t* slot_mirror; /* [n_slots/32]                                 */
 } gbf_layout;
 
 /* ---- library ----------------------------------------------------------- */
@@ -115,6 +120,18 @@ int gbf_layout_fill(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
  * entry.  n_uniform_h receives the number of compressed entries.           */
 int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off_h, const int32_t* slice_w_h,
                         const int32_t* slot_col_h, int32_t* slot_dm_h, int64_t* n_uniform_h);
+/* Mirror table of a uniform-width offset-compressed layout (uniform wo, all
+ * entries compressed): for every neighbour-side entry (s, k) the owner-side
+ * slot j of the same face in the slice of its owner cell.  *ok = 1 when j is
+ * the same for all lanes of every entry (then a symmetric matrix can be
+ * stored as its owner-side slots only: 32*wo floats per slice, and the
+ * neighbour-side coefficient of lane l is read at owner cell c' = cell +
+ * delta, index 32*wo*(c' >> 5) + 32*j + (c' & 31)); *ok = 0 otherwise.
+ * slot_mirror_h has n_slots/32 entries.  No reference counterpart (the
+ * reference always stores lower and upper, core/ldu_matrix.py:89-100).    */
+int gbf_layout_mirror(int32_t n_faces, int32_t n_slices, int32_t uniform_wo, int32_t uniform_wn,
+                      const int32_t* slot_face_h, const int32_t* owner_h,
+                      const int32_t* slot_dm_h, int8_t* slot_mirror_h, int32_t* ok);
 /* DIC wavefront: level(c) = 1 + max level of the cells j < c that c reads in
  * the reference's cell-ordered factorisation (preconditioners.py:124-128).
  * level_ptr_h has room for n_cells + 1 entries, level_cells_h for n_cells. */
@@ -159,6 +176,15 @@ int gbf_pack_f32(const gbf_layout* L, const float* own_src, const float* nei_src
 int gbf_pack_f64_to_f32(const gbf_layout* L, const double* own_src, const double* nei_src,
                         float* slot_coef, void* stream);
 
+/* Owner-side half of a symmetric FP64 matrix as FP32 (mixed solver): slot
+ * (s, j < wo) of the layout goes to coef_own[32*wo*s + 32*j + lane].  Every
+ * face's lower and upper are compared bit for bit; *differs (a DEVICE int32,
+ * zeroed by this call) becomes 1 if any pair differs, in which case the half
+ * storage does not represent the matrix and the caller keeps the full
+ * packing.  Needs a uniform-width layout.  No reference counterpart.      */
+int gbf_pack_sym_f64_to_f32(const gbf_layout* L, const double* lower, const double* upper,
+                            float* coef_own, int32_t* differs, void* stream);
+
 /* ---- Amul ----------------------------------------------------------------
  * LduMatrix.Ax, core/ldu_matrix.py:172-217 (nei_first = 0, coefficients
  * packed (lower, upper)) and LduMatrix.Ax_T, core/ldu_matrix.py:219-258
@@ -177,6 +203,14 @@ int gbf_amul_f32_f64out(const gbf_layout* L, const float* slot_coef, const float
  * inner operator of the mixed-precision solver.                            */
 int gbf_amul_f32(const gbf_layout* L, const float* slot_coef, const float* diag,
                  const float* x, float* y, int32_t nei_first, void* stream);
+/* gbf_amul_f32 of a symmetric matrix stored as its owner-side half
+ * (gbf_pack_sym_f64_to_f32); the neighbour-side coefficients are read from
+ * the owner cells' slots through L->slot_mirror.  Same products and sums,
+ * so the same bits as gbf_amul_f32 on the full packing.  Needs a hex 3+3
+ * layout (uniform wo = wn = 3, all entries compressed) with slot_mirror.
+ * No reference counterpart.                                                */
+int gbf_amul_sym_f32(const gbf_layout* L, const float* coef_own, const float* diag,
+                     const float* x, float* y, void* stream);
 
 /* ---- preconditioners -----------------------------------------------------
  * DICPreconditioner._build, solvers/preconditioners.py:88-133: level-
@@ -345,10 +379,139 @@ int gbf_explicit_laplacian_grad_d_f64(const gbf_layout* L, int32_t n_faces_total
                                       const double* phi, const double* g, double* g_face,
                                       double* g_cell, double* g_sum, void* stream);
 
+/* ---- smoothers -------------------------------------------------------------
+ * Gauss-Seidel: SmoothSolver's "GaussSeidel" smoother
+ * (solvers/smooth_solver.py:134-187; relax = 0: x_c = (b_c - off)/d_c) and
+ * GaussSeidelSmoother's sweeps (solvers/smoothers.py:63-149; relax = 1:
+ * x_c += omega (new - x_c)).  One sweep in the order of the level schedule
+ * from gbf_gs_schedule (device level_ptr / level_cells, plus the host copy
+ * of level_ptr that sizes the launches); slot_coef is the (lower, upper)
+ * packing; each row sum runs over the cell's faces in ascending face order,
+ * so the sweep is bitwise the reference's sequential loop.                 */
+int gbf_gs_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                    const int32_t* neighbour_h, int32_t reverse, int32_t* level_ptr_h,
+                    int32_t* level_cells_h, int32_t* n_levels, int32_t* max_level_size);
+int gbf_gauss_seidel_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                         const double* b, const int32_t* level_ptr, const int32_t* level_cells,
+                         const int32_t* level_ptr_h, int32_t n_levels, double omega,
+                         int32_t relax, double* x, void* stream);
+/* r = b - A x, A x bitwise LduMatrix.Ax (core/ldu_matrix.py:172-217); the
+ * residual of every smoother and of the smoothing solvers.                 */
+int gbf_residual_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
+                     const double* b, const double* x, double* r, void* stream);
+/* x += (omega / max(|diag|, 1e-30)) z (JacobiSmoother, smoothers.py:152-200)
+ * or, with diag == NULL, x += omega z (the DIC / DILU Richardson updates,
+ * smooth_solver.py:189-232, smoothers.py:203-260).                         */
+int gbf_relax_f64(int32_t n, double omega, const double* diag, const double* z, double* x,
+                  void* stream);
+/* *out (DEVICE) = |r|_2 in a fixed summation order (the residual norm of
+ * solvers/residual.py:112-145); workspace of gbf_norm2_workspace_bytes().  */
+size_t gbf_norm2_workspace_bytes(void);
+int gbf_norm2_f64(int32_t n, const double* r, double* out, void* workspace, void* stream);
+
+/* ---- GAMG ---------------------------------------------------------------------
+ * GAMGSolver (solvers/gamg.py:104-585).  Host, once per mesh topology:
+ * greedy aggregation in cell order (gamg.py:183-245; f2c[n_cells], the
+ * aggregate of each cell) and the coarse faces (gamg.py:249-331; arrays of
+ * n_faces entries, *n_cfaces used; face_to_cface = -1 for a face inside an
+ * aggregate).  Device, per matrix / V-cycle: restriction by aggregate sums
+ * (agg_ptr / agg_cells: each aggregate's fine cells ascending), coarse
+ * lower/upper as sums over each coarse face's fine faces in face order
+ * (cf_ptr / cf_faces), prolongation x += e[f2c].  Bitwise the reference's. */
+int gbf_gamg_aggregate(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                       const int32_t* neighbour_h, int32_t n_coarse_target, int32_t* f2c_h,
+                       int32_t* n_coarse);
+int gbf_gamg_coarse_faces(int32_t n_faces, const int32_t* owner_h, const int32_t* neighbour_h,
+                          const int32_t* f2c_h, int32_t* coarse_owner_h,
+                          int32_t* coarse_neighbour_h, int32_t* face_to_cface_h,
+                          int32_t* n_cfaces);
+int gbf_gamg_restrict_f64(int32_t n_coarse, const int32_t* agg_ptr, const int32_t* agg_cells,
+                          const double* fine, double* coarse, void* stream);
+int gbf_gamg_coarse_coeffs_f64(int32_t n_cfaces, const int32_t* cf_ptr, const int32_t* cf_faces,
+                               const double* lower, const double* upper, double* coarse_lower,
+                               double* coarse_upper, void* stream);
+int gbf_gamg_prolong_add_f64(int32_t n_fine, const int32_t* f2c, const double* e, double* x,
+                             void* stream);
+
+/* ---- pressure-corrector steps ---------------------------------------------
+ * The steps either side of the pressure solve in SIMPLE / PISO, bitwise the
+ * reference's (one rounding per operation in its order).  owner is the
+ * int32 owner of all n_faces faces, neighbour of the n_internal internal
+ * ones; vectors are [n][3]; weights NULL means 0.5 on every face.          */
+/* rhie_chow.py:56-78 compute_HbyA: HbyA = H / max(|A_p|, 1e-30).          */
+int gbf_hbya_f64(int32_t n_cells, const double* H, const double* A_p, double* HbyA,
+                 void* stream);
+/* rhie_chow.py:81-143 compute_face_flux_HbyA (p == NULL) and :206-250
+ * compute_face_flux (p != NULL: plus the Rhie-Chow term of
+ * gbf_rhie_chow_f64).                                                      */
+int gbf_face_flux_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
+                      const int32_t* neighbour, const double* HbyA, const double* face_areas,
+                      const double* weights, const double* p, const double* A_p,
+                      const double* delta, double* phi, void* stream);
+/* rhie_chow.py:146-203 rhie_chow_correction (phi_in == NULL: out = the
+ * correction (1/A_p)_f (p_P - p_N) |S_f| delta_f, 0 on boundary faces) and
+ * pressure_equation.py:269-332 correct_face_flux (phi_in != NULL: out =
+ * phi_in + correction on internal faces, phi_in on boundary faces).       */
+int gbf_rhie_chow_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
+                      const int32_t* neighbour, const double* p, const double* A_p,
+                      const double* face_areas, const double* delta, const double* weights,
+                      const double* phi_in, double* out, void* stream);
+/* pressure_equation.py:187-266 correct_velocity: U = HbyA - alpha/|A_p|
+ * grad(p), grad(p) by Gauss with linearly interpolated face pressure
+ * (boundary faces: the owner's), |U| limited to 1e4.  bnd_ptr / bnd_face as
+ * gbf_boundary_lists; weights [n_faces].                                   */
+int gbf_correct_velocity_f64(const gbf_layout* L, const int32_t* bnd_ptr, const int32_t* bnd_face,
+                             const double* face_areas, const double* weights,
+                             const double* volumes, const double* p, const double* A_p,
+                             const double* HbyA, double alpha, double* U, void* stream);
+/* pressure_equation.py:335-377 adjust_phi: *sum (DEVICE) = the boundary
+ * flux sum phi[n_internal..n_faces) (deterministic tree order), then
+ * gbf_adjust_phi_f64 subtracts *sum / n_boundary from every boundary flux. */
+int gbf_boundary_flux_sum_f64(int32_t n_faces, int32_t n_internal, const double* phi,
+                              double* sum, void* stream);
+int gbf_adjust_phi_f64(int32_t n_faces, int32_t n_internal, const double* sum, double* phi,
+                       void* stream);
+
+/* ---- mesh geometry ----------------------------------------------------------
+ * FvMesh geometry (mesh/fv_mesh.py:75-148 on mesh/mesh_geometry.py:35-395)
+ * of a polyhedral mesh: points [n_points][3]; faces as CSR face_ptr
+ * [n_faces + 1] / face_pts (vertex indices, OpenFOAM ordering: normal by
+ * the right-hand rule points out of the owner).  Vertex indices must lie in
+ * [0, n_points): the caller validates them.                                */
+/* Face centres (vertex mean) and area vectors (1/2 sum v_j x v_{j+1}), both
+ * [n_faces][3] (mesh_geometry.py:35-108).                                  */
+int gbf_face_geometry_f64(int32_t n_faces, const int32_t* face_ptr, const int32_t* face_pts,
+                          const double* points, double* face_centres, double* face_areas,
+                          void* stream);
+/* Host: cell -> face lists in the reference's visiting order (owned faces
+ * ascending, then neighboured internal faces ascending as ~face),
+ * mesh_geometry.py:191-196.  cell_ptr_h has n_cells + 1 entries,
+ * cell_faces_h n_faces + n_internal.                                       */
+int gbf_cell_faces(int32_t n_cells, int32_t n_faces, int32_t n_internal, const int32_t* owner_h,
+                   const int32_t* neighbour_h, int32_t* cell_ptr_h, int32_t* cell_faces_h);
+/* Cell volumes [n_cells] and centres [n_cells][3] by the tet decomposition
+ * about the mean of the cell's distinct vertices (mesh_geometry.py:139-254;
+ * the mean is taken in ascending vertex order).  *status (a DEVICE int32,
+ * zeroed by the call) becomes 1 if a cell has more than 64 distinct
+ * vertices; that cell gets NaN.                                            */
+int gbf_cell_geometry_f64(int32_t n_cells, const int32_t* cell_ptr, const int32_t* cell_faces,
+                          const int32_t* face_ptr, const int32_t* face_pts, const double* points,
+                          const double* face_centres, double* volumes, double* cell_centres,
+                          int32_t* status, void* stream);
+/* Linear interpolation weights and delta coefficients [n_faces]
+ * (mesh_geometry.py:262-395): internal faces |d_N|/(|d_P|+|d_N|) and
+ * 1/|(C_N - C_P).n_hat|; boundary faces 1 and 0.  owner/neighbour int32.   */
+int gbf_face_interp_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
+                        const int32_t* neighbour, const double* cell_centres,
+                        const double* face_centres, const double* face_areas, double* weights,
+                        double* delta, void* stream);
+
 /* ---- mixed precision -------------------------------------------------------
  * No reference counterpart (the north-star's precision pattern): PCG whose
- * Krylov recurrence, Amul (coef32 = FP32 packing of the FP64 matrix) and
- * diagonal preconditioner run in FP32, with FP64 reliable updates: when the
+ * Krylov recurrence, Amul (coef32 = FP32 packing of the FP64 matrix; with
+ * coef32_sym = 1 the owner-side half of a symmetric matrix from
+ * gbf_pack_sym_f64_to_f32, which needs L->slot_mirror and a hex 3+3 layout
+ * and gives the same bits) and diagonal preconditioner run in FP32, with FP64 reliable updates: when the
  * FP32 residual has dropped by `delta` (0 < delta < 1) since the last update
  * or below max(tolerance, rel_tol*|r0|), the FP32 correction is folded into
  * the FP64 x and the residual is replaced by the true b - A64 x (bitwise
@@ -358,8 +521,8 @@ int gbf_explicit_laplacian_grad_d_f64(const gbf_layout* L, int32_t n_faces_total
  * R->iterations = inner iterations + 1, R->outer_updates = FP64 updates.  */
 size_t gbf_mixed_pcg_workspace_bytes(int32_t n_cells);
 int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double* diag64,
-                        const float* coef32, const double* precond_d, const double* b,
-                        double* x, double delta, double* history, int32_t hist_cap,
+                        const float* coef32, int32_t coef32_sym, const double* precond_d,
+                        const double* b, double* x, double delta, double* history, int32_t hist_cap,
                         const gbf_solve_params* P, gbf_solve_result* R, void* workspace,
                         size_t workspace_bytes, void* stream);
 

@@ -61,6 +61,7 @@ class Layout(ctypes.Structure):
         ("owner", _c_vp),
         ("neighbour", _c_vp),
         ("slot_dm", _c_vp),
+        ("slot_mirror", _c_vp),
     ]
 
 
@@ -116,6 +117,41 @@ EXPORTED: dict[str, tuple] = {
     "gbf_layout_fill": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp, _c_vp,
                                        _c_vp]),
     "gbf_layout_compress": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i64)]),
+    "gbf_layout_mirror": (ctypes.c_int, [_c_i32, _c_i32, _c_i32, _c_i32, _c_vp, _c_vp, _c_vp,
+                                         _c_vp, _P(_c_i32)]),
+    "gbf_pack_sym_f64_to_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_amul_sym_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_gamg_aggregate": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_vp,
+                                          _P(_c_i32)]),
+    "gbf_gamg_coarse_faces": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                             _P(_c_i32)]),
+    "gbf_gamg_restrict_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_gamg_coarse_coeffs_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                  _c_vp, _c_vp]),
+    "gbf_gamg_prolong_add_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_gs_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp,
+                                       _P(_c_i32), _P(_c_i32)]),
+    "gbf_gauss_seidel_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32,
+                                            _c_dbl, _c_i32, _c_vp, _c_vp]),
+    "gbf_residual_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_relax_f64": (ctypes.c_int, [_c_i32, _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_norm2_workspace_bytes": (_c_size, []),
+    "gbf_norm2_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_hbya_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_face_flux_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                         _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_rhie_chow_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                         _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_correct_velocity_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                _c_vp, _c_vp, _c_dbl, _c_vp, _c_vp]),
+    "gbf_boundary_flux_sum_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp]),
+    "gbf_adjust_phi_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp]),
+    "gbf_face_geometry_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_cell_faces": (ctypes.c_int, [_c_i32, _c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_cell_geometry_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                             _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_face_interp_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                           _c_vp, _c_vp, _c_vp]),
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_sweep_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
@@ -159,9 +195,9 @@ EXPORTED: dict[str, tuple] = {
     "gbf_pcg_solve_f64_noalloc": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                                  _P(SolveParams), _P(SolveResult), _c_vp]),
     "gbf_mixed_pcg_workspace_bytes": (_c_size, [_c_i32]),
-    "gbf_mixed_pcg_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl,
-                                           _c_vp, _c_i32, _P(SolveParams), _P(SolveResult),
-                                           _c_vp, _c_size, _c_vp]),
+    "gbf_mixed_pcg_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp, _c_vp,
+                                           _c_dbl, _c_vp, _c_i32, _P(SolveParams),
+                                           _P(SolveResult), _c_vp, _c_size, _c_vp]),
     "gbf_batched_mixed_pcg_workspace_bytes": (_c_size, [_c_i32, _c_i32, _c_i32]),
     "gbf_batched_mixed_pcg_solve": (ctypes.c_int, [_L, _P(Batch), _c_vp, _c_vp, _c_vp, _c_vp,
                                                    _c_vp, _c_vp, _c_dbl, _P(SolveParams), _c_i32,

@@ -30,6 +30,10 @@ SOURCES = [
     "mixed.cu",
     "assemble.cu",
     "batched.cu",
+    "geometry.cu",
+    "pressure.cu",
+    "smooth.cu",
+    "gamg.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

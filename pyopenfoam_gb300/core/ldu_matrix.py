@@ -166,6 +166,32 @@ class LduMatrix:
         self._csr_cache[key] = out
         return out
 
+    def packed_sym32(self) -> torch.Tensor | None:
+        """FP32 owner-side half of a symmetric float64 matrix (lower == upper
+        bit for bit) on a layout that supports it, else None.  The mixed
+        solver's inner Amul then streams half the coefficient bytes and gives
+        the same bits as with the full packing."""
+        if self._dtype != torch.float64 or self._n_internal_faces == 0:
+            return None
+        topo = self.topology()
+        if not topo.symmetric_storage:
+            return None
+        lo, up = self._lower, self._upper
+        key = ("packed_sym32", lo.data_ptr(), lo._version, up.data_ptr(), up._version)
+        if key in self._csr_cache:
+            return self._csr_cache[key]
+        out = torch.empty(max(topo.n_slots // 2, 1), device=self._device, dtype=torch.float32)
+        flag = torch.zeros(1, device=self._device, dtype=torch.int32)
+        _lib.check(_lib.lib().gbf_pack_sym_f64_to_f32(topo.layout_ref, lo.data_ptr(),
+                                                      up.data_ptr(), out.data_ptr(),
+                                                      flag.data_ptr(), self._stream()),
+                   "gbf_pack_sym_f64_to_f32")
+        res = None if int(flag.item()) else out
+        for k in [k for k in self._csr_cache if k[0] == "packed_sym32"]:
+            del self._csr_cache[k]
+        self._csr_cache[key] = res
+        return res
+
     def _diag_free_sources(self, transposed: bool):
         return (self._upper, self._lower) if transposed else (self._lower, self._upper)
 

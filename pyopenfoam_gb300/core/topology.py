@@ -101,12 +101,23 @@ class Topology:
         uwo = int(w[0] & 0xFFFF) if self.uniform and self.n_slices else 0
         uwn = int(w[0] >> 16) if self.uniform and self.n_slices else 0
         all_uni = int(self.compress and self.n_uniform_entries == self.n_slots // 32)
+        # mirror table: lets a symmetric matrix be stored as its owner-side half
+        self.slot_mirror = None
+        if all_uni and uwo > 0 and self.n_faces > 0:
+            mir = np.empty(nent, np.int8)
+            ok = ctypes.c_int32()
+            check(L.gbf_layout_mirror(self.n_faces, self.n_slices, uwo, uwn, face.ctypes.data,
+                                      self._own_h.ctypes.data, dm.ctypes.data, mir.ctypes.data,
+                                      ctypes.byref(ok)), "gbf_layout_mirror")
+            if ok.value:
+                self.slot_mirror = to(mir)
         self.layout = Layout(
             self.n_cells, self.n_faces, self.n_slices, self.max_width, uwo, uwn, all_uni, 0,
             self.n_slots,
             self.slice_off.data_ptr(), self.slice_w.data_ptr(), self.slot_col.data_ptr(),
             self.slot_face.data_ptr(), self.owner32.data_ptr(), self.neighbour32.data_ptr(),
             self.slot_dm.data_ptr() if self.compress else None,
+            self.slot_mirror.data_ptr() if self.slot_mirror is not None else None,
         )
         self._dic: Schedule | None = None
         self._dilu: Schedule | None = None
@@ -122,6 +133,7 @@ class Topology:
         ctypes.pointer(L)[0] = self.layout
         L.slot_dm = None
         L.all_uniform = 0
+        L.slot_mirror = None
         return L
 
     def variable_width_layout(self) -> Layout:
@@ -132,7 +144,16 @@ class Topology:
         L.uniform_wo = 0
         L.uniform_wn = 0
         L.all_uniform = 0
+        L.slot_mirror = None
         return L
+
+    @property
+    def symmetric_storage(self) -> bool:
+        """True when the hex 3+3 kernels can read a symmetric matrix from
+        its owner-side half (uniform 3+3 compressed layout with a mirror
+        table)."""
+        return (self.slot_mirror is not None and self.layout.uniform_wo == 3
+                and self.layout.uniform_wn == 3 and self.layout.all_uniform == 1)
 
     def dic_schedule(self) -> Schedule:
         if self._dic is None:

@@ -40,29 +40,67 @@ __global__ void __launch_bounds__(kBlock)
 // FP32 Amul of a hex 3+3 layout with the coefficient / x / diagonal stream
 // staged through shared memory by bulk asynchronous copies; the cells of the
 // last, partial tile are computed from global memory by one block.
-template <typename A, bool NEI_FIRST>
+// SYM: coef is the owner-side half of a symmetric matrix (pack_sym_kernel).
+template <typename A, bool NEI_FIRST, bool SYM>
 __global__ void __launch_bounds__(kTileCells, 8)
     amul_stream_kernel(gbf_layout L, const float* __restrict__ coef,
                        const float* __restrict__ diag, const float* __restrict__ x,
                        A* __restrict__ y, int n_tiles) {
-  __shared__ HexRing ring;
-  const bool ok = hex_stream_tiles<A, NEI_FIRST>(ring, n_tiles, coef, x, diag, L.slot_dm,
-                                                 [&](int c, A v, float) { y[c] = v; });
+  __shared__ HexRing<SYM> ring;
+  const bool ok = hex_stream_tiles<A, NEI_FIRST, SYM>(ring, n_tiles, coef, x, diag, L.slot_dm,
+                                                      L.slot_mirror,
+                                                      [&](int c, A v, float) { y[c] = v; });
   if (blockIdx.x == n_tiles % gridDim.x) {
     const int c = n_tiles * kTileCells + threadIdx.x;
-    if (c < L.n_cells)
-      y[c] = cell_amul_fixed<float, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, __ldg(x + c));
+    if (c < L.n_cells) {
+      if constexpr (SYM)
+        y[c] = cell_amul_sym33<A>(L, coef, diag, x, c, __ldg(x + c));
+      else
+        y[c] = cell_amul_fixed<float, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, __ldg(x + c));
+    }
   }
   if (!ok && threadIdx.x == 0) atomicExch(&g_stream_fault, 1u);
 }
 
-template <typename A, bool NEI_FIRST>
+template <typename A, bool NEI_FIRST, bool SYM = false>
 static void launch_amul_stream(const gbf_layout* L, const float* coef, const float* diag,
                                const float* x, A* y, cudaStream_t s) {
   const int n_tiles = L->n_cells / kTileCells;
-  const int grid = wave_grid(amul_stream_kernel<A, NEI_FIRST>, kTileCells,
+  const int grid = wave_grid(amul_stream_kernel<A, NEI_FIRST, SYM>, kTileCells,
                              (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells);
-  amul_stream_kernel<A, NEI_FIRST><<<grid, kTileCells, 0, s>>>(*L, coef, diag, x, y, n_tiles);
+  amul_stream_kernel<A, NEI_FIRST, SYM>
+      <<<grid, kTileCells, 0, s>>>(*L, coef, diag, x, y, n_tiles);
+}
+
+// Owner-side half of a symmetric matrix: one thread per lane of every slice;
+// lanes whose face has lower != upper (bitwise) set *differs.
+__global__ void __launch_bounds__(kBlock)
+    pack_sym_kernel(gbf_layout L, const double* __restrict__ lower,
+                    const double* __restrict__ upper, float* __restrict__ own,
+                    int32_t* __restrict__ differs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.n_slices * 32) return;
+  const CellSlots cs = cell_slots(L, c);
+  const int s = c >> 5, lane = c & 31;
+  bool diff = false;
+  for (int k = 0; k < cs.wo; ++k) {
+    const int f = L.slot_face[cs.base + 32 * k];
+    float v = 0.0f;
+    if (f >= 0) {
+      const double lo = lower[f];
+      diff |= __double_as_longlong(lo) != __double_as_longlong(upper[f]);
+      v = (float)lo;
+    }
+    own[32 * cs.wo * s + 32 * k + lane] = v;
+  }
+  if (diff) atomicOr(differs, 1);
+}
+
+__global__ void __launch_bounds__(kBlock)
+    amul_sym_kernel(gbf_layout L, const float* __restrict__ own, const float* __restrict__ diag,
+                    const float* __restrict__ x, float* __restrict__ y) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += gridDim.x * blockDim.x)
+    y[c] = cell_amul_sym33<float>(L, own, diag, x, c, __ldg(x + c));
 }
 
 template <int KIND, typename T, typename A, bool NEI_FIRST>
@@ -150,6 +188,44 @@ extern "C" int gbf_pack_f32(const gbf_layout* L, const float* own_src, const flo
 extern "C" int gbf_pack_f64_to_f32(const gbf_layout* L, const double* own_src,
                                    const double* nei_src, float* slot_coef, void* stream) {
   return gbf::pack<double, float>(L, own_src, nei_src, slot_coef, stream);
+}
+
+extern "C" int gbf_pack_sym_f64_to_f32(const gbf_layout* L, const double* lower,
+                                       const double* upper, float* coef_own, int32_t* differs,
+                                       void* stream) {
+  using namespace gbf;
+  int rc = check_layout(L);
+  if (rc) return rc;
+  GBF_REQUIRE(differs, "pack_sym: NULL differs");
+  GBF_REQUIRE(L->uniform_wo > 0 || L->n_faces == 0, "pack_sym: needs a uniform-width layout");
+  cudaStream_t s = as_stream(stream);
+  GBF_CHECK_CUDA(cudaMemsetAsync(differs, 0, sizeof(int32_t), s));
+  if (L->n_slices == 0 || L->n_faces == 0) return GBF_OK;
+  GBF_REQUIRE(coef_own && lower && upper, "pack_sym: NULL pointer");
+  const int grid = (L->n_slices * 32 + kBlock - 1) / kBlock;
+  pack_sym_kernel<<<grid, kBlock, 0, s>>>(*L, lower, upper, coef_own, differs);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_amul_sym_f32(const gbf_layout* L, const float* coef_own, const float* diag,
+                                const float* x, float* y, void* stream) {
+  using namespace gbf;
+  int rc = check_layout(L);
+  if (rc) return rc;
+  if (L->n_cells == 0) return GBF_OK;
+  GBF_REQUIRE(layout_sym_ok(*L), "amul_sym: needs a hex 3+3 layout with a mirror table");
+  GBF_REQUIRE(diag && x && y && coef_own, "amul_sym: NULL pointer");
+  cudaStream_t s = as_stream(stream);
+  if (hex_stream_aligned(coef_own, x, diag, L->slot_dm) &&
+      (reinterpret_cast<uintptr_t>(L->slot_mirror) & 15u) == 0) {
+    launch_amul_stream<float, false, true>(L, coef_own, diag, x, y, s);
+  } else {
+    const int grid = wave_grid(amul_sym_kernel, kBlock, L->n_cells);
+    amul_sym_kernel<<<grid, kBlock, 0, s>>>(*L, coef_own, diag, x, y);
+  }
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
 }
 
 extern "C" int gbf_amul_f64(const gbf_layout* L, const double* slot_coef, const double* diag,

@@ -144,8 +144,59 @@ __device__ __forceinline__ A cell_amul_fixed(const gbf_layout& L, const T* __res
   return y;
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric hex 3+3 gather: the owner-side coefficients come from the
+// owner-side half `own` (32*3 floats per slice), the neighbour-side ones from
+// the owner cells' slots, whose owner-side slot j is L.slot_mirror's entry.
+// Same products and summation order as cell_amul_fixed<float, A, false, 3, 3>
+// on the full packing of the same (symmetric) matrix.
+// ---------------------------------------------------------------------------
+template <typename A>
+__device__ __forceinline__ A cell_amul_sym33(const gbf_layout& L, const float* __restrict__ own,
+                                             const float* __restrict__ diag,
+                                             const float* __restrict__ x, int c, float xc) {
+  const int s = c >> 5, lane = c & 31;
+  const int4* __restrict__ dm4 = reinterpret_cast<const int4*>(L.slot_dm) + 3 * s;
+  int d[6];
+  unsigned m[6];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int4 v = __ldg(dm4 + q);
+    d[2 * q] = v.x;
+    m[2 * q] = (unsigned)v.y;
+    d[2 * q + 1] = v.z;
+    m[2 * q + 1] = (unsigned)v.w;
+  }
+  float a[6], xv[6];
+  bool on[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) on[k] = (m[k] >> lane) & 1u;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) a[k] = __ldg(own + 96 * s + 32 * k + lane);
+#pragma unroll
+  for (int k = 3; k < 6; ++k) {
+    const int c2 = c + d[k];
+    const int j = __ldg(L.slot_mirror + 6 * s + k);
+    a[k] = on[k] ? __ldg(own + 96 * (c2 >> 5) + 32 * j + (c2 & 31)) : 0.0f;
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) xv[k] = on[k] ? __ldg(x + c + d[k]) : 0.0f;
+  A so = (A)0, sn = (A)0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (on[k]) so = add_rn(so, (A)__fmul_rn(a[k], xv[k]));
+#pragma unroll
+  for (int k = 3; k < 6; ++k)
+    if (on[k]) sn = add_rn(sn, (A)__fmul_rn(a[k], xv[k]));
+  A y = (A)__fmul_rn(__ldg(diag + c), xc);
+  y = add_rn(y, so);
+  return add_rn(y, sn);
+}
+
 // Layout kinds with a fixed-width kernel instantiation.
-enum { kLayoutGeneric = 0, kLayoutHex33 = 33 };
+// kLayoutHex33Sym: hex 3+3 with the coefficients of a symmetric matrix
+// stored as the owner-side half (FP32 only; chosen by the caller).
+enum { kLayoutGeneric = 0, kLayoutHex33 = 33, kLayoutHex33Sym = 34 };
 
 // The fixed-width gather reads slot_dm as int4, so it needs a 16-byte
 // aligned table.
@@ -170,12 +221,24 @@ inline int layout_kind(const gbf_layout& L) {
     }                                               \
   } while (0)
 
+// True when a symmetric matrix on this layout may be stored as its
+// owner-side half (hex 3+3 kind with a mirror table).
+inline bool layout_sym_ok(const gbf_layout& L) {
+  return layout_kind(L) == kLayoutHex33 && L.slot_mirror != nullptr;
+}
+
 template <int KIND, typename T, typename A, bool NEI_FIRST>
 __device__ __forceinline__ A cell_amul_k(const gbf_layout& L, const T* __restrict__ coef,
                                          const T* __restrict__ diag, const T* __restrict__ x,
                                          int c, T xc) {
-  if (KIND == kLayoutHex33) return cell_amul_fixed<T, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, xc);
-  return cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, xc);
+  if constexpr (KIND == kLayoutHex33Sym) {
+    static_assert(!NEI_FIRST, "a symmetric matrix is its own transpose");
+    return cell_amul_sym33<A>(L, coef, diag, x, c, xc);
+  } else if constexpr (KIND == kLayoutHex33) {
+    return cell_amul_fixed<T, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, xc);
+  } else {
+    return cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, xc);
+  }
 }
 
 }  // namespace gbf

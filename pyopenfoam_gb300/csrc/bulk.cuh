@@ -14,6 +14,14 @@
 // The HBM stream therefore stays in flight independently of the registers
 // the gather needs.
 //
+// For a symmetric matrix stored as its owner-side half (SYM), a tile streams
+// 8*3*32 owner-side coefficients (3072 B) and the slices' 48 mirror entries
+// (48 B) instead of the 6144 B of both sides; a neighbour-side coefficient
+// is the owner-side one of the owner cell, read from the stage when that cell
+// lies in the tile and from global memory (an L2 hit: its tile streamed
+// recently) otherwise.  Neighbour x values of cells inside the tile are read
+// from the stage as well.
+//
 // Every wait is bounded: after kWaitPolls unsuccessful polls the block
 // records a fault, drains (again bounded) the copies it has in flight and
 // stops streaming; the host turns the fault into GBF_DEVICE_TIMEOUT.
@@ -39,8 +47,30 @@ constexpr unsigned kStageBytes = sizeof(float) * (kTileSlices * kHexW * 32 + 2 *
                                  sizeof(int2) * kTileSlices * kHexW;
 static_assert(kStageBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
 
+struct __align__(128) HexStageSym {
+  float coef[kTileSlices * 3 * 32];
+  float x[kTileCells];
+  float d[kTileCells];
+  int2 dm[kTileSlices * kHexW];
+  int8_t mir[kTileSlices * kHexW];
+};
+constexpr unsigned kStageBytesSym = sizeof(float) * (kTileSlices * 3 * 32 + 2 * kTileCells) +
+                                    sizeof(int2) * kTileSlices * kHexW +
+                                    sizeof(int8_t) * kTileSlices * kHexW;
+static_assert(kStageBytesSym % 16 == 0, "bulk copies move multiples of 16 bytes");
+
+template <bool SYM>
+struct HexStageOf {
+  using type = HexStage;
+};
+template <>
+struct HexStageOf<true> {
+  using type = HexStageSym;
+};
+
+template <bool SYM>
 struct HexRing {
-  HexStage stage[kStages];
+  typename HexStageOf<SYM>::type stage[kStages];
   unsigned long long bar[kStages];
 };
 
@@ -92,15 +122,28 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
-// Issues the four copies of tile t into stage s (one thread).
-__device__ __forceinline__ void hex_issue(HexRing& R, int s, int t, const float* coef,
-                                          const float* x, const float* d, const int* slot_dm) {
+// Issues the copies of tile t into stage s (one thread).
+__device__ __forceinline__ void hex_issue(HexRing<false>& R, int s, int t, const float* coef,
+                                          const float* x, const float* d, const int* slot_dm,
+                                          const int8_t*) {
   HexStage& S = R.stage[s];
   mbar_arrive_expect_tx(&R.bar[s], kStageBytes);
   bulk_g2s(S.coef, coef + (size_t)t * (kTileSlices * kHexW * 32), sizeof(S.coef), &R.bar[s]);
   bulk_g2s(S.x, x + (size_t)t * kTileCells, sizeof(S.x), &R.bar[s]);
   bulk_g2s(S.d, d + (size_t)t * kTileCells, sizeof(S.d), &R.bar[s]);
   bulk_g2s(S.dm, slot_dm + (size_t)t * (2 * kTileSlices * kHexW), sizeof(S.dm), &R.bar[s]);
+}
+
+__device__ __forceinline__ void hex_issue(HexRing<true>& R, int s, int t, const float* own,
+                                          const float* x, const float* d, const int* slot_dm,
+                                          const int8_t* slot_mirror) {
+  HexStageSym& S = R.stage[s];
+  mbar_arrive_expect_tx(&R.bar[s], kStageBytesSym);
+  bulk_g2s(S.coef, own + (size_t)t * (kTileSlices * 3 * 32), sizeof(S.coef), &R.bar[s]);
+  bulk_g2s(S.x, x + (size_t)t * kTileCells, sizeof(S.x), &R.bar[s]);
+  bulk_g2s(S.d, d + (size_t)t * kTileCells, sizeof(S.d), &R.bar[s]);
+  bulk_g2s(S.dm, slot_dm + (size_t)t * (2 * kTileSlices * kHexW), sizeof(S.dm), &R.bar[s]);
+  bulk_g2s(S.mir, slot_mirror + (size_t)t * (kTileSlices * kHexW), sizeof(S.mir), &R.bar[s]);
 }
 
 // (A x)[c] of thread `tid` of the tile in stage S: the products and the
@@ -135,6 +178,57 @@ __device__ __forceinline__ A hex_cell_from_stage(const HexStage& S, int tid,
   return add_rn(y, sn);
 }
 
+// The symmetric form: (A x)[c] from the owner-side half.  Same products and
+// summation order as hex_cell_from_stage<A, false> on the full packing.
+template <typename A>
+__device__ __forceinline__ A hex_cell_from_stage_sym(const HexStageSym& S, int tid,
+                                                     const float* __restrict__ own,
+                                                     const float* __restrict__ x, int c) {
+  const int sl = tid >> 5, lane = tid & 31;
+  const int c0 = c - tid;  // first cell of the tile
+  float a[kHexW], xv[kHexW];
+  bool on[kHexW];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) a[k] = S.coef[(sl * 3 + k) * 32 + lane];
+#pragma unroll
+  for (int k = 0; k < kHexW; ++k) {
+    const int2 e = S.dm[sl * kHexW + k];
+    on[k] = ((unsigned)e.y >> lane) & 1u;
+    const int cn = c + e.x;
+    const unsigned in_tile = (unsigned)(cn - c0);
+    xv[k] = !on[k] ? 0.0f : (in_tile < (unsigned)kTileCells ? S.x[in_tile] : __ldg(x + cn));
+    if (k >= 3) {
+      const int j = S.mir[sl * kHexW + k];
+      const int i_own = 96 * (cn >> 5) + 32 * j + (cn & 31);
+      a[k] = !on[k] ? 0.0f
+                    : (in_tile < (unsigned)kTileCells ? S.coef[i_own - 3 * c0] : __ldg(own + i_own));
+    }
+  }
+  A so = (A)0, sn = (A)0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (on[k]) so = add_rn(so, (A)__fmul_rn(a[k], xv[k]));
+#pragma unroll
+  for (int k = 3; k < kHexW; ++k)
+    if (on[k]) sn = add_rn(sn, (A)__fmul_rn(a[k], xv[k]));
+  A y = (A)__fmul_rn(S.d[tid], S.x[tid]);
+  y = add_rn(y, so);
+  return add_rn(y, sn);
+}
+
+template <typename A, bool NEI_FIRST>
+__device__ __forceinline__ A hex_cell(const HexStage& S, int tid, const float*,
+                                      const float* __restrict__ x, int c) {
+  return hex_cell_from_stage<A, NEI_FIRST>(S, tid, x, c);
+}
+template <typename A, bool NEI_FIRST>
+__device__ __forceinline__ A hex_cell(const HexStageSym& S, int tid,
+                                      const float* __restrict__ own,
+                                      const float* __restrict__ x, int c) {
+  static_assert(!NEI_FIRST, "a symmetric matrix is its own transpose");
+  return hex_cell_from_stage_sym<A>(S, tid, own, x, c);
+}
+
 // True when the pointers the staged path streams from are 16-byte aligned.
 inline bool hex_stream_aligned(const void* coef, const void* x, const void* d,
                                const void* slot_dm) {
@@ -146,10 +240,11 @@ inline bool hex_stream_aligned(const void* coef, const void* x, const void* d,
 // Runs f(c, y, xc) for every cell of the full tiles assigned to this block
 // (tiles blockIdx.x, blockIdx.x + gridDim.x, ...).  Returns false if a wait
 // ran out (the block then stops streaming after draining its copies).
-template <typename A, bool NEI_FIRST, typename F>
-__device__ __forceinline__ bool hex_stream_tiles(HexRing& R, int n_tiles, const float* coef,
+template <typename A, bool NEI_FIRST, bool SYM, typename F>
+__device__ __forceinline__ bool hex_stream_tiles(HexRing<SYM>& R, int n_tiles, const float* coef,
                                                  const float* x, const float* d,
-                                                 const int* slot_dm, F&& f) {
+                                                 const int* slot_dm, const int8_t* slot_mirror,
+                                                 F&& f) {
   const int tid = threadIdx.x;
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) mbar_init(&R.bar[s], 1);
@@ -161,7 +256,7 @@ __device__ __forceinline__ bool hex_stream_tiles(HexRing& R, int n_tiles, const 
     for (int s = 0; s < kStages; ++s) {
       const int t = blockIdx.x + s * gridDim.x;
       if (t >= n_tiles) break;
-      hex_issue(R, s, t, coef, x, d, slot_dm);
+      hex_issue(R, s, t, coef, x, d, slot_dm, slot_mirror);
       ++issued;
     }
   }
@@ -176,12 +271,12 @@ __device__ __forceinline__ bool hex_stream_tiles(HexRing& R, int n_tiles, const 
       break;
     }
     const int c = t * kTileCells + tid;
-    f(c, hex_cell_from_stage<A, NEI_FIRST>(R.stage[s], tid, x, c), R.stage[s].x[tid]);
+    f(c, hex_cell<A, NEI_FIRST>(R.stage[s], tid, coef, x, c), R.stage[s].x[tid]);
     __syncthreads();  // every thread is done with stage s
     if (tid == 0) {
       const int tn = t + kStages * gridDim.x;
       if (tn < n_tiles) {
-        hex_issue(R, s, tn, coef, x, d, slot_dm);
+        hex_issue(R, s, tn, coef, x, d, slot_dm, slot_mirror);
         ++issued;
       }
     }

@@ -159,16 +159,18 @@ __global__ void __launch_bounds__(kBlock)
 // (bulk.cuh); the cells of the last, partial tile come from global memory.
 // A wait that runs out records st->fault, which the last block turns into
 // GBF_DEVICE_TIMEOUT once every block has arrived.
+template <bool SYM>
 __global__ void __launch_bounds__(kTileCells, 8)
     mp_ap_stream_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v,
                         int n_tiles) {
   if (v.st->status != GBF_RUNNING) return;
-  __shared__ HexRing ring;
+  __shared__ HexRing<SYM> ring;
   __shared__ double sh[kTileCells / 32];
   const int G = gridDim.x;
   DFAcc a;
-  const bool ok = hex_stream_tiles<float, false>(ring, n_tiles, coef32, v.p, v.d32, L.slot_dm,
-                                                 [&](int c, float y, float pc) {
+  const bool ok = hex_stream_tiles<float, false, SYM>(ring, n_tiles, coef32, v.p, v.d32,
+                                                      L.slot_dm, L.slot_mirror,
+                                                      [&](int c, float y, float pc) {
                                                    v.Ap[c] = y;
                                                    a.add_prod(pc, y);
                                                  });
@@ -176,7 +178,9 @@ __global__ void __launch_bounds__(kTileCells, 8)
     const int c = n_tiles * kTileCells + threadIdx.x;
     if (c < L.n_cells) {
       const float pc = __ldg(v.p + c);
-      const float y = cell_amul_fixed<float, float, false, 3, 3>(L, coef32, v.d32, v.p, c, pc);
+      const float y = SYM ? cell_amul_sym33<float>(L, coef32, v.d32, v.p, c, pc)
+                          : cell_amul_fixed<float, float, false, 3, 3>(L, coef32, v.d32, v.p,
+                                                                       c, pc);
       v.Ap[c] = y;
       a.add_prod(pc, y);
     }
@@ -392,7 +396,7 @@ extern "C" size_t gbf_mixed_pcg_workspace_bytes(int32_t n) {
 
 extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
                                    const double* diag64, const float* coef32,
-                                   const double* pd, const double* b, double* x, double delta,
+                                   int32_t coef32_sym, const double* pd, const double* b, double* x, double delta,
                                    double* hist, int32_t hist_cap, const gbf_solve_params* P,
                                    gbf_solve_result* R, void* ws, size_t ws_bytes,
                                    void* stream) {
@@ -413,6 +417,9 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
                   (L->n_faces == 0 || (coef64 && coef32)),
               "mixed_pcg: NULL pointer");
   GBF_REQUIRE(ws_bytes >= gbf_mixed_pcg_workspace_bytes(n), "mixed_pcg: workspace too small");
+  const bool sym = coef32_sym != 0 && L->n_faces > 0;
+  GBF_REQUIRE(!sym || layout_sym_ok(*L),
+              "mixed_pcg: coef32_sym needs a hex 3+3 layout with a mirror table");
   cudaStream_t s = as_stream(stream);
   char* w = static_cast<char*>(ws);
   const size_t vb = a256(sizeof(float) * (size_t)n);
@@ -427,10 +434,13 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   const bool hex = layout_kind(*L) == kLayoutHex33;
   // staged K_ap: hex layout, 16-byte aligned coefficient / vector streams
   // (the workspace vectors are 256-byte aligned)
-  const bool staged = hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
+  const bool staged = hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm) &&
+                      (!sym || (reinterpret_cast<uintptr_t>(L->slot_mirror) & 15u) == 0);
   const int n_tiles = n / kTileCells;
-  const int Ga = staged ? wave_grid(mp_ap_stream_kernel, kTileCells,
-                                    (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells)
+  const long long tile_work = (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells;
+  const int Ga = staged ? (sym ? wave_grid(mp_ap_stream_kernel<true>, kTileCells, tile_work)
+                               : wave_grid(mp_ap_stream_kernel<false>, kTileCells, tile_work))
+                 : sym  ? wave_grid(mp_ap_kernel<kLayoutHex33Sym>, kBlock, n)
                  : hex  ? wave_grid(mp_ap_kernel<kLayoutHex33>, kBlock, n)
                         : wave_grid(mp_ap_kernel<kLayoutGeneric>, kBlock, n);
   const int Ba = staged ? kTileCells : kBlock;
@@ -452,8 +462,12 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   while (hs.status == GBF_RUNNING && launched < limit) {
     for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
       const bool tb = timing_begin(kProbeMixedAp, s);
-      if (staged)
-        mp_ap_stream_kernel<<<Ga, Ba, 0, s>>>(*L, coef32, v, n_tiles);
+      if (staged && sym)
+        mp_ap_stream_kernel<true><<<Ga, Ba, 0, s>>>(*L, coef32, v, n_tiles);
+      else if (staged)
+        mp_ap_stream_kernel<false><<<Ga, Ba, 0, s>>>(*L, coef32, v, n_tiles);
+      else if (sym)
+        mp_ap_kernel<kLayoutHex33Sym><<<Ga, Ba, 0, s>>>(*L, coef32, v);
       else if (hex)
         mp_ap_kernel<kLayoutHex33><<<Ga, Ba, 0, s>>>(*L, coef32, v);
       else

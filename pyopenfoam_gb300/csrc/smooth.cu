@@ -1,0 +1,188 @@
+// Smoothers and the kernels of the host-driven smoothing solvers:
+//   Gauss-Seidel sweeps       solvers/smooth_solver.py:134-187 (SmoothSolver,
+//                             smoother "GaussSeidel"), solvers/smoothers.py:
+//                             63-149 (GaussSeidelSmoother, forward+backward,
+//                             relaxed)
+//   residual r = b - A x      every smoother's and solver's residual
+//   relaxation x += w s z     JacobiSmoother (smoothers.py:152-200), the
+//                             DIC/DILU Richardson smoothers
+//                             (smooth_solver.py:189-232, smoothers.py:203-260)
+//   |r|_2                     the residual norm of the convergence checks
+//
+// Gauss-Seidel runs as a level-scheduled wavefront (one launch per level,
+// gbf_gs_schedule): a cell's update reads the already-updated values of its
+// lower-numbered neighbours (forward) and the old values of the others, as
+// the reference's sequential cell loop does; no two neighbours share a level.
+// Each row sum follows the reference's loop over faces in ascending face
+// order (owner-side and neighbour-side slots merged by face index), one
+// rounding per operation, so the sweep is bitwise the reference's.
+#include <limits.h>
+#include <math.h>
+
+#include "amul.cuh"
+
+namespace gbf {
+
+template <bool RELAX>
+__global__ void __launch_bounds__(kBlock)
+    gs_level_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
+                    const double* __restrict__ b, const int32_t* __restrict__ level_ptr,
+                    const int32_t* __restrict__ level_cells, int level, double omega,
+                    double* x) {
+  const int start = __ldg(level_ptr + level);
+  const int count = __ldg(level_ptr + level + 1) - start;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int c = __ldg(level_cells + start + t);
+  const double dc = __ldg(diag + c);
+  const double xc = __ldcg(x + c);
+  double row = __dmul_rn(dc, xc);
+  if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    int i = 0, j = 0;
+    while (true) {
+      int fi = INT_MAX, fj = INT_MAX;
+      while (i < cs.wo && (fi = __ldg(L.slot_face + cs.base + 32 * i)) < 0) ++i;
+      if (i >= cs.wo) fi = INT_MAX;
+      while (j < cs.wn && (fj = __ldg(L.slot_face + cs.base + 32 * (cs.wo + j))) < 0) ++j;
+      if (j >= cs.wn) fj = INT_MAX;
+      if (fi == INT_MAX && fj == INT_MAX) break;
+      const int k = fi < fj ? i : cs.wo + j;
+      const int slot = cs.base + 32 * k;
+      const int col = slot_column(L, cs.e0 + k, slot, c);
+      row = __dadd_rn(row, __dmul_rn(__ldg(coef + slot), __ldcg(x + col)));
+      if (fi < fj)
+        ++i;
+      else
+        ++j;
+    }
+  }
+  const double off = __dsub_rn(row, __dmul_rn(dc, xc));
+  if (fabs(dc) > 1e-30) {
+    const double nv = __ddiv_rn(__dsub_rn(__ldg(b + c), off), dc);
+    x[c] = RELAX ? __dadd_rn(xc, __dmul_rn(omega, __dsub_rn(nv, xc))) : nv;
+  }
+}
+
+// r = b - A x with A x in the reference's order (cell_amul).
+template <int KIND>
+__global__ void __launch_bounds__(kBlock)
+    residual_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
+                    const double* __restrict__ b, const double* __restrict__ x,
+                    double* __restrict__ r) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += gridDim.x * blockDim.x)
+    r[c] = __dsub_rn(__ldg(b + c),
+                     cell_amul_k<KIND, double, double, false>(L, coef, diag, x, c, __ldg(x + c)));
+}
+
+// x += (omega * s_c) * z with s_c = 1 / max(|diag_c|, 1e-30), or
+// x += omega * z without a diagonal.
+__global__ void __launch_bounds__(kBlock)
+    relax_kernel(int n, double omega, const double* __restrict__ diag,
+                 const double* __restrict__ z, double* __restrict__ x) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double s = omega;
+  if (diag) {
+    const double a = fabs(__ldg(diag + c));
+    s = __dmul_rn(omega, __ddiv_rn(1.0, a > 1e-30 ? a : 1e-30));
+  }
+  x[c] = __dadd_rn(x[c], __dmul_rn(s, __ldg(z + c)));
+}
+
+constexpr int kNormBlocks = 1024;
+
+__global__ void __launch_bounds__(kBlock)
+    sumsq_partials_kernel(int n, const double* __restrict__ r, double* __restrict__ partials) {
+  __shared__ double sh[kBlock / 32];
+  double s = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const double v = __ldg(r + c);
+    s = __fma_rn(v, v, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kBlock)
+    sqrt_sum_kernel(int g, const double* __restrict__ partials, double* __restrict__ out) {
+  __shared__ double sh[kBlock / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < g; i += blockDim.x) s = __dadd_rn(s, partials[i]);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = sqrt(s);
+}
+
+}  // namespace gbf
+
+using namespace gbf;
+
+extern "C" int gbf_gauss_seidel_f64(const gbf_layout* L, const double* coef, const double* diag,
+                                    const double* b, const int32_t* level_ptr,
+                                    const int32_t* level_cells, const int32_t* level_ptr_h,
+                                    int32_t n_levels, double omega, int32_t relax, double* x,
+                                    void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  if (L->n_cells == 0) return GBF_OK;
+  GBF_REQUIRE(diag && b && x && level_ptr && level_cells && level_ptr_h && n_levels >= 0 &&
+                  (L->n_faces == 0 || coef),
+              "gauss_seidel: NULL pointer or bad level count");
+  cudaStream_t s = as_stream(stream);
+  for (int l = 0; l < n_levels; ++l) {
+    const int cnt = level_ptr_h[l + 1] - level_ptr_h[l];
+    if (cnt <= 0) continue;
+    const int grid = (cnt + kBlock - 1) / kBlock;
+    if (relax)
+      gs_level_kernel<true><<<grid, kBlock, 0, s>>>(*L, coef, diag, b, level_ptr, level_cells, l,
+                                                    omega, x);
+    else
+      gs_level_kernel<false><<<grid, kBlock, 0, s>>>(*L, coef, diag, b, level_ptr, level_cells,
+                                                     l, omega, x);
+  }
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_residual_f64(const gbf_layout* L, const double* coef, const double* diag,
+                                const double* b, const double* x, double* r, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  if (L->n_cells == 0) return GBF_OK;
+  GBF_REQUIRE(diag && b && x && r && (L->n_faces == 0 || coef), "residual: NULL pointer");
+  cudaStream_t s = as_stream(stream);
+  if (layout_kind(*L) == kLayoutHex33) {
+    const int grid = wave_grid(residual_kernel<kLayoutHex33>, kBlock, L->n_cells);
+    residual_kernel<kLayoutHex33><<<grid, kBlock, 0, s>>>(*L, coef, diag, b, x, r);
+  } else {
+    const int grid = wave_grid(residual_kernel<kLayoutGeneric>, kBlock, L->n_cells);
+    residual_kernel<kLayoutGeneric><<<grid, kBlock, 0, s>>>(*L, coef, diag, b, x, r);
+  }
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_relax_f64(int32_t n, double omega, const double* diag, const double* z,
+                             double* x, void* stream) {
+  GBF_REQUIRE(n >= 0, "relax: negative n");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(z && x, "relax: NULL pointer");
+  relax_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(n, omega, diag, z, x);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" size_t gbf_norm2_workspace_bytes(void) { return sizeof(double) * kNormBlocks; }
+
+extern "C" int gbf_norm2_f64(int32_t n, const double* r, double* out, void* workspace,
+                             void* stream) {
+  GBF_REQUIRE(n >= 0 && out && workspace && (n == 0 || r), "norm2: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  int g = (n + kBlock - 1) / kBlock;
+  g = g < 1 ? 1 : (g > kNormBlocks ? kNormBlocks : g);
+  double* partials = static_cast<double*>(workspace);
+  sumsq_partials_kernel<<<g, kBlock, 0, s>>>(n, r, partials);
+  sqrt_sum_kernel<<<1, kBlock, 0, s>>>(g, partials, out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}

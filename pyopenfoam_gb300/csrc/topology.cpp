@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <unordered_map>
 #include <vector>
 
 #include "gbfoam.h"
@@ -427,5 +428,215 @@ extern "C" int gbf_layout_compress(int32_t n_slices, const int32_t* slice_off,
     }
   }
   if (n_uniform) *n_uniform = uni;
+  return GBF_OK;
+}
+
+// Mirror table for symmetric matrices: each neighbour-side entry (s, k) of a
+// uniform-width compressed layout gets the owner-side slot j holding the
+// same face in its owner's slice, provided j is the same for every lane of
+// the entry and the entry is offset-compressed.
+extern "C" int gbf_layout_mirror(int32_t n_faces, int32_t n_slices, int32_t wo, int32_t wn,
+                                 const int32_t* slot_face, const int32_t* owner,
+                                 const int32_t* slot_dm, int8_t* slot_mirror, int32_t* ok) {
+  if (n_faces < 0 || n_slices < 0 || wo < 0 || wn < 0 || !ok ||
+      (n_slices > 0 && (!slot_face || !slot_dm || !slot_mirror)) || (n_faces > 0 && !owner)) {
+    gbf::set_error("layout_mirror: bad arguments");
+    return GBF_ERR_ARG;
+  }
+  *ok = (wo > 0 && wo <= 127 && n_faces > 0) ? 1 : 0;
+  const int64_t W = (int64_t)wo + wn;
+  std::vector<int8_t> own_j((size_t)n_faces, -1);
+  for (int64_t s = 0; s < n_slices; ++s)
+    for (int32_t j = 0; j < wo; ++j) {
+      slot_mirror[s * W + j] = -1;
+      for (int32_t l = 0; l < 32; ++l) {
+        const int32_t f = slot_face[32 * (s * W + j) + l];
+        if (f < 0) continue;
+        if (f >= n_faces || j > 127 || owner[f] != (int32_t)(32 * s + l)) {
+          *ok = 0;
+          continue;
+        }
+        own_j[(size_t)f] = (int8_t)j;
+      }
+    }
+  for (int64_t s = 0; s < n_slices; ++s)
+    for (int32_t k = wo; k < W; ++k) {
+      const int64_t e = s * W + k;
+      int32_t jj = -1;
+      for (int32_t l = 0; l < 32; ++l) {
+        const int32_t f = slot_face[32 * e + l];
+        if (f < 0) continue;
+        const int32_t j = (f < n_faces) ? own_j[(size_t)f] : -1;
+        if (j < 0 || (jj >= 0 && j != jj) || slot_dm[2 * e] == INT32_MIN ||
+            (int64_t)owner[f] != 32 * s + l + (int64_t)slot_dm[2 * e])
+          *ok = 0;
+        if (jj < 0) jj = j;
+      }
+      slot_mirror[e] = (int8_t)jj;
+    }
+  return GBF_OK;
+}
+
+// Cell -> face lists in the order the reference's cell-geometry loop visits
+// them (mesh/mesh_geometry.py:191-196): every face the cell owns, ascending
+// (boundary faces included), then every internal face it neighbours,
+// ascending, the latter stored as ~face.
+extern "C" int gbf_cell_faces(int32_t n_cells, int32_t n_faces, int32_t n_internal,
+                              const int32_t* owner, const int32_t* neighbour, int32_t* cell_ptr,
+                              int32_t* cell_faces) {
+  if (n_cells < 0 || n_faces < 0 || n_internal < 0 || n_internal > n_faces || !cell_ptr ||
+      (n_faces > 0 && (!owner || !cell_faces)) || (n_internal > 0 && !neighbour)) {
+    gbf::set_error("cell_faces: bad arguments");
+    return GBF_ERR_ARG;
+  }
+  for (int32_t f = 0; f < n_faces; ++f)
+    if (owner[f] < 0 || owner[f] >= n_cells || (f < n_internal &&
+                                                 (neighbour[f] < 0 || neighbour[f] >= n_cells))) {
+      gbf::set_error("cell_faces: face %d has a cell index outside [0, %d)", f, n_cells);
+      return GBF_ERR_RANGE;
+    }
+  std::vector<int64_t> cnt((size_t)n_cells + 1, 0);
+  for (int32_t f = 0; f < n_faces; ++f) cnt[(size_t)owner[f] + 1]++;
+  for (int32_t f = 0; f < n_internal; ++f) cnt[(size_t)neighbour[f] + 1]++;
+  for (int32_t c = 0; c < n_cells; ++c) cnt[c + 1] += cnt[c];
+  if (cnt[n_cells] > INT32_MAX) {
+    gbf::set_error("cell_faces: too many cell-face entries");
+    return GBF_ERR_ARG;
+  }
+  std::vector<int64_t> cur(cnt.begin(), cnt.end() - 1);
+  for (int32_t f = 0; f < n_faces; ++f) cell_faces[cur[owner[f]]++] = f;
+  for (int32_t f = 0; f < n_internal; ++f) cell_faces[cur[neighbour[f]]++] = ~f;
+  for (int32_t c = 0; c <= n_cells; ++c) cell_ptr[c] = (int32_t)cnt[c];
+  return GBF_OK;
+}
+
+// Gauss-Seidel wavefront: forward (reverse = 0) level(c) = 1 + max level of
+// the neighbours j < c (cells ascending); backward (reverse = 1) the same
+// over the neighbours j > c (cells descending).  Neighbours never share a
+// level, and every cell runs after the neighbours the sequential sweep has
+// already updated when it reaches the cell.
+extern "C" int gbf_gs_schedule(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                               int32_t reverse, int32_t* level_ptr, int32_t* level_cells,
+                               int32_t* n_levels, int32_t* max_level_size) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  std::vector<int64_t> ptr((size_t)n + 1, 0);
+  for (int32_t f = 0; f < nf; ++f) {
+    ptr[(size_t)own[f] + 1]++;
+    ptr[(size_t)nei[f] + 1]++;
+  }
+  for (int32_t c = 0; c < n; ++c) ptr[c + 1] += ptr[c];
+  std::vector<int32_t> adj((size_t)ptr[n]);
+  std::vector<int64_t> cur(ptr.begin(), ptr.end() - 1);
+  for (int32_t f = 0; f < nf; ++f) {
+    adj[cur[own[f]]++] = nei[f];
+    adj[cur[nei[f]]++] = own[f];
+  }
+  std::vector<int32_t> level((size_t)n, 0);
+  int32_t nl = (n > 0) ? 1 : 0;
+  for (int32_t q = 0; q < n; ++q) {
+    const int32_t c = reverse ? n - 1 - q : q;
+    int32_t l = 0;
+    for (int64_t k = ptr[c]; k < ptr[c + 1]; ++k) {
+      const int32_t j = adj[k];
+      if (reverse ? j > c : j < c) l = std::max(l, level[j] + 1);
+    }
+    level[c] = l;
+    nl = std::max(nl, l + 1);
+  }
+  bucket_by_level(n, level, nl, level_ptr, level_cells, max_level_size);
+  *n_levels = nl;
+  return GBF_OK;
+}
+
+// GAMG coarsening (solvers/gamg.py:183-245): greedy aggregation in cell
+// order.  Each unaggregated cell seeds an aggregate and takes its
+// unaggregated neighbours (adjacency in face order, owner side and
+// neighbour side as the faces list them); once the target count is reached
+// every remaining cell joins the aggregate of its first aggregated
+// neighbour (cell 0's aggregate if none), in cell order.
+extern "C" int gbf_gamg_aggregate(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                                  int32_t n_coarse_target, int32_t* f2c, int32_t* n_coarse) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  if (!n_coarse || (n > 0 && !f2c)) {
+    gbf::set_error("gamg_aggregate: NULL pointer");
+    return GBF_ERR_ARG;
+  }
+  std::vector<int64_t> ptr((size_t)n + 1, 0);
+  for (int32_t f = 0; f < nf; ++f) {
+    ptr[(size_t)own[f] + 1]++;
+    ptr[(size_t)nei[f] + 1]++;
+  }
+  for (int32_t c = 0; c < n; ++c) ptr[c + 1] += ptr[c];
+  std::vector<int32_t> adj((size_t)ptr[n]);
+  std::vector<int64_t> cur(ptr.begin(), ptr.end() - 1);
+  for (int32_t f = 0; f < nf; ++f) {
+    adj[cur[own[f]]++] = nei[f];
+    adj[cur[nei[f]]++] = own[f];
+  }
+  for (int32_t c = 0; c < n; ++c) f2c[c] = -1;
+  int32_t nag = 0;
+  for (int32_t cell = 0; cell < n; ++cell) {
+    if (f2c[cell] >= 0) continue;
+    const int32_t id = nag++;
+    f2c[cell] = id;
+    for (int64_t k = ptr[cell]; k < ptr[cell + 1]; ++k)
+      if (f2c[adj[k]] < 0) f2c[adj[k]] = id;
+    if (nag >= n_coarse_target) {
+      for (int32_t r = 0; r < n; ++r) {
+        if (f2c[r] >= 0) continue;
+        bool assigned = false;
+        for (int64_t k = ptr[r]; k < ptr[r + 1]; ++k)
+          if (f2c[adj[k]] >= 0) {
+            f2c[r] = f2c[adj[k]];
+            assigned = true;
+            break;
+          }
+        if (!assigned) f2c[r] = 0;
+      }
+      break;
+    }
+  }
+  for (int32_t c = 0; c < n; ++c)
+    if (f2c[c] < 0) f2c[c] = 0;
+  *n_coarse = nag;
+  return GBF_OK;
+}
+
+// GAMG coarse faces (solvers/gamg.py:249-331): fine faces whose two cells
+// fall in different aggregates, merged per unordered aggregate pair in order
+// of first appearance; the coarse face keeps the (owner, neighbour)
+// aggregates of its first fine face.  face_to_cface[f] = coarse face of
+// fine face f, -1 inside an aggregate.  Output arrays hold n_faces entries.
+extern "C" int gbf_gamg_coarse_faces(int32_t nf, const int32_t* own, const int32_t* nei,
+                                     const int32_t* f2c, int32_t* coarse_own, int32_t* coarse_nei,
+                                     int32_t* face_to_cface, int32_t* n_cfaces) {
+  if (nf < 0 || !n_cfaces ||
+      (nf > 0 && (!own || !nei || !f2c || !coarse_own || !coarse_nei || !face_to_cface))) {
+    gbf::set_error("gamg_coarse_faces: bad arguments");
+    return GBF_ERR_ARG;
+  }
+  std::unordered_map<uint64_t, int32_t> seen;
+  seen.reserve((size_t)nf);
+  int32_t nc = 0;
+  for (int32_t f = 0; f < nf; ++f) {
+    const int32_t cp = f2c[own[f]], cn = f2c[nei[f]];
+    if (cp == cn) {
+      face_to_cface[f] = -1;
+      continue;
+    }
+    const uint64_t key = ((uint64_t)(uint32_t)std::min(cp, cn) << 32) | (uint32_t)std::max(cp, cn);
+    auto it = seen.find(key);
+    if (it != seen.end()) {
+      face_to_cface[f] = it->second;
+    } else {
+      seen.emplace(key, nc);
+      coarse_own[nc] = cp;
+      coarse_nei[nc] = cn;
+      face_to_cface[f] = nc++;
+    }
+  }
+  *n_cfaces = nc;
   return GBF_OK;
 }

@@ -91,7 +91,7 @@ class UnrolledImplicitDiffusion:
 
     def _solve_normalised(self, A: LduMatrix, b: torch.Tensor, x0: torch.Tensor):
         """Solve A x = b with b and x0 scaled by the power of two that brings
-        max|b| into [0.5, 1), and the solution scaled back.  Power-of-two
+        max|b| into [2^29, 2^30), and the solution scaled back.  Power-of-two
         scaling is exact, so the iterates are those of the unscaled solve
         multiplied by 2^k -- except that the solver's absolute thresholds
         (the 1e-30 breakdown test on p.Ap) no longer stop a solve whose
@@ -100,7 +100,7 @@ class UnrolledImplicitDiffusion:
         m = float(b.abs().max()) if b.numel() else 0.0
         if m == 0.0 or not math.isfinite(m):
             return self.solver(A, b, x0)
-        k = -math.frexp(m)[1]
+        k = 30 - math.frexp(m)[1]
         s, inv = math.ldexp(1.0, k), math.ldexp(1.0, -k)
         x, it, res = self.solver(A, b * s, x0 * s)
         return x * inv, it, res * inv
@@ -186,25 +186,43 @@ class UnrolledImplicitDiffusion:
     def central_difference(self, gamma: torch.Tensor, x0: torch.Tensor, target: torch.Tensor,
                            face: int, h: float = 1e-6) -> float:
         """(L(gamma + h e_f) - L(gamma - h e_f)) / (2h), evaluated without
-        cancellation.  The difference d_t = x+_t - x-_t of the two perturbed
-        trajectories obeys exactly
-            A+ d_{t+1} = d_t / dt - (A+ - A-) x-_{t+1},   d_0 = 0,
-        and A+ - A- is exact in floating point (the perturbed coefficients
-        differ by a factor << 2, so their differences are exact by
-        Sterbenz's lemma).  Solving for d instead of subtracting x+ from x-
-        keeps the quotient accurate to the solver tolerance relative to |d|
-        rather than |x|; L+ - L- = sum d (x+ + x- - 2 target).  The
-        difference systems are solved with power-of-two normalisation
-        (``_solve_normalised``): |d| is ~2h |dx/dgamma|, small enough that
-        the solver's absolute breakdown threshold would otherwise end the
-        solves early."""
-        gp, gm = gamma.clone(), gamma.clone()
-        gp[face] += h
-        gm[face] -= h
-        Ap, Am = self.system(gp), self.system(gm)
-        dA = LduMatrix(Ap.n_cells, Ap.owner, Ap.neighbour, device=Ap.device)
-        dA._topology = Ap.topology()
-        dA.diag, dA.lower, dA.upper = Ap.diag - Am.diag, Ap.lower - Am.lower, Ap.upper - Am.upper
+        cancellation.
+
+        The assembled matrix is linear in gamma, A(gamma +- h e_f) =
+        A(gamma) +- h E with E = fvm.laplacian(e_f), so the perturbed
+        matrices are formed from A(gamma) and E instead of by re-assembly.
+        (Re-assembling would round the perturbed diagonals, |diag| ~ 1/dt +
+        sum c >> h c_f, and that rounding -- which breaks the zero row sum
+        of the perturbation -- enters the quotient divided by h; since the
+        gradient results from a near-cancellation between the diagonal and
+        off-diagonal parts of dA/dgamma, it would dominate the check.)
+
+        The difference d_t = x+_t - x-_t of the two trajectories obeys
+            A+ d_{t+1} = d_t / dt - 2h E x-_{t+1},   d_0 = 0,
+        so d is solved for directly, accurate to the solver tolerance
+        relative to |d| rather than |x|, and L+ - L- = sum d (x+ + x- -
+        2 target).  The difference systems are solved with power-of-two
+        normalisation (``_solve_normalised``): their right-hand sides are
+        small and local, and the solver's absolute breakdown threshold
+        would otherwise end the solves early."""
+        e = torch.zeros_like(gamma)
+        e[face] = 1.0
+        A0 = self.system(gamma)
+        with torch.no_grad():
+            E = fvm.laplacian(e, torch.zeros(1), mesh=self.mesh)
+
+        def shifted(sign: float) -> LduMatrix:
+            M = LduMatrix(A0.n_cells, A0.owner, A0.neighbour, device=A0.device)
+            M._topology = A0.topology()
+            M.diag = A0.diag + (sign * h) * E.diag
+            M.lower = A0.lower + (sign * h) * E.lower
+            M.upper = A0.upper + (sign * h) * E.upper
+            return M
+
+        Ap, Am = shifted(1.0), shifted(-1.0)
+        dA = LduMatrix(A0.n_cells, A0.owner, A0.neighbour, device=A0.device)
+        dA._topology = A0.topology()
+        dA.diag, dA.lower, dA.upper = (2.0 * h) * E.diag, (2.0 * h) * E.lower, (2.0 * h) * E.upper
         xm = x0.to(self.md.device, torch.float64)
         d = torch.zeros_like(xm)
         for _ in range(self.steps):
@@ -213,8 +231,7 @@ class UnrolledImplicitDiffusion:
             d, _, _ = self._solve_normalised(Ap, rhs, d)
             xm = xm_next
         xp = xm + d
-        two_h = float(gp[face] - gm[face])  # the perturbation actually applied (exact)
-        return float(torch.dot(d, xp + xm - 2.0 * target)) / two_h
+        return float(torch.dot(d, xp + xm - 2.0 * target)) / (2.0 * h)
 
     def final_state(self, gamma: torch.Tensor, x0: torch.Tensor) -> torch.Tensor:
         A = self.system(gamma)

@@ -74,9 +74,13 @@ def _register_defaults() -> None:
     from .mixed import MixedPrecisionPCGSolver
     from .pbicgstab import PBiCGSTABSolver
     from .pcg import PCGSolver
+    from .gamg import GAMGSolver
+    from .smooth_solver import SmoothSolver
 
+    _SOLVER_REGISTRY["GAMG"] = GAMGSolver
     _SOLVER_REGISTRY["PCG"] = PCGSolver
     _SOLVER_REGISTRY["PBICGSTAB"] = PBiCGSTABSolver
+    _SOLVER_REGISTRY["SMOOTHSOLVER"] = SmoothSolver
     _SOLVER_REGISTRY["MIXEDPCG"] = MixedPrecisionPCGSolver
 
 
@@ -101,8 +105,14 @@ def create_solver(name: str, *, tolerance: float = 1e-6, rel_tol: float = 0.01,
 
 def solver_from_dict(solver_name: str, solver_dict: dict[str, Any]) -> LinearSolverBase:
     """Solver from an fvSolution sub-dictionary (linear_solver.py:259-304):
-    ``tolerance``, ``relTol``, ``maxIter``, ``preconditioner``."""
+    ``tolerance``, ``relTol``, ``maxIter``, ``preconditioner`` and, for
+    smoothSolver, ``smoother`` and ``nSweeps``."""
     extra: dict[str, Any] = {}
+    if solver_name.upper().replace("-", "").replace("_", "") == "SMOOTHSOLVER":
+        if "smoother" in solver_dict:
+            extra["smoother"] = solver_dict["smoother"]
+        if "nSweeps" in solver_dict:
+            extra["n_sweeps"] = int(solver_dict["nSweeps"])
     if "preconditioner" in solver_dict:
         extra["preconditioner"] = solver_dict["preconditioner"]
     return create_solver(

@@ -31,11 +31,18 @@ __all__ = ["MixedPrecisionPCGSolver"]
 class MixedPrecisionPCGSolver(LinearSolverBase):
     """PCG with FP32 inner iterations and FP64 reliable updates.
 
-    ``delta`` (keyword only) is the residual reduction between FP64 updates."""
+    ``delta`` (keyword only) is the residual reduction between FP64 updates.
+    ``symmetric_storage`` (keyword only, default False): when the matrix is
+    symmetric bit for bit and its layout allows it, the FP32 inner Amul
+    reads only the owner-side half of the off-diagonals (same results, 35 %
+    fewer DRAM bytes, but three more gathered loads per cell: on GB300 at
+    256^3 the kernel is then latency-bound and slower, 139.6 vs 121.8 us per
+    launch, so it is off by default)."""
 
     def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 1000,
                  min_iter: int = 0, verbose: bool = False, preconditioner: str = "DIC", *,
-                 delta: float = 0.1, check_every: int = 32) -> None:
+                 delta: float = 0.1, check_every: int = 32,
+                 symmetric_storage: bool = False) -> None:
         super().__init__(tolerance=tolerance, rel_tol=rel_tol, max_iter=max_iter,
                          min_iter=min_iter, verbose=verbose)
         self._precond_type = preconditioner.upper()
@@ -43,6 +50,7 @@ class MixedPrecisionPCGSolver(LinearSolverBase):
             raise ValueError(f"delta must be in (0, 1), got {delta}")
         self._delta = float(delta)
         self._check_every = int(check_every)
+        self._symmetric_storage = bool(symmetric_storage)
         self.last_result: _lib.SolveResult | None = None
 
     def _make_preconditioner(self, matrix: LduMatrix) -> Preconditioner | None:
@@ -72,7 +80,11 @@ class MixedPrecisionPCGSolver(LinearSolverBase):
         pd = None if precond is None else precond.precond_diag
         topo = matrix.topology()
         coef64 = matrix.packed()
-        coef32 = matrix.packed(dtype=torch.float32)
+        # symmetric matrices: the inner Amul streams only the owner-side half
+        coef32 = matrix.packed_sym32() if self._symmetric_storage else None
+        sym = coef32 is not None
+        if not sym:
+            coef32 = matrix.packed(dtype=torch.float32)
         L = _lib.lib()
         cap = 4096
         hist = torch.zeros(cap, device=dev, dtype=torch.float64)
@@ -83,7 +95,8 @@ class MixedPrecisionPCGSolver(LinearSolverBase):
         R = _lib.SolveResult()
         _lib.check(
             L.gbf_mixed_pcg_solve(topo.layout_ref, coef64.data_ptr(), matrix.diag.data_ptr(),
-                                  coef32.data_ptr(), None if pd is None else pd.data_ptr(),
+                                  coef32.data_ptr(), int(sym),
+                                  None if pd is None else pd.data_ptr(),
                                   b.data_ptr(), x.data_ptr(), self._delta, hist.data_ptr(), cap,
                                   ctypes.byref(P), ctypes.byref(R), ws.data_ptr(), ws.numel(),
                                   _lib.stream_ptr(dev)),

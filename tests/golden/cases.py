@@ -174,3 +174,86 @@ def dlap_case(tag: str) -> dict:
     d["kind"], d["D"] = kind, D
     d["expect"] = {k[len(tag) + 1:]: z[k] for k in z.files if k.startswith(tag + "_")}
     return d
+
+
+# ---------------------------------------------------------------------------
+# Polyhedral meshes for the geometry goldens (points, faces, owner,
+# neighbour, boundary) in OpenFOAM conventions: owner < neighbour, internal
+# faces before boundary faces, normals out of the owner.
+# ---------------------------------------------------------------------------
+def hex_polymesh(nx: int, ny: int, nz: int, jitter: float = 0.2, seed: int = 11) -> dict:
+    """Jittered hex mesh of the unit box as a polyMesh."""
+    from pyopenfoam_gb300.mesh.hex_mesh import PATCH_NAMES, HexMesh
+
+    m = HexMesh(nx, ny, nz, jitter=jitter, seed=seed)
+    cells = np.concatenate([m._int_cell, m._bnd_cell])
+    kind = np.concatenate([m._int_dir, m._bnd_kind + 3])
+    faces = m._face_points(cells, kind)
+    boundary = [{"name": p, "type": "patch", "startFace": m.patches[p].start,
+                 "nFaces": m.patches[p].size} for p in PATCH_NAMES]
+    return dict(points=m._points.copy(), face_ptr=np.arange(0, 4 * faces.shape[0] + 1, 4),
+                face_pts=faces.ravel().astype(np.int64), owner=m._owner_np.copy(),
+                neighbour=m._neigh_np.copy(), boundary=boundary)
+
+
+def prism_polymesh(nx: int, ny: int, nz: int, jitter: float = 0.15, seed: int = 12) -> dict:
+    """Each hex of an nx*ny*nz box split along its xy diagonal into two
+    triangular prisms (triangle and quad faces, five faces per cell)."""
+    rng = np.random.default_rng(seed)
+    P = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)  # noqa: E731
+    gx, gy, gz = (np.linspace(0.0, 1.0, n + 1) for n in (nx, ny, nz))
+    Z, Y, X = np.meshgrid(gz, gy, gx, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    pid = np.arange(pts.shape[0])
+    ii, jj, kk = pid % (nx + 1), (pid // (nx + 1)) % (ny + 1), pid // ((nx + 1) * (ny + 1))
+    inner = (ii > 0) & (ii < nx) & (jj > 0) & (jj < ny) & (kk > 0) & (kk < nz)
+    h = np.array([1.0 / nx, 1.0 / ny, 1.0 / nz])
+    pts[inner] += rng.uniform(-jitter, jitter, (int(inner.sum()), 3)) * h
+    # cells: triangles (a, b, c) in xy, counter-clockwise seen from +z
+    cell_tris = []
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                p00, p10, p11, p01 = (i, j), (i + 1, j), (i + 1, j + 1), (i, j + 1)
+                cell_tris.append((k, (p00, p10, p11)))
+                cell_tris.append((k, (p00, p11, p01)))
+    n_cells = len(cell_tris)
+    centroid = np.array([np.mean([pts[P(a, b, kk_)] for (a, b) in tri for kk_ in (k, k + 1)],
+                                 axis=0) for k, tri in cell_tris])
+    faces: dict[tuple, list] = {}
+    for c, (k, tri) in enumerate(cell_tris):
+        bot = [P(a, b, k) for (a, b) in tri]
+        top = [P(a, b, k + 1) for (a, b) in tri]
+        cand = [bot, top] + [[bot[q], bot[(q + 1) % 3], top[(q + 1) % 3], top[q]]
+                              for q in range(3)]
+        for f in cand:
+            faces.setdefault(tuple(sorted(f)), []).append((c, f))
+    internal, bnd = [], []
+    for key, users in faces.items():
+        if len(users) == 2:
+            (c0, f0), (c1, _) = sorted(users)
+            internal.append((c0, c1, f0))
+        else:
+            bnd.append((users[0][0], users[0][1]))
+    internal.sort(key=lambda t: (t[0], t[1]))
+    bnd.sort(key=lambda t: t[0])
+
+    def orient(f, frm, to):
+        v = pts[f]
+        a = 0.5 * sum(np.cross(v[q], v[(q + 1) % len(f)]) for q in range(len(f)))
+        return f if np.dot(a, to - frm) > 0 else f[::-1]
+
+    flist, own, nei = [], [], []
+    for c0, c1, f in internal:
+        flist.append(orient(f, centroid[c0], centroid[c1]))
+        own.append(c0)
+        nei.append(c1)
+    for c0, f in bnd:
+        flist.append(orient(f, centroid[c0], pts[f].mean(axis=0)))
+        own.append(c0)
+    ptr = np.concatenate([[0], np.cumsum([len(f) for f in flist])])
+    return dict(points=pts, face_ptr=ptr.astype(np.int64),
+                face_pts=np.concatenate(flist).astype(np.int64),
+                owner=np.array(own, np.int64), neighbour=np.array(nei, np.int64),
+                boundary=[{"name": "walls", "type": "wall", "startFace": len(internal),
+                           "nFaces": len(bnd)}], n_cells=n_cells)

@@ -4,6 +4,10 @@ Run in a checkout that has the reference project next to it:
 
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --dlap
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --geometry
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --pressure
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --smooth
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --gamg
 
 It imports the reference's own classes (``pyfoam.core.ldu_matrix``,
 ``pyfoam.solvers.*``, ``pyfoam.discretisation.operators.fvm``,
@@ -273,10 +277,188 @@ def dlap(ref_root: str) -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def geometry(ref_root: str) -> None:
+    """FvMesh geometry goldens (mesh/fv_mesh.py:75-148 on
+    mesh/mesh_geometry.py:35-395) of a jittered hex polyMesh, a triangular
+    prism polyMesh and the reference's own two-cell unit-test mesh, inputs
+    included -> reference_geometry.npz."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import torch
+    from pyfoam.core.dtype import INDEX_DTYPE
+    from pyfoam.mesh.fv_mesh import FvMesh
+
+    from tests.golden.cases import hex_polymesh, prism_polymesh
+
+    torch.set_num_threads(8)
+    out = {}
+    two = dict(points=np.array(_TWO_CELL_POINTS, np.float64),
+               face_ptr=np.arange(0, 4 * len(_TWO_CELL_FACES) + 1, 4),
+               face_pts=np.array(_TWO_CELL_FACES, np.int64).ravel(),
+               owner=np.array(_TWO_CELL_OWNER, np.int64), neighbour=np.array([1], np.int64))
+    for tag, mesh in (("hex", hex_polymesh(4, 3, 3)), ("prism", prism_polymesh(3, 2, 2)),
+                      ("two", two)):
+        ptr, pts = mesh["face_ptr"], mesh["face_pts"]
+        faces = [torch.tensor(pts[ptr[i]:ptr[i + 1]], dtype=INDEX_DTYPE)
+                 for i in range(ptr.shape[0] - 1)]
+        m = FvMesh(points=torch.tensor(mesh["points"], dtype=torch.float64), faces=faces,
+                   owner=torch.tensor(mesh["owner"], dtype=INDEX_DTYPE),
+                   neighbour=torch.tensor(mesh["neighbour"], dtype=INDEX_DTYPE))
+        m.compute_geometry()
+        for k in ("points", "face_ptr", "face_pts", "owner", "neighbour"):
+            out[f"{tag}_{k}"] = np.asarray(mesh[k])
+        for k in ("face_centres", "face_areas", "cell_volumes", "cell_centres", "face_weights",
+                  "delta_coefficients"):
+            out[f"{tag}_{k}"] = getattr(m, k).numpy().copy()
+        out[f"{tag}_n_cells"] = np.int64(m.n_cells)
+        print(tag, m.n_cells, float(m.total_volume), flush=True)
+    path = os.path.join(HERE, "reference_geometry.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+def pressure(ref_root: str) -> None:
+    """Pressure-corrector steps either side of the solve on the jittered 6^3
+    mesh: correct_velocity, correct_face_flux, adjust_phi
+    (solvers/pressure_equation.py:187-377) and the Rhie-Chow functions
+    (solvers/rhie_chow.py:56-250) -> reference_pressure.npz."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import torch
+    from pyfoam.discretisation.weights import compute_centre_weights
+    from pyfoam.solvers import rhie_chow as RC
+    from pyfoam.solvers.pressure_equation import (adjust_phi, correct_face_flux,
+                                                  correct_velocity)
+
+    torch.set_num_threads(8)
+    t = torch.from_numpy
+    jc = jitter_case(6, seed=1)
+    mesh = jc["mesh"]
+    n, nf, ni = mesh.n_cells, mesh.n_faces, mesh.n_internal_faces
+    w = compute_centre_weights(mesh.cell_centres, mesh.face_centres, mesh.owner, mesh.neighbour,
+                               ni, nf, dtype=torch.float64)
+    mesh.face_weights = w
+    rng = np.random.default_rng(21)
+    A_p = rng.uniform(0.5, 3.0, n) * np.where(rng.random(n) < 0.2, -1, 1)
+    A_p[4] = 0.0
+    p = rng.uniform(-1.0, 1.0, n)
+    H = rng.normal(0.0, 1.0, (n, 3))
+    HbyA = rng.normal(0.0, 1.0, (n, 3))
+    HbyA[7] = [3e4, -2e4, 1e4]  # above the 1e4 velocity limit
+    phi = rng.normal(0.0, 1.0, nf)
+    out = dict(A_p=A_p, p=p, H=H, HbyA=HbyA, phi=phi, weights=w.numpy().copy())
+    out["cv"] = correct_velocity(t(HbyA), t(HbyA), t(p), t(A_p), mesh).numpy().copy()
+    out["cv_a07"] = correct_velocity(t(HbyA), t(HbyA), t(p), t(A_p), mesh,
+                                     alpha=0.7).numpy().copy()
+    out["cff"] = correct_face_flux(t(phi), t(p), t(A_p), mesh, face_weights=w).numpy().copy()
+    ph = t(phi).clone()
+    out["adj_ret"] = np.int64(adjust_phi(ph, mesh))
+    out["adj_phi"] = ph.numpy().copy()
+    own, nei = mesh.owner, mesh.neighbour
+    S, dl, V = mesh.face_areas, mesh.delta_coefficients, mesh.cell_volumes
+    out["hbya"] = RC.compute_HbyA(t(H), t(A_p)).numpy().copy()
+    out["ffh_w"] = RC.compute_face_flux_HbyA(t(HbyA), S, own, nei, ni, w).numpy().copy()
+    out["ffh_half"] = RC.compute_face_flux_HbyA(t(HbyA), S, own, nei, ni).numpy().copy()
+    out["rc_w"] = RC.rhie_chow_correction(t(p), t(A_p), S, dl, own, nei, ni, V, w).numpy().copy()
+    out["rc_half"] = RC.rhie_chow_correction(t(p), t(A_p), S, dl, own, nei, ni, V).numpy().copy()
+    out["ff_w"] = RC.compute_face_flux(t(HbyA), t(p), t(A_p), S, dl, own, nei, ni, V,
+                                       w).numpy().copy()
+    path = os.path.join(HERE, "reference_pressure.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+def smoothers(ref_root: str) -> None:
+    """SmoothSolver (solvers/smooth_solver.py:37-232) with its three
+    smoothers and the standalone smoothers (solvers/smoothers.py:63-260) on
+    seeded diagonally dominant 4^3 systems, triangular and permuted face
+    order -> reference_smooth.npz."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import torch
+    from pyfoam.core.ldu_matrix import LduMatrix
+    from pyfoam.solvers.smooth_solver import SmoothSolver
+    from pyfoam.solvers.smoothers import DICGSmoother, GaussSeidelSmoother, JacobiSmoother
+
+    torch.set_num_threads(8)
+    t = torch.from_numpy
+    out = {}
+    for tag, perm in (("tri", False), ("perm", True)):
+        c = random_ldu(4, seed=31, permute_faces=perm)
+        m = LduMatrix(c["n"], t(c["owner"]), t(c["neighbour"]))
+        m.diag, m.lower, m.upper = t(c["diag"]), t(c["lower"]), t(c["upper"])
+        b, x0 = t(c["r"]), t(c["x"])
+        for sm in ("GaussSeidel", "DIC", "DILU"):
+            s = SmoothSolver(tolerance=0.0, rel_tol=0.0, max_iter=3, smoother=sm, n_sweeps=2,
+                             omega=0.9 if sm != "GaussSeidel" else 1.0)
+            x, it, res = s(m, b, x0)
+            out[f"{tag}_ss_{sm}_x"] = x.numpy().copy()
+            out[f"{tag}_ss_{sm}_it"] = np.int64(it)
+            out[f"{tag}_ss_{sm}_res"] = np.float64(res)
+        out[f"{tag}_gs_x"] = GaussSeidelSmoother(m, omega=0.8).smooth(x0, b, 2).numpy().copy()
+        out[f"{tag}_jac_x"] = JacobiSmoother(m).smooth(x0, b, 3).numpy().copy()
+        out[f"{tag}_dicg_x"] = DICGSmoother(m, omega=0.9).smooth(x0, b, 2).numpy().copy()
+        print(tag, flush=True)
+    path = os.path.join(HERE, "reference_smooth.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+def gamg(ref_root: str) -> None:
+    """GAMGSolver (solvers/gamg.py:104-585) on a 6^3 Poisson system and a
+    random diagonally dominant 5^3 system with permuted faces: hierarchy
+    (aggregation maps, coarse coefficients) and x after a fixed number of
+    V-cycles -> reference_gamg.npz."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import torch
+    from pyfoam.core.ldu_matrix import LduMatrix
+    from pyfoam.solvers.gamg import GAMGSolver
+
+    torch.set_num_threads(8)
+    t = torch.from_numpy
+    out = {}
+    cases = {"poi": c1_poisson(6, seed=4), "rnd": random_ldu(5, seed=41, permute_faces=True)}
+    cases["rnd"]["b"] = cases["rnd"]["r"]
+    for tag, c in cases.items():
+        m = LduMatrix(c["n"], t(c["owner"]), t(c["neighbour"]))
+        m.diag, m.lower, m.upper = t(c["diag"]), t(c["lower"]), t(c["upper"])
+        s = GAMGSolver(tolerance=0.0, rel_tol=0.0, max_iter=4, min_cells_coarse=10)
+        x, it, res = s(m, t(c["b"]), torch.zeros(c["n"], dtype=torch.float64))
+        out[f"{tag}_x"] = x.numpy().copy()
+        out[f"{tag}_it"] = np.int64(it)
+        out[f"{tag}_res"] = np.float64(res)
+        # the hierarchy, rebuilt with the reference's own static methods
+        temp = m
+        sizes = [m.n_cells]
+        for lvl in range(3):
+            if temp.n_cells <= 10:
+                break
+            agg = GAMGSolver._build_aggregates(temp, max(temp.n_cells // 2, 10))
+            if agg.n_coarse >= temp.n_cells:
+                break
+            cl = GAMGSolver._build_coarse_matrix(temp, agg)
+            out[f"{tag}_f2c{lvl}"] = agg.fine_to_coarse.numpy().copy()
+            for k in ("diag", "lower", "upper", "owner", "neighbour"):
+                out[f"{tag}_L{lvl + 1}_{k}"] = getattr(cl, k).numpy().copy()
+            sizes.append(cl.n_cells)
+            temp = LduMatrix(cl.n_cells, cl.owner, cl.neighbour)
+            temp.diag, temp.lower, temp.upper = cl.diag, cl.lower, cl.upper
+        out[f"{tag}_sizes"] = np.array(sizes, np.int64)
+        print(tag, it, res, sizes, flush=True)
+    path = os.path.join(HERE, "reference_gamg.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else os.environ.get("PYFOAM_REFERENCE", "")
     if "--dlap" in sys.argv:
         dlap(root)
+    elif "--geometry" in sys.argv:
+        geometry(root)
+    elif "--pressure" in sys.argv:
+        pressure(root)
+    elif "--smooth" in sys.argv:
+        smoothers(root)
+    elif "--gamg" in sys.argv:
+        gamg(root)
     else:
         main(root)

@@ -216,3 +216,57 @@ def test_staged_float32_amul_matches_generic_gather(N):
     fault = ctypes.c_int32(-1)
     _lib.check(L.gbf_stream_fault(ctypes.byref(fault)))
     assert fault.value == 0
+
+
+@pytest.mark.parametrize("N", [7, 20, 64])
+def test_symmetric_half_storage_amul_matches_full_packing(N):
+    """A symmetric matrix (lower == upper) stored as its owner-side half:
+    gbf_amul_sym_f32 -- staged (aligned) and global-memory (unaligned x)
+    paths -- gives the bits of gbf_amul_f32 on the full packing and of the
+    float oracle; a non-symmetric matrix is refused by the packing."""
+    import ctypes
+
+    from pyopenfoam_gb300 import _lib
+
+    c = random_ldu(N, 23, False)
+    m = mat(c["n"], c["owner"], c["neighbour"], c["diag"], c["lower"], c["lower"])
+    topo = m.topology()
+    assert topo.symmetric_storage
+    half = m.packed_sym32()
+    assert half is not None and half.numel() == topo.n_slots // 2
+    full = m.packed(dtype=torch.float32)
+    L = _lib.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    n = c["n"]
+    d32 = m.diag.float().contiguous()
+    xa = torch.as_tensor(c["x"]).float().to(DEV)  # 16-byte aligned
+    xbuf = torch.zeros(n + 4, device=DEV, dtype=torch.float32)
+    xbuf[1:n + 1] = xa
+    xu = xbuf[1:n + 1]  # the same values, 4 bytes off alignment
+    y_full = torch.empty(n, device=DEV, dtype=torch.float32)
+    _lib.check(L.gbf_amul_f32(topo.layout_ref, full.data_ptr(), d32.data_ptr(), xa.data_ptr(),
+                              y_full.data_ptr(), 0, st))
+    for x in (xa, xu):
+        y = torch.empty(n, device=DEV, dtype=torch.float32)
+        for _ in range(2):
+            _lib.check(L.gbf_amul_sym_f32(topo.layout_ref, half.data_ptr(), d32.data_ptr(),
+                                          x.data_ptr(), y.data_ptr(), st))
+            a, b = y.cpu().numpy(), y_full.cpu().numpy()
+            assert (a.view(np.uint32) == b.view(np.uint32)).all()
+    ref = O.amul(c["owner"], c["neighbour"], c["diag"].astype(np.float32),
+                 c["lower"].astype(np.float32), c["lower"].astype(np.float32),
+                 c["x"].astype(np.float32), float_accumulate=True)
+    np.testing.assert_array_equal(y_full.cpu().numpy(), ref)
+    fault = ctypes.c_int32(-1)
+    _lib.check(L.gbf_stream_fault(ctypes.byref(fault)))
+    assert fault.value == 0
+    # lower != upper in one face: no half storage
+    m.upper = torch.as_tensor(c["lower"]).clone()
+    up = m.upper.clone()
+    up[5] = up[5] * 0.5
+    m.upper = up
+    assert m.packed_sym32() is None
+    # -0.0 vs +0.0 differ in bits: not symmetric for the packing either
+    lo = torch.zeros_like(up)
+    m.lower, m.upper = lo, -lo
+    assert m.packed_sym32() is None

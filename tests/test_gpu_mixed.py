@@ -94,3 +94,23 @@ def test_mixed_zero_rhs_and_float32_rejected():
         MixedPrecisionPCGSolver()(m32, torch.ones(2), torch.zeros(2))
     with pytest.raises(TypeError):
         PCGSolver()(m32, torch.ones(2), torch.zeros(2))
+
+
+@pytest.mark.parametrize("N", [20, 48])
+def test_mixed_symmetric_half_storage_gives_identical_solve(N):
+    """The inner Amul on the owner-side half of a symmetric matrix gives the
+    bits of the full-packing Amul, so the whole mixed solve -- iterations,
+    FP64 updates, x -- is bit for bit the same with and without it."""
+    d = hex_poisson(N, seed=5)
+    m = mat(d)
+    assert m.topology().symmetric_storage and m.packed_sym32() is not None
+    out = []
+    for sym in (True, False):
+        s = MixedPrecisionPCGSolver(tolerance=0.0, rel_tol=1e-10, max_iter=5000,
+                                    symmetric_storage=sym)
+        x, it, res = s(m, torch.as_tensor(d["b"]), torch.zeros(d["n"], dtype=f64))
+        assert s.last_info.converged
+        out.append((x.cpu().numpy(), it, res, s.last_result.outer_updates))
+    (xa, ia, ra, ua), (xb, ib, rb, ub) = out
+    assert (ia, ra, ua) == (ib, rb, ub)
+    assert (xa.view(np.int64) == xb.view(np.int64)).all()

@@ -1,0 +1,73 @@
+"""SmoothSolver (GaussSeidel / DIC / DILU smoothers) and the standalone
+smoothers (GaussSeidelSmoother, JacobiSmoother, DICGSmoother) on the GPU
+against the reference's own outputs (tests/golden/reference_smooth.npz,
+make_golden.py --smooth) on 4^3 systems with triangular and with permuted
+face order (a third of the faces owner > neighbour).
+
+Bars: x bitwise and the same iteration count; the final residual norm to
+1e-13 relative (a different summation order of the same residual)."""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from pyopenfoam_gb300 import LduMatrix, create_solver, solver_from_dict
+from pyopenfoam_gb300.solvers import (DICGSmoother, GaussSeidelSmoother, JacobiSmoother,
+                                      SmoothSolver)
+from tests.golden.cases import hex_poisson, random_ldu
+
+pytestmark = pytest.mark.gpu
+SM = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_smooth.npz"))
+
+
+def _case(perm):
+    c = random_ldu(4, seed=31, permute_faces=perm)
+    m = LduMatrix(c["n"], torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(c[k]) for k in ("diag", "lower", "upper"))
+    return m, torch.as_tensor(c["r"]), torch.as_tensor(c["x"])
+
+
+def _eq(a, b):
+    return (np.ascontiguousarray(a).view(np.int64) == np.ascontiguousarray(b).view(np.int64)).all()
+
+
+@pytest.mark.parametrize("tag,perm", [("tri", False), ("perm", True)])
+@pytest.mark.parametrize("sm", ["GaussSeidel", "DIC", "DILU"])
+def test_smooth_solver_matches_reference(tag, perm, sm):
+    m, b, x0 = _case(perm)
+    s = SmoothSolver(tolerance=0.0, rel_tol=0.0, max_iter=3, smoother=sm, n_sweeps=2,
+                     omega=0.9 if sm != "GaussSeidel" else 1.0)
+    x, it, res = s(m, b, x0)
+    assert x.device.type == "cuda"
+    assert _eq(x.cpu().numpy(), SM[f"{tag}_ss_{sm}_x"]), sm
+    assert it == int(SM[f"{tag}_ss_{sm}_it"])
+    assert abs(res - float(SM[f"{tag}_ss_{sm}_res"])) <= 1e-13 * float(SM[f"{tag}_ss_{sm}_res"])
+
+
+@pytest.mark.parametrize("tag,perm", [("tri", False), ("perm", True)])
+def test_smoothers_match_reference(tag, perm):
+    m, b, x0 = _case(perm)
+    assert _eq(GaussSeidelSmoother(m, omega=0.8).smooth(x0, b, 2).cpu().numpy(), SM[f"{tag}_gs_x"])
+    assert _eq(JacobiSmoother(m).smooth(x0, b, 3).cpu().numpy(), SM[f"{tag}_jac_x"])
+    assert _eq(DICGSmoother(m, omega=0.9).smooth(x0, b, 2).cpu().numpy(), SM[f"{tag}_dicg_x"])
+
+
+def test_smooth_solver_converges_and_factory():
+    d = hex_poisson(12, seed=3)
+    m = LduMatrix(d["n"], torch.as_tensor(d["owner"]), torch.as_tensor(d["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(d[k]) for k in ("diag", "lower", "upper"))
+    b = torch.as_tensor(d["b"])
+    s = solver_from_dict("smoothSolver", {"smoother": "GaussSeidel", "nSweeps": 3,
+                                          "tolerance": 0.0, "relTol": 1e-3, "maxIter": 2000})
+    assert isinstance(s, SmoothSolver) and s._n_sweeps == 3
+    x, it, res = s(m, b, torch.zeros_like(b))
+    assert s.last_info.converged
+    r = b.cuda() - m.Ax(x)
+    assert float(r.norm()) / float(b.norm()) < 1e-3
+    assert isinstance(create_solver("smoothsolver", smoother="DIC"), SmoothSolver)
+    with pytest.raises(ValueError):
+        SmoothSolver(smoother="Jacobi")(m, b, torch.zeros_like(b))

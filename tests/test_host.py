@@ -207,3 +207,93 @@ def test_layout_offset_compression_reproduces_columns(perm):
     if not perm:
         # structured numbering: every slot is one offset per slice
         assert nu.value == col.shape[0] // 32
+
+
+@pytest.mark.parametrize("N", [32, 20, 16, 7])
+def test_layout_mirror_maps_neighbour_slots_to_owner_slots(N):
+    """Every neighbour-side slot of a hex layout points (offset + mirror
+    slot) at the owner-side slot of the same face, which is what the
+    symmetric half storage reads; irregular numberings report ok = 0."""
+    n, own, nei = hex_faces(N)
+    off, w, col, face, mw = _layout(n, own, nei, pad=5)
+    ns = off.shape[0] - 1
+    wo, wn = int(w[0] & 0xFFFF), int(w[0] >> 16)
+    assert all(int(v) == int(w[0]) for v in w[:ns])  # uniform widths
+    W = wo + wn
+    ne = ns * W
+    dm = np.empty(2 * ne, np.int32)
+    nu = ctypes.c_int64()
+    L = _lib.lib()
+    _lib.check(L.gbf_layout_compress(ns, off.ctypes.data, w.ctypes.data, col.ctypes.data,
+                                     dm.ctypes.data, ctypes.byref(nu)))
+    assert nu.value == ne
+    o32 = np.ascontiguousarray(own, np.int32)
+    mir = np.empty(ne, np.int8)
+    ok = ctypes.c_int32()
+    _lib.check(L.gbf_layout_mirror(own.shape[0], ns, wo, wn, face.ctypes.data, o32.ctypes.data,
+                                   dm.ctypes.data, mir.ctypes.data, ctypes.byref(ok)))
+    pos_own = {}  # face -> (owner cell, owner-side slot j)
+    for s in range(ns):
+        for j in range(wo):
+            for lane in range(32):
+                f = face[32 * (s * W + j) + lane]
+                if f >= 0:
+                    pos_own[int(f)] = (32 * s + lane, j)
+    uniform = True
+    for s in range(ns):
+        for k in range(wo, W):
+            e = s * W + k
+            js = set()
+            for lane in range(32):
+                f = face[32 * e + lane]
+                if f < 0:
+                    continue
+                cell_o, j = pos_own[int(f)]
+                assert cell_o == 32 * s + lane + dm[2 * e]
+                js.add(j)
+            if len(js) > 1:
+                uniform = False
+            elif js and ok.value:
+                assert mir[e] == js.pop()
+    assert ok.value == int(uniform)
+    if N % 32 == 0:
+        assert ok.value == 1
+    # bad owner table: refused
+    bad = o32.copy()
+    bad[0] += 1
+    _lib.check(L.gbf_layout_mirror(own.shape[0], ns, wo, wn, face.ctypes.data, bad.ctypes.data,
+                                   dm.ctypes.data, mir.ctypes.data, ctypes.byref(ok)))
+    assert ok.value == 0
+
+
+def test_polymesh_reader_round_trip_and_mixed_faces(tmp_path):
+    """ASCII polyMesh files: write, read back, compare (uniform quads take
+    the reshape path, the prism mesh's triangles + quads the counted path);
+    comments are skipped and binary files are refused."""
+    from pyopenfoam_gb300.io import read_faces, read_mesh, write_mesh
+    from pyopenfoam_gb300.io.mesh_io import BoundaryPatch
+    from tests.golden.cases import hex_polymesh, prism_polymesh
+
+    for tag, d in (("hex", hex_polymesh(3, 2, 2)), ("prism", prism_polymesh(2, 2, 1))):
+        ptr, pts = d["face_ptr"], d["face_pts"]
+        faces = [pts[ptr[i]:ptr[i + 1]] for i in range(ptr.shape[0] - 1)]
+        patches = [BoundaryPatch(b["name"], b["type"], b["nFaces"], b["startFace"], ["g1"])
+                   for b in d["boundary"]]
+        out = tmp_path / tag
+        write_mesh(out, d["points"], faces, d["owner"], d["neighbour"], patches)
+        md = read_mesh(out)
+        assert np.array_equal(md.points.numpy(), d["points"])
+        assert np.array_equal(md.face_ptr, ptr) and np.array_equal(md.face_pts, pts)
+        assert np.array_equal(md.owner.numpy(), d["owner"])
+        assert np.array_equal(md.neighbour.numpy(), d["neighbour"])
+        assert [(p.name, p.n_faces, p.start_face, p.in_groups) for p in md.boundary] == \
+               [(b["name"], b["nFaces"], b["startFace"], ["g1"]) for b in d["boundary"]]
+        assert md.n_cells == int(d["owner"].max()) + 1
+    f = tmp_path / "faces_commented"
+    f.write_text("/* c */\nFoamFile\n{\n format ascii;\n class faceList;\n}\n// x\n"
+                 "2\n(\n3(0 1 2) // tri\n4(2 3 4 5)\n)\n")
+    _, (p, q) = read_faces(f)
+    assert p.tolist() == [0, 3, 7] and q.tolist() == [0, 1, 2, 2, 3, 4, 5]
+    f.write_text("FoamFile\n{\n format binary;\n}\n2\n(\n)\n")
+    with pytest.raises(ValueError):
+        read_faces(f)
