@@ -433,6 +433,19 @@ int gbf_gamg_coarse_coeffs_f64(int32_t n_cfaces, const int32_t* cf_ptr, const in
 int gbf_gamg_prolong_add_f64(int32_t n_fine, const int32_t* f2c, const double* e, double* x,
                              void* stream);
 
+/* out = x + a*y (one rounding each; out may alias x or y): the vector
+ * updates of PBiCGSolver (solvers/pbicg.py:161-200).                       */
+int gbf_xpay_f64(int32_t n, const double* x, double a, const double* y, double* out,
+                 void* stream);
+/* *out (DEVICE) = a . b in a fixed summation order (torch.dot of the
+ * reference solvers); workspace of gbf_norm2_workspace_bytes().            */
+int gbf_dot_f64(int32_t n, const double* a, const double* b, double* out, void* workspace,
+                void* stream);
+/* DiagonalSolver (solvers/diagonal.py:55-85): x = b / max(|diag|, 1e-30),
+ * r = b - diag*x.                                                          */
+int gbf_diagonal_solve_f64(int32_t n, const double* diag, const double* b, double* x, double* r,
+                           void* stream);
+
 /* ---- pressure-corrector steps ---------------------------------------------
  * The steps either side of the pressure solve in SIMPLE / PISO, bitwise the
  * reference's (one rounding per operation in its order).  owner is the

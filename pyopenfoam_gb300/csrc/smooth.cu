@@ -90,7 +90,46 @@ __global__ void __launch_bounds__(kBlock)
   x[c] = __dadd_rn(x[c], __dmul_rn(s, __ldg(z + c)));
 }
 
+// out = x + a * y (one rounding each); out may alias x or y.
+__global__ void __launch_bounds__(kBlock)
+    xpay_kernel(int n, const double* x, double a, const double* y, double* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) out[c] = __dadd_rn(x[c], __dmul_rn(a, y[c]));
+}
+
+// DiagonalSolver: x = b / max(|d|, 1e-30), r = b - d * x.
+__global__ void __launch_bounds__(kBlock)
+    diagonal_solve_kernel(int n, const double* __restrict__ d, const double* __restrict__ b,
+                          double* __restrict__ x, double* __restrict__ r) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double dc = __ldg(d + c), a = fabs(dc), bc = __ldg(b + c);
+  const double xc = __ddiv_rn(bc, a > 1e-30 ? a : 1e-30);
+  x[c] = xc;
+  r[c] = __dsub_rn(bc, __dmul_rn(dc, xc));
+}
+
 constexpr int kNormBlocks = 1024;
+
+__global__ void __launch_bounds__(kBlock)
+    dot_partials_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                        double* __restrict__ partials) {
+  __shared__ double sh[kBlock / 32];
+  double s = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+    s = __fma_rn(__ldg(a + c), __ldg(b + c), s);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kBlock)
+    sum_partials_kernel(int g, const double* __restrict__ partials, double* __restrict__ out) {
+  __shared__ double sh[kBlock / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < g; i += blockDim.x) s = __dadd_rn(s, partials[i]);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = s;
+}
 
 __global__ void __launch_bounds__(kBlock)
     sumsq_partials_kernel(int n, const double* __restrict__ r, double* __restrict__ partials) {
@@ -183,6 +222,40 @@ extern "C" int gbf_norm2_f64(int32_t n, const double* r, double* out, void* work
   double* partials = static_cast<double*>(workspace);
   sumsq_partials_kernel<<<g, kBlock, 0, s>>>(n, r, partials);
   sqrt_sum_kernel<<<1, kBlock, 0, s>>>(g, partials, out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_xpay_f64(int32_t n, const double* x, double a, const double* y, double* out,
+                            void* stream) {
+  GBF_REQUIRE(n >= 0, "xpay: negative n");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(x && y && out, "xpay: NULL pointer");
+  xpay_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(n, x, a, y, out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_dot_f64(int32_t n, const double* a, const double* b, double* out,
+                           void* workspace, void* stream) {
+  GBF_REQUIRE(n >= 0 && out && workspace && (n == 0 || (a && b)), "dot: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  int g = (n + kBlock - 1) / kBlock;
+  g = g < 1 ? 1 : (g > kNormBlocks ? kNormBlocks : g);
+  double* partials = static_cast<double*>(workspace);
+  dot_partials_kernel<<<g, kBlock, 0, s>>>(n, a, b, partials);
+  sum_partials_kernel<<<1, kBlock, 0, s>>>(g, partials, out);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_diagonal_solve_f64(int32_t n, const double* diag, const double* b, double* x,
+                                      double* r, void* stream) {
+  GBF_REQUIRE(n >= 0, "diagonal_solve: negative n");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(diag && b && x && r, "diagonal_solve: NULL pointer");
+  diagonal_solve_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(n, diag, b,
+                                                                                   x, r);
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }

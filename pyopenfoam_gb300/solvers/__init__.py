@@ -1,9 +1,11 @@
 """GPU linear solvers with the reference's ``pyfoam.solvers`` interface."""
 
 from .batched import BatchedPCGSolver
+from .diagonal import DiagonalSolver
 from .gamg import GAMGSolver
 from .linear_solver import LinearSolverBase, create_solver, register_solver, solver_from_dict
 from .mixed import MixedPrecisionPCGSolver
+from .pbicg import PBiCGSolver
 from .pbicgstab import PBiCGSTABSolver
 from .pcg import PCGSolver
 from .preconditioners import DICPreconditioner, DILUPreconditioner, Preconditioner
@@ -19,5 +21,5 @@ __all__ = [
     "DILUPreconditioner", "Preconditioner", "ConvergenceInfo", "ResidualMonitor",
     "BatchedPCGSolver", "assemble_pressure_equation", "solve_pressure_equation",
     "correct_velocity", "correct_face_flux", "adjust_phi", "GaussSeidelSmoother",
-    "JacobiSmoother", "DICGSmoother", "GAMGSolver",
+    "JacobiSmoother", "DICGSmoother", "GAMGSolver", "PBiCGSolver", "DiagonalSolver",
 ]

@@ -74,9 +74,13 @@ def _register_defaults() -> None:
     from .mixed import MixedPrecisionPCGSolver
     from .pbicgstab import PBiCGSTABSolver
     from .pcg import PCGSolver
+    from .diagonal import DiagonalSolver
     from .gamg import GAMGSolver
+    from .pbicg import PBiCGSolver
     from .smooth_solver import SmoothSolver
 
+    _SOLVER_REGISTRY["PBICG"] = PBiCGSolver
+    _SOLVER_REGISTRY["DIAGONAL"] = DiagonalSolver
     _SOLVER_REGISTRY["GAMG"] = GAMGSolver
     _SOLVER_REGISTRY["PCG"] = PCGSolver
     _SOLVER_REGISTRY["PBICGSTAB"] = PBiCGSTABSolver
