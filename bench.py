@@ -409,12 +409,14 @@ def run_ours(args, rank, world, local):
     design = design_bytes_ap(n, F, topo.n_slices, sym)
     traffic = NCU_TRAFFIC_AP_256["sym" if sym else "full"] if args.n == 256 else None
     extra["iterations"] = iters[-1]
+    extra["inner_iterations_per_s"] = iters[-1] / sec
     extra["outer_updates"] = mixed.last_result.outer_updates
     extra["true_rel_residual"] = true_rel_residual(m, x, b)
     if x64 is not None:
         extra["x_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(x - x64) /
                                            torch.linalg.vector_norm(x64))
         extra["speedup_vs_fp64"] = extra["fp64_pcg_s"] / sec
+        extra["fp64_iterations_per_s"] = extra["fp64_iterations"] / extra["fp64_pcg_s"]
     extra["amul"] = time_amul(m, dev)
 
     # --- end to end through the public API with host buffers ---

@@ -30,12 +30,15 @@ __device__ __forceinline__ A slot_sum(const gbf_layout& L, const T* __restrict__
     for (int k = 0; k < 4; ++k) a[k] = (k < cnt) ? __ldg(coef + i0 + 32 * k) : (T)0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
+    if (col[0] >= 0) s = first_term((A)mul_rn(a[0], xv[0]));
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 1; k < 4; ++k)
       if (col[k] >= 0) s = add_rn(s, (A)mul_rn(a[k], xv[k]));
   } else {
+    const int col0 = slot_column(L, e0, i0, c);
+    if (col0 >= 0) s = first_term((A)mul_rn(__ldg(coef + i0), __ldg(x + col0)));
 #pragma unroll 4
-    for (int k = 0; k < cnt; ++k) {
+    for (int k = 1; k < cnt; ++k) {
       const int col = slot_column(L, e0 + k, i0 + 32 * k, c);
       if (col >= 0) s = add_rn(s, (A)mul_rn(__ldg(coef + i0 + 32 * k), __ldg(x + col)));
     }
@@ -70,11 +73,13 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
       }
 #pragma unroll
       for (int k = 0; k < 8; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
+      if (col[0] >= 0) so = first_term((A)mul_rn(a[0], xv[0]));
 #pragma unroll
-      for (int k = 0; k < 4; ++k)
+      for (int k = 1; k < 4; ++k)
         if (col[k] >= 0) so = add_rn(so, (A)mul_rn(a[k], xv[k]));
+      if (col[4] >= 0) sn = first_term((A)mul_rn(a[4], xv[4]));
 #pragma unroll
-      for (int k = 4; k < 8; ++k)
+      for (int k = 5; k < 8; ++k)
         if (col[k] >= 0) sn = add_rn(sn, (A)mul_rn(a[k], xv[k]));
     } else {
       so = slot_sum<T, A>(L, coef, x, c, cs.base, cs.e0, cs.wo);
@@ -127,11 +132,13 @@ __device__ __forceinline__ A cell_amul_fixed(const gbf_layout& L, const T* __res
     xv[k] = on[k] ? __ldg(x + c + d[k]) : (T)0;
   }
   A so = (A)0, sn = (A)0;
+  if (WO > 0 && on[0]) so = first_term((A)mul_rn(a[0], xv[0]));
 #pragma unroll
-  for (int k = 0; k < WO; ++k)
+  for (int k = 1; k < WO; ++k)
     if (on[k]) so = add_rn(so, (A)mul_rn(a[k], xv[k]));
+  if (WN > 0 && on[WO]) sn = first_term((A)mul_rn(a[WO], xv[WO]));
 #pragma unroll
-  for (int k = WO; k < W; ++k)
+  for (int k = WO + 1; k < W; ++k)
     if (on[k]) sn = add_rn(sn, (A)mul_rn(a[k], xv[k]));
   A y = (A)mul_rn(__ldg(diag + c), xc);
   if (NEI_FIRST) {
@@ -182,11 +189,13 @@ __device__ __forceinline__ A cell_amul_sym33(const gbf_layout& L, const float* _
 #pragma unroll
   for (int k = 0; k < 6; ++k) xv[k] = on[k] ? __ldg(x + c + d[k]) : 0.0f;
   A so = (A)0, sn = (A)0;
+  if (on[0]) so = first_term((A)__fmul_rn(a[0], xv[0]));
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
+  for (int k = 1; k < 3; ++k)
     if (on[k]) so = add_rn(so, (A)__fmul_rn(a[k], xv[k]));
+  if (on[3]) sn = first_term((A)__fmul_rn(a[3], xv[3]));
 #pragma unroll
-  for (int k = 3; k < 6; ++k)
+  for (int k = 4; k < 6; ++k)
     if (on[k]) sn = add_rn(sn, (A)__fmul_rn(a[k], xv[k]));
   A y = (A)__fmul_rn(__ldg(diag + c), xc);
   y = add_rn(y, so);

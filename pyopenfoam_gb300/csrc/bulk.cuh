@@ -163,11 +163,13 @@ __device__ __forceinline__ A hex_cell_from_stage(const HexStage& S, int tid,
     xv[k] = on[k] ? __ldg(x + c + e.x) : 0.0f;
   }
   A so = (A)0, sn = (A)0;
+  if (on[0]) so = first_term((A)__fmul_rn(a[0], xv[0]));
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
+  for (int k = 1; k < 3; ++k)
     if (on[k]) so = add_rn(so, (A)__fmul_rn(a[k], xv[k]));
+  if (on[3]) sn = first_term((A)__fmul_rn(a[3], xv[3]));
 #pragma unroll
-  for (int k = 3; k < kHexW; ++k)
+  for (int k = 4; k < kHexW; ++k)
     if (on[k]) sn = add_rn(sn, (A)__fmul_rn(a[k], xv[k]));
   A y = (A)__fmul_rn(S.d[tid], S.x[tid]);
   if (NEI_FIRST) {
@@ -205,11 +207,13 @@ __device__ __forceinline__ A hex_cell_from_stage_sym(const HexStageSym& S, int t
     }
   }
   A so = (A)0, sn = (A)0;
+  if (on[0]) so = first_term((A)__fmul_rn(a[0], xv[0]));
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
+  for (int k = 1; k < 3; ++k)
     if (on[k]) so = add_rn(so, (A)__fmul_rn(a[k], xv[k]));
+  if (on[3]) sn = first_term((A)__fmul_rn(a[3], xv[3]));
 #pragma unroll
-  for (int k = 3; k < kHexW; ++k)
+  for (int k = 4; k < kHexW; ++k)
     if (on[k]) sn = add_rn(sn, (A)__fmul_rn(a[k], xv[k]));
   A y = (A)__fmul_rn(S.d[tid], S.x[tid]);
   y = add_rn(y, so);

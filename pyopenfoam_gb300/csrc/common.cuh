@@ -167,6 +167,17 @@ __device__ __forceinline__ T reduce_partials(const T* partials, int n, T* sh) {
   return block_sum(v, sh);
 }
 
+// 0.0 + p without a floating-point add: p itself, except that -0.0 becomes
+// +0.0.  The first term of a running sum that starts at 0.0 enters this way,
+// which saves one FP64 add per sum (GB300's FP64 rate bounds the bitwise
+// FP64 gathers) and gives the same bits as the addition.
+__device__ __forceinline__ double first_term(double p) {
+  return __double_as_longlong(p) == (long long)0x8000000000000000ULL ? 0.0 : p;
+}
+__device__ __forceinline__ float first_term(float p) {
+  return __float_as_int(p) == (int)0x80000000u ? 0.0f : p;
+}
+
 // Canonical IEEE helpers (one rounding each, never contracted to FMA).
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
