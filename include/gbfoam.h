@@ -247,8 +247,16 @@ typedef struct gbf_solve_params {
   int32_t min_iter;
   int32_t check_every;  /* iterations between host status reads (0 = 32)   */
   int32_t variant;      /* PBiCGStab: 0 = reference omega = (t.z)/(t.t)
-                           (pbicgstab.py:210), 1 = standard (t.s)/(t.t);
-                           ignored by PCG                                 */
+                           (pbicgstab.py:210), 1 = standard (t.s)/(t.t).
+                           FP64 PCG: 0 = automatic (one cooperative launch
+                           for the whole solve up to 2^21 cells, three
+                           kernels per iteration above), 1 = three kernels
+                           per iteration, 2 = one cooperative launch.
+                           Both forms apply the same per-element arithmetic
+                           and monitor rules; their dot products differ in
+                           summation order (block count).  A barrier wait
+                           of the cooperative form that runs out gives
+                           status GBF_DEVICE_TIMEOUT.                      */
 } gbf_solve_params;
 
 typedef struct gbf_solve_result {
@@ -441,6 +449,13 @@ int gbf_xpay_f64(int32_t n, const double* x, double a, const double* y, double* 
  * reference solvers); workspace of gbf_norm2_workspace_bytes().            */
 int gbf_dot_f64(int32_t n, const double* a, const double* b, double* out, void* workspace,
                 void* stream);
+/* FvMatrix.relax (core/fv_matrix.py:192-235), in place: diag = diag / a,
+ * source = source + ((1 - a) * diag) * field_old with one_minus_a = 1 - a
+ * computed by the caller.  True IEEE division (a torch division of a CUDA
+ * tensor by a scalar multiplies by the reciprocal instead, which is not the
+ * reference's CPU result).                                                  */
+int gbf_fv_relax_f64(int32_t n, double a, double one_minus_a, double* diag, double* source,
+                     const double* field_old, void* stream);
 /* DiagonalSolver (solvers/diagonal.py:55-85): x = b / max(|diag|, 1e-30),
  * r = b - diag*x.                                                          */
 int gbf_diagonal_solve_f64(int32_t n, const double* diag, const double* b, double* x, double* r,

@@ -121,6 +121,7 @@ EXPORTED: dict[str, tuple] = {
                                          _c_vp, _P(_c_i32)]),
     "gbf_pack_sym_f64_to_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_amul_sym_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_fv_relax_f64": (ctypes.c_int, [_c_i32, _c_dbl, _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_xpay_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_dbl, _c_vp, _c_vp, _c_vp]),
     "gbf_dot_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_diagonal_solve_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),

@@ -9,6 +9,7 @@ from typing import Any, Protocol
 
 import torch
 
+from .. import _lib
 from .dtype import assert_floating
 from .ldu_matrix import LduMatrix
 
@@ -72,9 +73,17 @@ class FvMatrix(LduMatrix):
         self._field_old = field_old.to(device=self._device, dtype=self._dtype)
         self._relaxation_factor = under_relaxation_factor
         if under_relaxation_factor < 1.0:
-            a = under_relaxation_factor
-            self._diag = (self._diag / a).contiguous()
-            self._source = self._source + ((1.0 - a) * self._diag * self._field_old)
+            a = float(under_relaxation_factor)
+            if self._dtype != torch.float64:
+                self._diag = (self._diag / a).contiguous()
+                self._source = self._source + ((1.0 - a) * self._diag * self._field_old)
+            else:
+                self._diag = self._diag.clone().contiguous()
+                self._source = self._source.clone().contiguous()
+                old = self._field_old.contiguous()
+                _lib.check(_lib.lib().gbf_fv_relax_f64(
+                    self._n_cells, a, 1.0 - a, self._diag.data_ptr(), self._source.data_ptr(),
+                    old.data_ptr(), _lib.stream_ptr(self._device)), "gbf_fv_relax_f64")
             self.invalidate_cache()
 
     def set_reference(self, cell_index: int, value: float = 0.0) -> None:

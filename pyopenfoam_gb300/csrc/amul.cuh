@@ -12,10 +12,21 @@
 
 namespace gbf {
 
+// Load of the multiplied vector: through the read-only path, or (COH) from
+// L2 only -- for persistent kernels in which other blocks rewrite the vector
+// between phases, so that no stale L1 line is read.
+template <bool COH, typename T>
+__device__ __forceinline__ T ldx(const T* p) {
+  if constexpr (COH)
+    return __ldcg(p);
+  else
+    return __ldg(p);
+}
+
 // Sum over `cnt` slots starting at slot k0 of cell c (slot index i0 =
 // base + 32*k0, compressed entry e0 + k0) of coef[slot] * x[col[slot]],
 // skipping padding (col < 0).  Products are rounded in T, sums in A.
-template <typename T, typename A>
+template <typename T, typename A, bool COH = false>
 __device__ __forceinline__ A slot_sum(const gbf_layout& L, const T* __restrict__ coef,
                                       const T* __restrict__ x, int c, int i0, int e0, int cnt) {
   A s = (A)0;
@@ -29,25 +40,25 @@ __device__ __forceinline__ A slot_sum(const gbf_layout& L, const T* __restrict__
 #pragma unroll
     for (int k = 0; k < 4; ++k) a[k] = (k < cnt) ? __ldg(coef + i0 + 32 * k) : (T)0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
+    for (int k = 0; k < 4; ++k) xv[k] = (col[k] >= 0) ? ldx<COH>(x + col[k]) : (T)0;
     if (col[0] >= 0) s = first_term((A)mul_rn(a[0], xv[0]));
 #pragma unroll
     for (int k = 1; k < 4; ++k)
       if (col[k] >= 0) s = add_rn(s, (A)mul_rn(a[k], xv[k]));
   } else {
     const int col0 = slot_column(L, e0, i0, c);
-    if (col0 >= 0) s = first_term((A)mul_rn(__ldg(coef + i0), __ldg(x + col0)));
+    if (col0 >= 0) s = first_term((A)mul_rn(__ldg(coef + i0), ldx<COH>(x + col0)));
 #pragma unroll 4
     for (int k = 1; k < cnt; ++k) {
       const int col = slot_column(L, e0 + k, i0 + 32 * k, c);
-      if (col >= 0) s = add_rn(s, (A)mul_rn(__ldg(coef + i0 + 32 * k), __ldg(x + col)));
+      if (col >= 0) s = add_rn(s, (A)mul_rn(__ldg(coef + i0 + 32 * k), ldx<COH>(x + col)));
     }
   }
   return s;
 }
 
 // (A x)[c] with x[c] already loaded as xc.
-template <typename T, typename A, bool NEI_FIRST>
+template <typename T, typename A, bool NEI_FIRST, bool COH = false>
 __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict__ coef,
                                        const T* __restrict__ diag, const T* __restrict__ x,
                                        int c, T xc) {
@@ -72,7 +83,7 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
         a[4 + k] = (k < cs.wn) ? __ldg(coef + cs.base + 32 * (cs.wo + k)) : (T)0;
       }
 #pragma unroll
-      for (int k = 0; k < 8; ++k) xv[k] = (col[k] >= 0) ? __ldg(x + col[k]) : (T)0;
+      for (int k = 0; k < 8; ++k) xv[k] = (col[k] >= 0) ? ldx<COH>(x + col[k]) : (T)0;
       if (col[0] >= 0) so = first_term((A)mul_rn(a[0], xv[0]));
 #pragma unroll
       for (int k = 1; k < 4; ++k)
@@ -82,8 +93,8 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
       for (int k = 5; k < 8; ++k)
         if (col[k] >= 0) sn = add_rn(sn, (A)mul_rn(a[k], xv[k]));
     } else {
-      so = slot_sum<T, A>(L, coef, x, c, cs.base, cs.e0, cs.wo);
-      sn = slot_sum<T, A>(L, coef, x, c, cs.base + 32 * cs.wo, cs.e0 + cs.wo, cs.wn);
+      so = slot_sum<T, A, COH>(L, coef, x, c, cs.base, cs.e0, cs.wo);
+      sn = slot_sum<T, A, COH>(L, coef, x, c, cs.base + 32 * cs.wo, cs.e0 + cs.wo, cs.wn);
     }
     if (NEI_FIRST) {
       y = add_rn(y, sn);
@@ -103,7 +114,7 @@ __device__ __forceinline__ A cell_amul(const gbf_layout& L, const T* __restrict_
 // 128-bit loads, and no slot needs a width predicate or a slot_col
 // fallback.  Same products and summation order as cell_amul.
 // ---------------------------------------------------------------------------
-template <typename T, typename A, bool NEI_FIRST, int WO, int WN>
+template <typename T, typename A, bool NEI_FIRST, int WO, int WN, bool COH = false>
 __device__ __forceinline__ A cell_amul_fixed(const gbf_layout& L, const T* __restrict__ coef,
                                              const T* __restrict__ diag,
                                              const T* __restrict__ x, int c, T xc) {
@@ -129,7 +140,7 @@ __device__ __forceinline__ A cell_amul_fixed(const gbf_layout& L, const T* __res
 #pragma unroll
   for (int k = 0; k < W; ++k) {
     on[k] = (m[k] >> lane) & 1u;
-    xv[k] = on[k] ? __ldg(x + c + d[k]) : (T)0;
+    xv[k] = on[k] ? ldx<COH>(x + c + d[k]) : (T)0;
   }
   A so = (A)0, sn = (A)0;
   if (WO > 0 && on[0]) so = first_term((A)mul_rn(a[0], xv[0]));
@@ -236,7 +247,7 @@ inline bool layout_sym_ok(const gbf_layout& L) {
   return layout_kind(L) == kLayoutHex33 && L.slot_mirror != nullptr;
 }
 
-template <int KIND, typename T, typename A, bool NEI_FIRST>
+template <int KIND, typename T, typename A, bool NEI_FIRST, bool COH = false>
 __device__ __forceinline__ A cell_amul_k(const gbf_layout& L, const T* __restrict__ coef,
                                          const T* __restrict__ diag, const T* __restrict__ x,
                                          int c, T xc) {
@@ -244,9 +255,9 @@ __device__ __forceinline__ A cell_amul_k(const gbf_layout& L, const T* __restric
     static_assert(!NEI_FIRST, "a symmetric matrix is its own transpose");
     return cell_amul_sym33<A>(L, coef, diag, x, c, xc);
   } else if constexpr (KIND == kLayoutHex33) {
-    return cell_amul_fixed<T, A, NEI_FIRST, 3, 3>(L, coef, diag, x, c, xc);
+    return cell_amul_fixed<T, A, NEI_FIRST, 3, 3, COH>(L, coef, diag, x, c, xc);
   } else {
-    return cell_amul<T, A, NEI_FIRST>(L, coef, diag, x, c, xc);
+    return cell_amul<T, A, NEI_FIRST, COH>(L, coef, diag, x, c, xc);
   }
 }
 

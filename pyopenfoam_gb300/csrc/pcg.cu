@@ -25,10 +25,17 @@
 
 namespace gbf {
 
+// Software grid barrier of the single-launch (cooperative) PCG.
+struct GridBarrier {
+  unsigned int count, gen;
+  int fault, pad;
+};
+
 struct PcgState {
   double rz, alpha, beta, res0, res, pAp;
   int iter, status, n_hist, pad;
   unsigned int ticket[4];
+  GridBarrier bar;
 };
 
 struct PcgVecs {
@@ -172,6 +179,217 @@ __global__ void __launch_bounds__(kBlock) pcg_p_kernel(int n, PcgVecs v) {
     v.p[c] = __dadd_rn(v.z[c], __dmul_rn(beta, v.p[c]));
 }
 
+// ---------------------------------------------------------------------------
+// Single-launch PCG for launch-bound (small and medium) systems.
+//
+// The three phases of an iteration run inside one cooperative launch whose
+// blocks are all resident, separated by a grid barrier; every block reduces
+// the per-block partials itself in the same fixed order, so all blocks hold
+// the same scalars and take the same decisions without a further barrier.
+// Same arithmetic per element and same ResidualMonitor rules as the
+// three-kernel form.  Vectors that other blocks rewrite during the launch
+// (p, and the partials) are read from L2 (__ldcg), never through L1.
+//
+// Every barrier wait is bounded: after kBarrierPolls polls (with a 100 ns
+// sleep each, ~2 s) the block records a fault and returns; blocks that reach
+// a barrier after a fault return at once.  The host turns a fault into
+// GBF_DEVICE_TIMEOUT.
+// ---------------------------------------------------------------------------
+constexpr long long kBarrierPolls = 1LL << 24;
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, unsigned int nblocks) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned int* vgen = &bar->gen;
+    volatile int* vfault = &bar->fault;
+    const unsigned int g = *vgen;
+    __threadfence();
+    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
+      atomicExch(&bar->count, 0u);
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      long long polls = 0;
+      while (*vgen == g) {
+        if (*vfault != 0 || ++polls > kBarrierPolls) {
+          atomicExch(&bar->fault, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    if (*vfault != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <int KIND, bool PREC>
+__global__ void __launch_bounds__(kBlock)
+    pcg_persistent_kernel(gbf_layout L, const double* __restrict__ coef,
+                          const double* __restrict__ diag, const double* __restrict__ pd,
+                          const double* __restrict__ b, double* __restrict__ x, PcgVecs v,
+                          double* hist, gbf_solve_params P) {
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x, n = L.n_cells;
+  const int c0 = blockIdx.x * blockDim.x + threadIdx.x, cs = G * blockDim.x;
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+  PcgState* st = v.st;
+  GridBarrier* bar = &st->bar;
+  double* partA = v.partials;       // p.Ap partials      [G]
+  double* partB = v.partials + G;   // r.r, r.z partials  [2G]
+
+  // r = b - A x, z = M^-1 r, p = z
+  double rr = 0.0, rz = 0.0;
+  for (int c = c0; c < n; c += cs) {
+    const double y = cell_amul_k<KIND, double, double, false>(L, coef, diag, x, c, __ldg(x + c));
+    const double rc = __dsub_rn(__ldg(b + c), y);
+    const double zc = PREC ? __ddiv_rn(rc, __ldg(pd + c)) : rc;
+    v.r[c] = rc;
+    v.z[c] = zc;
+    v.p[c] = zc;
+    rr = fma(rc, rc, rr);
+    rz = fma(rc, zc, rz);
+  }
+  rr = block_sum(rr, sh);
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) {
+    partB[blockIdx.x] = rr;
+    partB[G + blockIdx.x] = rz;
+  }
+  if (!grid_barrier(bar, G)) return;
+  double s0 = reduce_partials(partB, G, sh);
+  double s1 = reduce_partials(partB + G, G, sh);
+  __shared__ double bc[2];
+  if (threadIdx.x == 0) {
+    bc[0] = s0;
+    bc[1] = s1;
+  }
+  __syncthreads();
+  const double res0 = sqrt(bc[0]);
+  double rzv = bc[1], res = res0;
+  int iter = 1, n_hist = 1;
+  int status = monitor_converged(res0, res0, 0, P) ? GBF_CONVERGED
+               : (P.max_iter < 1 ? GBF_MAX_ITER : GBF_RUNNING);
+  if (lead) hist[0] = res0;
+
+  for (int launched = 0; status == GBF_RUNNING && launched < P.max_iter; ++launched) {
+    // Ap = A p, p.Ap
+    double acc = 0.0;
+    for (int c = c0; c < n; c += cs) {
+      const double pc = __ldcg(v.p + c);
+      const double y = cell_amul_k<KIND, double, double, false, true>(L, coef, diag, v.p, c, pc);
+      v.Ap[c] = y;
+      acc = fma(pc, y, acc);
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) partA[blockIdx.x] = acc;
+    if (!grid_barrier(bar, G)) return;
+    s0 = reduce_partials(partA, G, sh);
+    if (threadIdx.x == 0) bc[0] = s0;
+    __syncthreads();
+    const double pAp = bc[0];
+    if (fabs(pAp) < 1e-30) {  // pcg.py:153-156: x returned as is
+      status = GBF_BREAKDOWN;
+      break;
+    }
+    const double alpha = rzv / pAp;
+    // x += alpha p, r -= alpha Ap, z = M^-1 r, r.r, r.z
+    rr = 0.0;
+    rz = 0.0;
+    for (int c = c0; c < n; c += cs) {
+      const double xc = __dadd_rn(x[c], __dmul_rn(alpha, __ldcg(v.p + c)));
+      const double rc = __dsub_rn(v.r[c], __dmul_rn(alpha, v.Ap[c]));
+      const double zc = PREC ? __ddiv_rn(rc, __ldg(pd + c)) : rc;
+      x[c] = xc;
+      v.r[c] = rc;
+      v.z[c] = zc;
+      rr = fma(rc, rc, rr);
+      rz = fma(rc, zc, rz);
+    }
+    rr = block_sum(rr, sh);
+    rz = block_sum(rz, sh);
+    if (threadIdx.x == 0) {
+      partB[blockIdx.x] = rr;
+      partB[G + blockIdx.x] = rz;
+    }
+    if (!grid_barrier(bar, G)) return;
+    s0 = reduce_partials(partB, G, sh);
+    s1 = reduce_partials(partB + G, G, sh);
+    if (threadIdx.x == 0) {
+      bc[0] = s0;
+      bc[1] = s1;
+    }
+    __syncthreads();
+    const int it = iter;
+    res = sqrt(bc[0]);
+    if (lead) hist[it] = res;
+    n_hist = it + 1;
+    if (monitor_converged(res, res0, it, P)) {
+      status = GBF_CONVERGED;
+      break;
+    }
+    const double beta = bc[1] / rzv;
+    rzv = bc[1];
+    iter = it + 1;
+    if (it >= P.max_iter) {
+      status = GBF_MAX_ITER;
+      break;
+    }
+    // p = z + beta p
+    for (int c = c0; c < n; c += cs) v.p[c] = __dadd_rn(v.z[c], __dmul_rn(beta, v.p[c]));
+    if (!grid_barrier(bar, G)) return;
+  }
+  if (lead) {
+    st->status = status;
+    st->res = res;
+    st->res0 = res0;
+    st->n_hist = n_hist;
+    st->iter = iter;
+    st->rz = rzv;
+  }
+}
+
+// Blocks of the single-launch PCG that can be resident at once (0 if the
+// device cannot launch it cooperatively).
+template <int KIND, bool PREC>
+static int persistent_grid(int n) {
+  int dev = 0, coop = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!coop || sms <= 0) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_persistent_kernel<KIND, PREC>,
+                                                    kBlock, 0) != cudaSuccess || per_sm <= 0)
+    return 0;
+  long long g = (long long)per_sm * sms;
+  const long long need = (n + kBlock - 1) / kBlock;
+  if (g > need) g = need;
+  if (g > kMaxGrid / 2) g = kMaxGrid / 2;  // partA + partB fit the partials buffer
+  return g < 1 ? 1 : (int)g;
+}
+
+template <int KIND, bool PREC>
+static cudaError_t launch_persistent(int grid, const gbf_layout* L, const double* coef,
+                                     const double* diag, const double* pd, const double* b,
+                                     double* x, PcgVecs v, double* hist,
+                                     const gbf_solve_params* P, cudaStream_t s) {
+  gbf_layout Lc = *L;
+  gbf_solve_params Pc = *P;
+  void* args[] = {&Lc, (void*)&coef, (void*)&diag, (void*)&pd, (void*)&b, &x, &v, &hist, &Pc};
+  return cudaLaunchCooperativeKernel((const void*)pcg_persistent_kernel<KIND, PREC>,
+                                     dim3(grid), dim3(kBlock), args, 0, s);
+}
+
+// Systems up to this many cells run the single-launch form under
+// variant 0 (above it the per-iteration launch cost is negligible).
+constexpr int kPersistentMaxCells = 1 << 21;
+
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace gbf
@@ -216,10 +434,45 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
   v.partials = reinterpret_cast<double*>(w + 4 * vb);
   v.st = reinterpret_cast<PcgState*>(w + 4 * vb + align256(sizeof(double) * 2 * kMaxGrid));
 
+  GBF_REQUIRE(P->variant >= 0 && P->variant <= 2, "pcg: variant must be 0, 1 or 2");
+  GBF_CHECK_CUDA(cudaMemsetAsync(v.st, 0, sizeof(PcgState), s));
+
+  // single launch (variant 2, or variant 0 on a launch-bound system)
+  if (P->variant == 2 || (P->variant == 0 && n <= kPersistentMaxCells)) {
+    const bool hex = layout_kind(*L) == kLayoutHex33;
+    const int Gp = hex ? (pd ? persistent_grid<kLayoutHex33, true>(n)
+                             : persistent_grid<kLayoutHex33, false>(n))
+                       : (pd ? persistent_grid<kLayoutGeneric, true>(n)
+                             : persistent_grid<kLayoutGeneric, false>(n));
+    if (Gp > 0) {
+      cudaError_t e;
+      if (hex)
+        e = pd ? launch_persistent<kLayoutHex33, true>(Gp, L, coef, diag, pd, b, x, v, hist, P, s)
+               : launch_persistent<kLayoutHex33, false>(Gp, L, coef, diag, pd, b, x, v, hist, P,
+                                                        s);
+      else
+        e = pd ? launch_persistent<kLayoutGeneric, true>(Gp, L, coef, diag, pd, b, x, v, hist, P,
+                                                         s)
+               : launch_persistent<kLayoutGeneric, false>(Gp, L, coef, diag, pd, b, x, v, hist,
+                                                          P, s);
+      GBF_CHECK_CUDA(e);
+      PcgState hs;
+      GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+      GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+      R->iterations = hs.n_hist;
+      R->status = hs.bar.fault ? GBF_DEVICE_TIMEOUT
+                               : (hs.status == GBF_RUNNING ? GBF_MAX_ITER : hs.status);
+      R->final_residual = hs.res;
+      R->initial_residual = hs.res0;
+      R->launches = 1;
+      return GBF_OK;
+    }
+    GBF_REQUIRE(P->variant != 2, "pcg: the device cannot run the single-launch form");
+  }
+
   int G = reduction_grid();
   const int need = (n + kBlock - 1) / kBlock;
   if (G > need) G = need;
-  GBF_CHECK_CUDA(cudaMemsetAsync(v.st, 0, sizeof(PcgState), s));
   if (pd)
     pcg_init_kernel<true><<<G, kBlock, 0, s>>>(*L, coef, diag, pd, b, x, v, hist, *P);
   else

@@ -109,6 +109,18 @@ __global__ void __launch_bounds__(kBlock)
   r[c] = __dsub_rn(bc, __dmul_rn(dc, xc));
 }
 
+// FvMatrix.relax: diag /= a; source += ((1 - a) * diag) * field_old, with
+// one_minus_a = 1 - a computed by the caller in double.
+__global__ void __launch_bounds__(kBlock)
+    fv_relax_kernel(int n, double a, double one_minus_a, double* __restrict__ diag,
+                    double* __restrict__ source, const double* __restrict__ old) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double d = __ddiv_rn(diag[c], a);
+  diag[c] = d;
+  source[c] = __dadd_rn(source[c], __dmul_rn(__dmul_rn(one_minus_a, d), __ldg(old + c)));
+}
+
 constexpr int kNormBlocks = 1024;
 
 __global__ void __launch_bounds__(kBlock)
@@ -256,6 +268,17 @@ extern "C" int gbf_diagonal_solve_f64(int32_t n, const double* diag, const doubl
   GBF_REQUIRE(diag && b && x && r, "diagonal_solve: NULL pointer");
   diagonal_solve_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(n, diag, b,
                                                                                    x, r);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_fv_relax_f64(int32_t n, double a, double one_minus_a, double* diag,
+                                double* source, const double* field_old, void* stream) {
+  GBF_REQUIRE(n >= 0, "fv_relax: negative n");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(diag && source && field_old, "fv_relax: NULL pointer");
+  fv_relax_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, as_stream(stream)>>>(
+      n, a, one_minus_a, diag, source, field_old);
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }

@@ -48,6 +48,9 @@ def run_solver(fn_name: str, ws_name: str, matrix: LduMatrix, source: torch.Tens
                             ctypes.byref(R), ws.data_ptr(), ws.numel(), _lib.stream_ptr(dev)),
         fn_name,
     )
+    if R.status == _lib.GBF_DEVICE_TIMEOUT:
+        raise RuntimeError(f"{fn_name}: a bounded wait inside the solver kernel ran out; "
+                           "the result is invalid")
     if R.iterations > 0 and n > 0:
         monitor.record(hist[: R.iterations].tolist())
     else:

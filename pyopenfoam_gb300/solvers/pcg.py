@@ -25,16 +25,24 @@ class PCGSolver(LinearSolverBase):
     """PCG for symmetric positive-definite LDU matrices.
 
     ``preconditioner`` is ``"DIC"`` (default), ``"DILU"`` or ``"none"``.
-    ``check_every`` (keyword only, GPU knob) is the number of iterations
-    between host reads of the device status block."""
+    GPU knobs (keyword only): ``check_every`` is the number of iterations
+    between host reads of the device status block; ``launch`` is
+    ``"auto"`` (default: the whole solve in one cooperative launch with grid
+    barriers up to 2^21 cells, where per-iteration launches would dominate,
+    three kernels per iteration above), ``"kernels"`` or ``"single"``."""
+
+    _LAUNCH = {"auto": 0, "kernels": 1, "single": 2}
 
     def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 1000,
                  min_iter: int = 0, verbose: bool = False, preconditioner: str = "DIC", *,
-                 check_every: int = 32) -> None:
+                 check_every: int = 32, launch: str = "auto") -> None:
         super().__init__(tolerance=tolerance, rel_tol=rel_tol, max_iter=max_iter,
                          min_iter=min_iter, verbose=verbose)
         self._precond_type = preconditioner.upper()
         self._check_every = int(check_every)
+        if launch not in self._LAUNCH:
+            raise ValueError(f"launch must be one of {sorted(self._LAUNCH)}, got {launch!r}")
+        self._launch = launch
 
     def _make_preconditioner(self, matrix: LduMatrix) -> Preconditioner | None:
         if self._precond_type == "DIC":
@@ -51,6 +59,8 @@ class PCGSolver(LinearSolverBase):
                monitor: ResidualMonitor, max_iter: int) -> tuple[torch.Tensor, ConvergenceInfo]:
         precond = self._make_preconditioner(matrix)
         pd = None if precond is None else precond.precond_diag
-        x, info, _ = run_solver("gbf_pcg_solve_f64", "gbf_pcg_workspace_bytes", matrix, source,
-                                x0, monitor, max_iter, pd, max_iter + 1, self._check_every)
+        x, info, R = run_solver("gbf_pcg_solve_f64", "gbf_pcg_workspace_bytes", matrix, source,
+                                x0, monitor, max_iter, pd, max_iter + 1, self._check_every,
+                                variant=self._LAUNCH[self._launch])
+        self.last_result = R
         return x, info

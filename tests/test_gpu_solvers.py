@@ -215,3 +215,39 @@ def test_pbicgstab_first_iterations_on_jittered_mesh():
     assert it == o.iterations == 5
     assert relerr(x.cpu().numpy(), o.x) < 1e-8
     assert relerr(s.last_info.residual_history, o.history) < 1e-9
+
+
+@pytest.mark.parametrize("N,prec", [(32, "DIC"), (20, "none"), (7, "DILU")])
+def test_pcg_single_launch_and_kernel_forms_agree(N, prec):
+    """The single cooperative launch (grid barriers) and the three-kernel
+    form run the same iteration: same iteration count and status, x and the
+    residual history within 1e-12 (their dot products sum in different
+    block orders), both within 1e-8 of the oracle."""
+    from pyopenfoam_gb300.mesh.poisson import hex_poisson
+
+    d = hex_poisson(N, seed=7)
+    m = LduMatrix(d["n"], torch.as_tensor(d["owner"]), torch.as_tensor(d["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(d[k]) for k in ("diag", "lower", "upper"))
+    b = torch.as_tensor(d["b"])
+    out = {}
+    for launch in ("single", "kernels"):
+        s = PCGSolver(tolerance=0.0, rel_tol=1e-9, max_iter=2000, preconditioner=prec,
+                      launch=launch)
+        x, it, res = s(m, b, torch.zeros_like(b))
+        assert s.last_result.launches == (1 if launch == "single" else s.last_result.launches)
+        out[launch] = (x.cpu().numpy(), it, s.last_info.converged,
+                       np.array(s.last_info.residual_history))
+    (xs, its, cs, hs), (xk, itk, ck, hk) = out["single"], out["kernels"]
+    assert its == itk and cs and ck
+    assert np.abs(xs - xk).max() <= 1e-12 * np.abs(xk).max()
+    assert np.abs(hs - hk).max() <= 1e-12 * hk[0]
+    pd = (None if prec == "none" else
+          (O.dic_build if prec == "DIC" else lambda o, n_, dg, up: O.dilu_build(
+              o, n_, dg, d["lower"], up))(d["owner"], d["neighbour"], d["diag"], d["upper"]))
+    o = O.pcg(d["owner"], d["neighbour"], d["diag"], d["lower"], d["upper"], d["b"],
+              np.zeros(d["n"]), pd, 0.0, 1e-9, 2000)
+    assert o.iterations == its
+    assert np.abs(xs - o.x).max() <= 1e-8 * np.abs(o.x).max()
+    with pytest.raises(ValueError):
+        PCGSolver(launch="graph")
