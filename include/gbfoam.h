@@ -88,6 +88,13 @@ int gbf_stream_fault(int32_t* fault);
 int gbf_version(void);
 /* Number of SMs of the current device (grid sizing of the reductions).     */
 int gbf_device_sm_count(int32_t* n_sm);
+/* Self-test of the bounded device-side waits (no reference counterpart):
+ * makes a grid-barrier wait (one participant never arrives) and an mbarrier
+ * wait (nothing ever completes it) run out after short poll limits, on the
+ * current device.  timed_out_h[0] = 1 if the barrier wait gave up,
+ * [1] = 1 if the mbarrier wait gave up, [2] = the barrier's fault word.
+ * Allocates and frees a few bytes of device memory; synchronises.          */
+int gbf_selftest_bounded_waits(int32_t* timed_out_h);
 /* Kernel timing probes (no reference counterpart; used by the benchmark to
  * time the dominant kernel inside a solve).  While enabled, the solvers
  * bracket the launches of their Amul kernels with CUDA events on the

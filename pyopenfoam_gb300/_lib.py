@@ -110,6 +110,7 @@ EXPORTED: dict[str, tuple] = {
     "gbf_last_error": (ctypes.c_char_p, []),
     "gbf_version": (ctypes.c_int, []),
     "gbf_device_sm_count": (ctypes.c_int, [_P(_c_i32)]),
+    "gbf_selftest_bounded_waits": (ctypes.c_int, [_c_vp]),
     "gbf_timing_enable": (ctypes.c_int, [_c_i32, _c_i32]),
     "gbf_timing_read": (ctypes.c_int, [_c_i32, _P(_c_i32), _P(_c_dbl)]),
     "gbf_layout_plan": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _P(_c_i32),

@@ -34,6 +34,7 @@ SOURCES = [
     "pressure.cu",
     "smooth.cu",
     "gamg.cu",
+    "selftest.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -420,6 +420,7 @@ extern "C" int gbf_batched_mixed_pcg_solve(const gbf_layout* L, const gbf_batch*
                                            const gbf_solve_params* P, int32_t block_size,
                                            int32_t use_graph, gbf_solve_result* R, void* ws,
                                            size_t ws_bytes, void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_batched_mixed_pcg_solve");
   int rc = check_layout(L);
   if (rc) return rc;
   GBF_REQUIRE(B && P && R, "batched_pcg: NULL batch/params/result");

@@ -7,9 +7,21 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "gbfoam.h"
 
 namespace gbf {
+
+// NVTX range for the duration of a scope (shows each solve and
+// factorisation as one named range in Nsight timelines; free without a
+// profiler attached).
+struct NvtxScope {
+  explicit NvtxScope(const char* name) { nvtxRangePushA(name); }
+  ~NvtxScope() { nvtxRangePop(); }
+  NvtxScope(const NvtxScope&) = delete;
+  NvtxScope& operator=(const NvtxScope&) = delete;
+};
 
 // Per-thread error message (gbf_last_error()).
 void set_error(const char* fmt, ...);

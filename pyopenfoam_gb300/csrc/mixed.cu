@@ -400,6 +400,7 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
                                    double* hist, int32_t hist_cap, const gbf_solve_params* P,
                                    gbf_solve_result* R, void* ws, size_t ws_bytes,
                                    void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_mixed_pcg_solve");
   int rc = check_layout(L);
   if (rc) return rc;
   GBF_REQUIRE(P && R, "mixed_pcg: NULL params/result");

@@ -276,6 +276,7 @@ extern "C" int gbf_pbicgstab_solve_f64(const gbf_layout* L, const double* coef,
                                        double* x, double* hist, const gbf_solve_params* P,
                                        gbf_solve_result* R, void* ws, size_t ws_bytes,
                                        void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_pbicgstab_solve_f64");
   int rc = check_layout(L);
   if (rc) return rc;
   GBF_REQUIRE(P && R, "pbicgstab: NULL params/result");

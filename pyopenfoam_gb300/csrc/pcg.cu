@@ -22,14 +22,9 @@
 #include <string.h>
 
 #include "amul.cuh"
+#include "barrier.cuh"
 
 namespace gbf {
-
-// Software grid barrier of the single-launch (cooperative) PCG.
-struct GridBarrier {
-  unsigned int count, gen;
-  int fault, pad;
-};
 
 struct PcgState {
   double rz, alpha, beta, res0, res, pAp;
@@ -195,40 +190,6 @@ __global__ void __launch_bounds__(kBlock) pcg_p_kernel(int n, PcgVecs v) {
 // a barrier after a fault return at once.  The host turns a fault into
 // GBF_DEVICE_TIMEOUT.
 // ---------------------------------------------------------------------------
-constexpr long long kBarrierPolls = 1LL << 24;
-
-__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, unsigned int nblocks) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    volatile unsigned int* vgen = &bar->gen;
-    volatile int* vfault = &bar->fault;
-    const unsigned int g = *vgen;
-    __threadfence();
-    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
-      atomicExch(&bar->count, 0u);
-      __threadfence();
-      atomicAdd(&bar->gen, 1u);
-    } else {
-      long long polls = 0;
-      while (*vgen == g) {
-        if (*vfault != 0 || ++polls > kBarrierPolls) {
-          atomicExch(&bar->fault, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(100);
-      }
-    }
-    __threadfence();
-    if (*vfault != 0) ok = 0;
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
 template <int KIND, bool PREC>
 __global__ void __launch_bounds__(kBlock)
     pcg_persistent_kernel(gbf_layout L, const double* __restrict__ coef,
@@ -406,6 +367,7 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
                                  const double* pd, const double* b, double* x, double* hist,
                                  const gbf_solve_params* P, gbf_solve_result* R, void* ws,
                                  size_t ws_bytes, void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_pcg_solve_f64");
   int rc = check_layout(L);
   if (rc) return rc;
   GBF_REQUIRE(P && R, "pcg: NULL params/result");
@@ -579,6 +541,7 @@ extern "C" int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* coef
                                          const double* diag, const double* pd, const double* b,
                                          double* x, double* hist, const gbf_solve_params* P,
                                          gbf_solve_result* R, void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_pcg_solve_f64_noalloc");
   int rc = check_layout(L);
   if (rc) return rc;
   GBF_REQUIRE(P && R, "pcg_noalloc: NULL params/result");

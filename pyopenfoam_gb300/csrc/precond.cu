@@ -81,6 +81,7 @@ extern "C" int gbf_dic_build_f64(const gbf_layout* L, const double* coef, const 
                                  const int32_t* level_ptr, const int32_t* level_cells,
                                  int32_t n_levels, int32_t max_level_size, double* d_out,
                                  void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_dic_build_f64");
   int rc = check_layout(L);
   if (rc) return rc;
   const int n = L->n_cells;
@@ -104,6 +105,7 @@ extern "C" int gbf_dilu_build_f64(const gbf_layout* L, const double* lower, cons
                                   const double* diag, const int32_t* level_ptr,
                                   const int32_t* level_faces, int32_t n_levels,
                                   int32_t max_level_size, double* d_out, void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_dilu_build_f64");
   int rc = check_layout(L);
   if (rc) return rc;
   const int n = L->n_cells;

@@ -173,6 +173,7 @@ extern "C" int gbf_gauss_seidel_f64(const gbf_layout* L, const double* coef, con
                                     const int32_t* level_cells, const int32_t* level_ptr_h,
                                     int32_t n_levels, double omega, int32_t relax, double* x,
                                     void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_gauss_seidel_f64");
   int rc = check_layout(L);
   if (rc) return rc;
   if (L->n_cells == 0) return GBF_OK;

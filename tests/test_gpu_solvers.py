@@ -251,3 +251,24 @@ def test_pcg_single_launch_and_kernel_forms_agree(N, prec):
     assert np.abs(xs - o.x).max() <= 1e-8 * np.abs(o.x).max()
     with pytest.raises(ValueError):
         PCGSolver(launch="graph")
+
+
+def test_bounded_waits_give_up_instead_of_hanging():
+    """Failure detection without a GPU fault: a grid-barrier wait whose
+    partner block never arrives and an mbarrier wait that nothing completes
+    both run out after their poll limits and report it; the context stays
+    usable (a solve afterwards still works)."""
+    import ctypes
+
+    from pyopenfoam_gb300 import _lib
+
+    out = (ctypes.c_int32 * 3)()
+    _lib.check(_lib.lib().gbf_selftest_bounded_waits(out))
+    assert list(out) == [1, 1, 1]
+    c = c1_poisson(8)
+    m = LduMatrix(c["n"], torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(c[k]) for k in ("diag", "lower", "upper"))
+    x, it, res = PCGSolver(tolerance=0.0, rel_tol=1e-8, launch="single")(
+        m, torch.as_tensor(c["b"]), torch.zeros(c["n"], dtype=torch.float64))
+    assert it > 1 and torch.isfinite(x).all()
