@@ -272,3 +272,38 @@ def test_bounded_waits_give_up_instead_of_hanging():
     x, it, res = PCGSolver(tolerance=0.0, rel_tol=1e-8, launch="single")(
         m, torch.as_tensor(c["b"]), torch.zeros(c["n"], dtype=torch.float64))
     assert it > 1 and torch.isfinite(x).all()
+
+
+@pytest.mark.parametrize("launch", ["single", "kernels"])
+def test_breakdown_and_nan_follow_the_reference(launch):
+    """Failure modes of the reference solvers, reproduced (no exception, no
+    hang): a zero matrix breaks down at the first p.Ap (|pAp| < 1e-30,
+    pcg.py:153-156) and returns x0 unconverged after one check; a NaN in the
+    right-hand side makes every comparison false, so the solve runs to
+    max_iter and returns unconverged -- the same outcome as the oracle."""
+    c = c1_poisson(6)
+    n = c["n"]
+    m = LduMatrix(n, torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    # zero matrix: breakdown
+    x, it, res = PCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=50, launch=launch)(
+        m, torch.as_tensor(c["b"]), torch.zeros(n, dtype=torch.float64))
+    zeros = np.zeros(m.n_internal_faces)
+    pd = O.dic_build(c["owner"], c["neighbour"], np.zeros(n), zeros)
+    o = O.pcg(c["owner"], c["neighbour"], np.zeros(n), zeros, zeros, c["b"], np.zeros(n), pd,
+              0.0, 1e-8, 50)
+    assert it == o.iterations == 1 and not o.converged
+    assert torch.count_nonzero(x) == 0
+    # NaN right-hand side: runs to max_iter, unconverged, NaN solution
+    m.diag, m.lower, m.upper = (torch.as_tensor(c[k]) for k in ("diag", "lower", "upper"))
+    b = torch.as_tensor(c["b"]).clone()
+    b[3] = float("nan")
+    s = PCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=7, launch=launch)
+    x, it, res = s(m, b, torch.zeros(n, dtype=torch.float64))
+    bn = c["b"].copy()
+    bn[3] = np.nan
+    o = O.pcg(c["owner"], c["neighbour"], c["diag"], c["lower"], c["upper"], bn, np.zeros(n),
+              O.dic_build(c["owner"], c["neighbour"], c["diag"], c["upper"]), 0.0, 1e-8, 7)
+    assert not s.last_info.converged and not o.converged
+    assert it == o.iterations
+    assert np.isnan(res) and not torch.isfinite(x).all()
