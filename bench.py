@@ -72,10 +72,11 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
-    p.add_argument("--workload", choices=["c3", "c1", "c2", "c4", "c5"], default="c3",
+    p.add_argument("--workload", choices=["c3", "c1", "c2", "c4", "c5", "next"], default="c3",
                    help="c3 (default, the headline): 256^3 mixed vs FP64 PCG; c1: 32^3 "
                         "PCG+DIC to 1e-6; c2: 128^3 jittered convection-diffusion with "
-                        "PBiCGStab+DILU; c5: adjoint gradient of 20 implicit steps at 96^3")
+                        "PBiCGStab+DILU; c5: adjoint gradient of 20 implicit steps at 96^3; "
+                        "next: geometry, correctors, GAMG and smoothers")
     p.add_argument("--fd-faces", type=int, default=32, help="c5: faces checked by central "
                                                             "differences")
     return p.parse_args()
@@ -726,6 +727,110 @@ def run_c5(args, rank, world, local):
                "fd_median_rel_err": statistics.median(errs), "fd_seconds": t_fd})
 
 
+def _event_time(fn, reps: int = 5, warmup: int = 2) -> float:
+    """Mean seconds of fn() over `reps` calls, CUDA events on the current
+    stream after `warmup` calls."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def run_next(args, rank, world, local):
+    """The rows either side of the solve on one mesh: GPU FvMesh geometry
+    of a jittered N^3 polyMesh (default 128^3) against the vectorised numpy
+    restatement of the same formulas; the pressure correctors and Rhie-Chow
+    fluxes on that mesh; GAMG and SmoothSolver on an N/2 cube Poisson
+    system.  Times are CUDA-event means; bytes are the arrays each kernel
+    reads and writes once (gathers of neighbour values counted once)."""
+    from pyopenfoam_gb300 import LduMatrix
+    from pyopenfoam_gb300.mesh import FvMesh, HexMesh
+    from pyopenfoam_gb300.mesh.poisson import hex_poisson
+    from pyopenfoam_gb300.solvers import GAMGSolver, SmoothSolver, rhie_chow
+    from pyopenfoam_gb300.solvers.pressure_equation import correct_face_flux, correct_velocity
+
+    dev = torch.device("cuda", local)
+    N = 128 if args.n == 256 else args.n
+    h = HexMesh(N, jitter=0.2, seed=1, geometry=False)
+    d = h.polymesh()
+    nf, ni, n = d["face_ptr"].shape[0] - 1, d["neighbour"].shape[0], h.n_cells
+    out = {"n_cells": n, "n_faces": nf, "n_internal_faces": ni}
+    m = FvMesh(d["points"], (d["face_ptr"], d["face_pts"]), d["owner"], d["neighbour"],
+               d["boundary"], device=dev)
+    m.compute_geometry()  # warm (addressing upload, module load)
+
+    def geo():
+        m._geo.clear()
+        m.compute_geometry()
+
+    t_geo = _event_time(geo, reps=3, warmup=1)
+    geo_bytes = nf * (8 + 16 + 48) + d["points"].shape[0] * 24 + n * (24 + 32) + nf * 16
+    t0 = time.perf_counter()
+    HexMesh(N, jitter=0.2, seed=1)  # numpy restatement of the geometry formulas
+    t_np = time.perf_counter() - t0
+    out["geometry"] = {"gpu_s": t_geo, "cpu_numpy_s": t_np, "speedup": t_np / t_geo,
+                       "bytes": geo_bytes, "GBs": geo_bytes / t_geo / 1e9}
+    rng = np.random.default_rng(5)
+    HbyA = torch.as_tensor(rng.normal(size=(n, 3))).to(dev)
+    p = torch.as_tensor(rng.uniform(-1, 1, n)).to(dev)
+    A = torch.as_tensor(rng.uniform(0.5, 2.0, n)).to(dev)
+    phi = torch.as_tensor(rng.normal(size=nf)).to(dev)
+    w = m.face_weights
+    t_cv = _event_time(lambda: correct_velocity(HbyA, HbyA, p, A, m))
+    t_cf = _event_time(lambda: correct_face_flux(phi, p, A, m, face_weights=w))
+    own, nei, S, dl, V = m.owner, m.neighbour, m.face_areas, m.delta_coefficients, m.cell_volumes
+    t_rc = _event_time(lambda: rhie_chow.compute_face_flux(HbyA, p, A, S, dl, own, nei, ni, V, w))
+    cv_bytes = n * (24 + 8 + 8 + 8 + 24) + 2 * ni * (24 + 8) + (nf - ni) * 24
+    ff_bytes = nf * (8 + 24 + 8 + 8 + 8) + n * (8 + 8)
+    rc_bytes = nf * (8 + 24 + 8 + 8 + 8) + n * (24 + 8 + 8)
+    out["correct_velocity"] = {"s": t_cv, "bytes": cv_bytes, "GBs": cv_bytes / t_cv / 1e9}
+    out["correct_face_flux"] = {"s": t_cf, "bytes": ff_bytes, "GBs": ff_bytes / t_cf / 1e9}
+    out["rhie_chow_face_flux"] = {"s": t_rc, "bytes": rc_bytes, "GBs": rc_bytes / t_rc / 1e9}
+
+    Nm = max(N // 2, 8)
+    sd = hex_poisson(Nm, seed=2)
+    mm = LduMatrix(sd["n"], torch.as_tensor(sd["owner"]), torch.as_tensor(sd["neighbour"]),
+                   device=dev)
+    mm.diag, mm.lower, mm.upper = (torch.as_tensor(sd[k]) for k in ("diag", "lower", "upper"))
+    b = torch.as_tensor(sd["b"]).to(dev)
+    g = GAMGSolver(tolerance=0.0, rel_tol=1e-3, max_iter=200)
+    t0 = time.perf_counter()
+    g(mm, b, torch.zeros_like(b))
+    torch.cuda.synchronize()
+    t_first = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    x, it, res = g(mm, b, torch.zeros_like(b))
+    torch.cuda.synchronize()
+    t_g = time.perf_counter() - t0
+    out["gamg"] = {"n_cells": sd["n"], "levels": [lv.n_cells for lv in g.last_levels],
+                   "v_cycles": it, "converged": g.last_info.converged, "solve_s": t_g,
+                   "s_per_v_cycle": t_g / max(it, 1), "first_solve_incl_hierarchy_s": t_first}
+    sm = SmoothSolver(tolerance=0.0, rel_tol=0.0, max_iter=5, smoother="GaussSeidel",
+                      n_sweeps=2)
+    sm(mm, b, torch.zeros_like(b))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sm(mm, b, torch.zeros_like(b))
+    torch.cuda.synchronize()
+    t_s = time.perf_counter() - t0
+    out["smooth_gauss_seidel"] = {"n_cells": sd["n"], "sweeps": 10,
+                                  "s_per_sweep_incl_checks": t_s / 10}
+    if rank == 0:
+        _line(args, world, f"rows next to the solve: GPU geometry, correctors, GAMG, smoothers "
+              f"({N}^3 mesh)", t_geo, "s", False,
+              {"workload": f"jittered {N}^3 hex polyMesh (geometry, correctors); {Nm}^3 Poisson "
+                           "(GAMG, SmoothSolver)", "n_cells": n},
+              out, cpu_baseline={"value": t_np, "unit": "s", "cores": 1, "kind": "port",
+                                 "sample": "numpy restatement of the geometry formulas, same "
+                                           "mesh (the reference's Python loops take hours)"})
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup()
@@ -739,6 +844,8 @@ def main():
         run_c4(args, rank, world, local)
     elif args.workload == "c5":
         run_c5(args, rank, world, local)
+    elif args.workload == "next":
+        run_next(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

@@ -476,19 +476,24 @@ int gbf_diagonal_solve_f64(int32_t n, const double* diag, const double* b, doubl
 /* rhie_chow.py:56-78 compute_HbyA: HbyA = H / max(|A_p|, 1e-30).          */
 int gbf_hbya_f64(int32_t n_cells, const double* H, const double* A_p, double* HbyA,
                  void* stream);
+/* inv[c] = 1 / max(|A_p[c]|, 1e-30): the per-cell inverse diagonal that
+ * the Rhie-Chow and face-flux corrections interpolate (rhie_chow.py:182-183,
+ * pressure_equation.py:303-304).                                           */
+int gbf_inv_abs_clamped_f64(int32_t n, const double* A_p, double* inv, void* stream);
 /* rhie_chow.py:81-143 compute_face_flux_HbyA (p == NULL) and :206-250
  * compute_face_flux (p != NULL: plus the Rhie-Chow term of
- * gbf_rhie_chow_f64).                                                      */
+ * gbf_rhie_chow_f64; inv_A_p from gbf_inv_abs_clamped_f64).                */
 int gbf_face_flux_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
                       const int32_t* neighbour, const double* HbyA, const double* face_areas,
-                      const double* weights, const double* p, const double* A_p,
+                      const double* weights, const double* p, const double* inv_A_p,
                       const double* delta, double* phi, void* stream);
 /* rhie_chow.py:146-203 rhie_chow_correction (phi_in == NULL: out = the
  * correction (1/A_p)_f (p_P - p_N) |S_f| delta_f, 0 on boundary faces) and
  * pressure_equation.py:269-332 correct_face_flux (phi_in != NULL: out =
- * phi_in + correction on internal faces, phi_in on boundary faces).       */
+ * phi_in + correction on internal faces, phi_in on boundary faces);
+ * inv_A_p from gbf_inv_abs_clamped_f64.                                    */
 int gbf_rhie_chow_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
-                      const int32_t* neighbour, const double* p, const double* A_p,
+                      const int32_t* neighbour, const double* p, const double* inv_A_p,
                       const double* face_areas, const double* delta, const double* weights,
                       const double* phi_in, double* out, void* stream);
 /* pressure_equation.py:187-266 correct_velocity: U = HbyA - alpha/|A_p|

@@ -143,6 +143,7 @@ EXPORTED: dict[str, tuple] = {
     "gbf_norm2_workspace_bytes": (_c_size, []),
     "gbf_norm2_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_hbya_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_inv_abs_clamped_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp]),
     "gbf_face_flux_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                          _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_rhie_chow_f64": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,

@@ -44,17 +44,25 @@ __global__ void __launch_bounds__(kBlock)
   for (int k = 0; k < 3; ++k) out[3 * (size_t)c + k] = __ddiv_rn(__ldg(H + 3 * (size_t)c + k), d);
 }
 
-// (1/A_p)_f (p_P - p_N) |S_f| delta_f of internal face f.
+__global__ void __launch_bounds__(kBlock)
+    inv_abs_kernel(int n, const double* __restrict__ A, double* __restrict__ inv) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) inv[c] = inv_abs_clamped(__ldg(A + c));
+}
+
+// (1/A_p)_f (p_P - p_N) |S_f| delta_f of internal face f; ia = the per-cell
+// 1 / max(|A_p|, 1e-30) (one division per cell, as the reference computes
+// it before interpolating).
 __device__ __forceinline__ double rc_term(int f, const int32_t* __restrict__ own,
                                           const int32_t* __restrict__ nei,
                                           const double* __restrict__ p,
-                                          const double* __restrict__ A,
+                                          const double* __restrict__ inv_A,
                                           const double* __restrict__ areas,
                                           const double* __restrict__ delta,
                                           const double* __restrict__ w) {
   const int P = __ldg(own + f), N = __ldg(nei + f);
   const double wf = w ? __ldg(w + f) : 0.5;
-  const double ia = lerp_w(wf, inv_abs_clamped(__ldg(A + P)), inv_abs_clamped(__ldg(A + N)));
+  const double ia = lerp_w(wf, __ldg(inv_A + P), __ldg(inv_A + N));
   const double dp = __dsub_rn(__ldg(p + P), __ldg(p + N));
   return __dmul_rn(__dmul_rn(__dmul_rn(ia, dp), fma_norm3(areas + 3 * (size_t)f)),
                    __ldg(delta + f));
@@ -189,36 +197,46 @@ extern "C" int gbf_hbya_f64(int32_t n_cells, const double* H, const double* A_p,
   return GBF_OK;
 }
 
+extern "C" int gbf_inv_abs_clamped_f64(int32_t n, const double* A, double* inv, void* stream) {
+  GBF_REQUIRE(n >= 0, "inv_abs_clamped: negative n");
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(A && inv, "inv_abs_clamped: NULL pointer");
+  inv_abs_kernel<<<grid_of(n), kBlock, 0, as_stream(stream)>>>(n, A, inv);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
 extern "C" int gbf_face_flux_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
                                  const int32_t* neighbour, const double* HbyA,
                                  const double* face_areas, const double* weights, const double* p,
-                                 const double* A_p, const double* delta, double* phi,
+                                 const double* inv_A_p, const double* delta, double* phi,
                                  void* stream) {
   GBF_REQUIRE(n_faces >= 0 && n_internal >= 0 && n_internal <= n_faces,
               "face_flux: bad face counts");
   if (n_faces == 0) return GBF_OK;
   GBF_REQUIRE(owner && HbyA && face_areas && phi && (n_internal == 0 || neighbour) &&
-                  (!p || (A_p && delta)),
+                  (!p || (inv_A_p && delta)),
               "face_flux: NULL pointer");
   face_flux_kernel<<<grid_of(n_faces), kBlock, 0, as_stream(stream)>>>(
-      n_faces, n_internal, owner, neighbour, HbyA, face_areas, weights, p, A_p, delta, phi);
+      n_faces, n_internal, owner, neighbour, HbyA, face_areas, weights, p, inv_A_p, delta, phi);
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }
 
 extern "C" int gbf_rhie_chow_f64(int32_t n_faces, int32_t n_internal, const int32_t* owner,
-                                 const int32_t* neighbour, const double* p, const double* A_p,
+                                 const int32_t* neighbour, const double* p, const double* inv_A_p,
                                  const double* face_areas, const double* delta,
                                  const double* weights, const double* phi_in, double* out,
                                  void* stream) {
   GBF_REQUIRE(n_faces >= 0 && n_internal >= 0 && n_internal <= n_faces,
               "rhie_chow: bad face counts");
   if (n_faces == 0) return GBF_OK;
-  GBF_REQUIRE(out && (n_internal == 0 || (owner && neighbour && p && A_p && face_areas &&
+  GBF_REQUIRE(out && (n_internal == 0 || (owner && neighbour && p && inv_A_p && face_areas &&
                                           delta)),
               "rhie_chow: NULL pointer");
   rc_kernel<<<grid_of(n_faces), kBlock, 0, as_stream(stream)>>>(
-      phi_in ? 1 : 0, n_faces, n_internal, owner, neighbour, p, A_p, face_areas, delta, weights,
+      phi_in ? 1 : 0, n_faces, n_internal, owner, neighbour, p, inv_A_p, face_areas, delta,
+      weights,
       phi_in, out);
   GBF_CHECK_LAUNCH();
   return GBF_OK;

@@ -80,6 +80,10 @@ class HexMesh:
         Patches that get a non-zero boundary delta coefficient.
     device, dtype :
         Where the torch tensors of the mesh live.
+    geometry : bool
+        Compute the geometry with the vectorised numpy restatement (default).
+        ``False`` keeps only points and addressing, e.g. for ``polymesh()``
+        whose geometry the GPU ``FvMesh`` computes.
     """
 
     def __init__(
@@ -93,6 +97,7 @@ class HexMesh:
         dirichlet: tuple[str, ...] = ("x0",),
         device: torch.device | str = "cpu",
         dtype: torch.dtype = torch.float64,
+        geometry: bool = True,
     ) -> None:
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
@@ -145,7 +150,8 @@ class HexMesh:
 
         self._owner_np = owner_all
         self._neigh_np = neigh
-        self._geometry()
+        if geometry:
+            self._geometry()
 
     # ------------------------------------------------------------------
     def _make_points(self) -> np.ndarray:
@@ -339,6 +345,19 @@ class HexMesh:
     @property
     def points(self) -> torch.Tensor:
         return self._tensor("points", self._points, self.dtype)
+
+    def polymesh(self) -> dict:
+        """The mesh as polyMesh arrays: points (n_points, 3), faces as CSR
+        (face_ptr, face_pts; four vertices each, normal out of the owner),
+        owner (all faces), neighbour (internal faces) and the boundary
+        patches (name, type, startFace, nFaces)."""
+        cells = np.concatenate([self._int_cell, self._bnd_cell])
+        kind = np.concatenate([self._int_dir, self._bnd_kind + 3])
+        faces = self._face_points(cells, kind)
+        return dict(points=self._points, face_ptr=np.arange(0, 4 * faces.shape[0] + 1, 4),
+                    face_pts=faces.ravel(), owner=self._owner_np, neighbour=self._neigh_np,
+                    boundary=[{"name": p.name, "type": "patch", "startFace": p.start,
+                               "nFaces": p.size} for p in self.patches.values()])
 
     def to(self, device=None, dtype=None) -> "HexMesh":
         """Return a shallow copy whose tensors live on ``device``/``dtype``."""

@@ -134,7 +134,7 @@ class GAMGSolver(LinearSolverBase):
     def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 100,
                  min_iter: int = 0, verbose: bool = False, n_pre_smooth: int = 2,
                  n_post_smooth: int = 2, max_levels: int = 10, min_cells_coarse: int = 10,
-                 smoother: str = "PCG") -> None:
+                 smoother: str = "PCG", *, use_graph: bool = True) -> None:
         super().__init__(tolerance=tolerance, rel_tol=rel_tol, max_iter=max_iter,
                          min_iter=min_iter, verbose=verbose)
         self._n_pre_smooth = n_pre_smooth
@@ -142,6 +142,7 @@ class GAMGSolver(LinearSolverBase):
         self._max_levels = max_levels
         self._min_cells_coarse = min_cells_coarse
         self._smoother_type = smoother.upper()  # stored; the reference smooths with Jacobi
+        self._use_graph = bool(use_graph)
         self.last_levels: list[GAMGLevel] = []
 
     # ------------------------------------------------------------------
@@ -200,6 +201,9 @@ class GAMGSolver(LinearSolverBase):
         if build_topo:
             topo_cache[tkey] = aggs_topo
         out = (levels, aggs)
+        # one hierarchy (and its captured cycle) per matrix: drop stale ones
+        for k in [k for k in matrix._csr_cache if k[0] in ("gamg", "gamg_cycle")]:
+            del matrix._csr_cache[k]
         matrix._csr_cache[key] = out
         return out
 
@@ -242,17 +246,57 @@ class GAMGSolver(LinearSolverBase):
             raise ValueError(f"source/x0 have {b.shape[0]}/{x.shape[0]} elements, expected {n}")
         levels, aggs = self._hierarchy(matrix)
         self.last_levels = levels
-        L = _lib.lib()
-        ws = torch.empty(int(L.gbf_norm2_workspace_bytes()), device=dev, dtype=torch.uint8)
-        nrm = torch.empty(1, device=dev, dtype=torch.float64)
-        r = torch.empty_like(x)
+        cyc = self._cycle(matrix, levels, aggs)
+        cyc["x"].copy_(x)
+        cyc["b"].copy_(b)
         converged = False
         for i in range(1, max_iter + 1):
-            self._v_cycle(levels, aggs, 0, x, b)
-            residual(matrix, b, x, r)
-            _lib.check(L.gbf_norm2_f64(n, r.data_ptr(), nrm.data_ptr(), ws.data_ptr(),
-                                       _lib.stream_ptr(dev)), "gbf_norm2_f64")
-            if monitor.check(float(nrm.item()), i):
+            cyc["run"]()
+            if monitor.check(float(cyc["nrm"].item()), i):
                 converged = True
                 break
-        return x, monitor.build_info(converged=converged)
+        return cyc["x"].clone(), monitor.build_info(converged=converged)
+
+    def _cycle(self, matrix: LduMatrix, levels, aggs) -> dict:
+        """One V-cycle plus the residual norm on static buffers, captured
+        once into a CUDA graph per hierarchy (the cycle is a few hundred
+        small launches, so replaying the graph removes the per-launch host
+        cost); eager launches if capture is off or fails."""
+        key = ("gamg_cycle", id(levels))
+        hit = matrix._csr_cache.get(key)
+        if hit is not None:
+            return hit
+        dev, n = matrix.device, matrix.n_cells
+        L = _lib.lib()
+        buf = {"x": torch.zeros(n, device=dev, dtype=torch.float64),
+               "b": torch.zeros(n, device=dev, dtype=torch.float64),
+               "r": torch.empty(n, device=dev, dtype=torch.float64),
+               "ws": torch.empty(int(L.gbf_norm2_workspace_bytes()), device=dev,
+                                 dtype=torch.uint8),
+               "nrm": torch.empty(1, device=dev, dtype=torch.float64), "levels": levels}
+
+        def body():
+            self._v_cycle(levels, aggs, 0, buf["x"], buf["b"])
+            residual(matrix, buf["b"], buf["x"], buf["r"])
+            _lib.check(L.gbf_norm2_f64(n, buf["r"].data_ptr(), buf["nrm"].data_ptr(),
+                                       buf["ws"].data_ptr(), _lib.stream_ptr(dev)),
+                       "gbf_norm2_f64")
+
+        buf["run"] = body
+        if self._use_graph and n > 0:
+            try:
+                side = torch.cuda.Stream(device=dev)
+                side.wait_stream(torch.cuda.current_stream(dev))
+                with torch.cuda.stream(side):
+                    body()  # warm-up: module load, occupancy queries, allocator pool
+                torch.cuda.current_stream(dev).wait_stream(side)
+                torch.cuda.synchronize(dev)
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph):
+                    body()
+                buf["graph"] = graph
+                buf["run"] = graph.replay
+            except RuntimeError:
+                buf["run"] = body
+        matrix._csr_cache[key] = buf
+        return buf

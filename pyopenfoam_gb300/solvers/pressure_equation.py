@@ -112,7 +112,10 @@ def correct_face_flux(phi: torch.Tensor, p: torch.Tensor, A_p: torch.Tensor, mes
     dev = md.device
     topo = md.topology()
     ph = _f64(phi, dev, md.n_faces, "phi")
-    pp, A = _f64(p, dev, md.n_cells, "p"), _f64(A_p, dev, md.n_cells, "A_p")
+    from .rhie_chow import inv_abs_clamped
+
+    pp = _f64(p, dev, md.n_cells, "p")
+    A = inv_abs_clamped(_f64(A_p, dev, md.n_cells, "A_p"))
     w = _f64(mesh.face_weights if face_weights is None else face_weights, dev)
     out = torch.empty_like(ph)
     _lib.check(_lib.lib().gbf_rhie_chow_f64(

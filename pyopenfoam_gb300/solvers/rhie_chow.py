@@ -41,6 +41,18 @@ def compute_HbyA(H: torch.Tensor, A_p: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def inv_abs_clamped(A_p: torch.Tensor) -> torch.Tensor:
+    """1 / max(|A_p|, 1e-30) per cell, on the GPU."""
+    A = torch.as_tensor(A_p).detach().to(dtype=torch.float64).contiguous()
+    dev = resolve_device(A.device)
+    A = A.to(dev)
+    inv = torch.empty_like(A)
+    _lib.check(_lib.lib().gbf_inv_abs_clamped_f64(A.shape[0], A.data_ptr(), inv.data_ptr(),
+                                                  _lib.stream_ptr(dev)),
+               "gbf_inv_abs_clamped_f64")
+    return inv
+
+
 def _flux(HbyA, face_areas, owner, neighbour, n_internal_faces, face_weights, p=None, A_p=None,
           delta_coefficients=None):
     dev = resolve_device(HbyA.device)
@@ -53,7 +65,7 @@ def _flux(HbyA, face_areas, owner, neighbour, n_internal_faces, face_weights, p=
     w = None if face_weights is None else _f64(face_weights, dev)
     ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
     pp = None if p is None else _f64(p, dev)
-    A = None if A_p is None else _f64(A_p, dev)
+    A = None if A_p is None else inv_abs_clamped(_f64(A_p, dev))
     d = None if delta_coefficients is None else _f64(delta_coefficients, dev)
     phi = torch.empty(nf, device=dev, dtype=torch.float64)
     _lib.check(_lib.lib().gbf_face_flux_f64(nf, ni, own.data_ptr(),
@@ -79,7 +91,7 @@ def rhie_chow_correction(p: torch.Tensor, A_p: torch.Tensor, face_areas: torch.T
     S = _f64(face_areas, dev)
     nf, ni = S.shape[0], int(n_internal_faces)
     own, nei = _i32(owner, dev), _i32(neighbour, dev)
-    pp, A, d = _f64(p, dev), _f64(A_p, dev), _f64(delta_coefficients, dev)
+    pp, A, d = _f64(p, dev), inv_abs_clamped(_f64(A_p, dev)), _f64(delta_coefficients, dev)
     w = None if face_weights is None else _f64(face_weights, dev)
     out = torch.empty(nf, device=dev, dtype=torch.float64)
     _lib.check(_lib.lib().gbf_rhie_chow_f64(nf, ni, own.data_ptr(),
