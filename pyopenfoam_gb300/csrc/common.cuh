@@ -7,6 +7,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <utility>
+
 #include <nvtx3/nvToolsExt.h>
 
 #include "gbfoam.h"
@@ -22,6 +24,34 @@ struct NvtxScope {
   NvtxScope(const NvtxScope&) = delete;
   NvtxScope& operator=(const NvtxScope&) = delete;
 };
+
+// Programmatic dependent launch (sm_90+): a kernel launched with
+// launch_pdl may be scheduled while the previous kernel on the stream is
+// still finishing; it must call pdl_wait() before it reads anything that
+// kernel wrote (the wait returns once the previous grid has completed and
+// its memory is visible).  pdl_launch_dependents() lets the next kernel be
+// scheduled as this grid's blocks retire.  Both are no-ops for a kernel
+// launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Per-thread error message (gbf_last_error()).
 void set_error(const char* fmt, ...);

@@ -129,6 +129,8 @@ __global__ void __launch_bounds__(kBlock)
 template <int KIND>
 __global__ void __launch_bounds__(kBlock)
     mp_ap_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (v.st->status != GBF_RUNNING) return;
   __shared__ double sh[kBlock / 32];
   const int G = gridDim.x;
@@ -163,6 +165,8 @@ template <bool SYM>
 __global__ void __launch_bounds__(kTileCells, 8)
     mp_ap_stream_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v,
                         int n_tiles) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (v.st->status != GBF_RUNNING) return;
   __shared__ HexRing<SYM> ring;
   __shared__ double sh[kTileCells / 32];
@@ -209,6 +213,8 @@ __global__ void __launch_bounds__(kTileCells, 8)
 __global__ void __launch_bounds__(kBlock)
     mp_update_kernel(int n, double* __restrict__ x, MixedVecs v, double delta,
                      gbf_solve_params P) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (v.st->status != GBF_RUNNING) return;
   __shared__ double sh[kBlock / 32];
   const int G = gridDim.x;
@@ -307,6 +313,8 @@ __global__ void __launch_bounds__(kBlock)
                    const double* __restrict__ diag64, const double* __restrict__ b,
                    const double* __restrict__ x, MixedVecs v, double* hist, int hist_cap,
                    gbf_solve_params P) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (v.st->status != GBF_RUNNING || v.st->phase != MP_TRUE_RESIDUAL) return;
   __shared__ double sh[kBlock / 32];
   const int G = gridDim.x;
@@ -353,6 +361,8 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 __global__ void __launch_bounds__(kBlock) mp_p_kernel(int n, MixedVecs v) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (v.st->status != GBF_RUNNING) return;
   const float beta = (float)v.st->beta;
   const int n4 = n >> 2;
@@ -462,21 +472,29 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   const int limit = P->max_iter + 2;
   while (hs.status == GBF_RUNNING && launched < limit) {
     for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
-      const bool tb = timing_begin(kProbeMixedAp, s);
+      // every kernel of the iteration is a programmatic dependent launch of
+      // the previous one; one K_ap launch in eight is bracketed by events
+      // for the timing probe (an event between two kernels serialises them)
+      const bool tb = (launched % 8 == 0) && timing_begin(kProbeMixedAp, s);
+      const gbf_layout Lv = *L;
+      cudaError_t e;
       if (staged && sym)
-        mp_ap_stream_kernel<true><<<Ga, Ba, 0, s>>>(*L, coef32, v, n_tiles);
+        e = launch_pdl(mp_ap_stream_kernel<true>, Ga, Ba, s, Lv, coef32, v, n_tiles);
       else if (staged)
-        mp_ap_stream_kernel<false><<<Ga, Ba, 0, s>>>(*L, coef32, v, n_tiles);
+        e = launch_pdl(mp_ap_stream_kernel<false>, Ga, Ba, s, Lv, coef32, v, n_tiles);
       else if (sym)
-        mp_ap_kernel<kLayoutHex33Sym><<<Ga, Ba, 0, s>>>(*L, coef32, v);
+        e = launch_pdl(mp_ap_kernel<kLayoutHex33Sym>, Ga, Ba, s, Lv, coef32, v);
       else if (hex)
-        mp_ap_kernel<kLayoutHex33><<<Ga, Ba, 0, s>>>(*L, coef32, v);
+        e = launch_pdl(mp_ap_kernel<kLayoutHex33>, Ga, Ba, s, Lv, coef32, v);
       else
-        mp_ap_kernel<kLayoutGeneric><<<Ga, Ba, 0, s>>>(*L, coef32, v);
+        e = launch_pdl(mp_ap_kernel<kLayoutGeneric>, Ga, Ba, s, Lv, coef32, v);
       if (tb) timing_end(kProbeMixedAp, s);
-      mp_update_kernel<<<Gu, kBlock, 0, s>>>(n, x, v, delta, *P);
-      mp_true_kernel<<<Gt, kBlock, 0, s>>>(*L, coef64, diag64, b, x, v, hist, hist_cap, *P);
-      mp_p_kernel<<<Gp, kBlock, 0, s>>>(n, v);
+      if (e == cudaSuccess) e = launch_pdl(mp_update_kernel, Gu, kBlock, s, n, x, v, delta, *P);
+      if (e == cudaSuccess)
+        e = launch_pdl(mp_true_kernel, Gt, kBlock, s, Lv, coef64, diag64, b,
+                       static_cast<const double*>(x), v, hist, hist_cap, *P);
+      if (e == cudaSuccess) e = launch_pdl(mp_p_kernel, Gp, kBlock, s, n, v);
+      GBF_CHECK_CUDA(e);
     }
     GBF_CHECK_LAUNCH();
     GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
