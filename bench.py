@@ -570,8 +570,10 @@ def c2_system(N: int, dev):
 
 def run_c2(args, rank, world, local):
     """128^3 jittered convection-diffusion, PBiCGStab+DILU to 1e-8."""
+    import ctypes
+
     from oracle import oracle as O
-    from pyopenfoam_gb300 import PBiCGSTABSolver
+    from pyopenfoam_gb300 import MixedPrecisionPBiCGSTABSolver, PBiCGSTABSolver, _lib
 
     dev = torch.device("cuda", local)
     N = 128 if args.n == 256 else args.n
@@ -579,9 +581,9 @@ def run_c2(args, rank, world, local):
     mesh, A, b = c2_system(N, dev)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
-    res = {}
-    for omega in ("standard", "reference"):
-        s = PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000, omega=omega)
+    L = _lib.lib()
+
+    def timed(s):
         ts = []
         for i in range(args.warmup + args.steps):
             A.invalidate_cache()
@@ -591,9 +593,40 @@ def run_c2(args, rank, world, local):
             torch.cuda.synchronize()
             if i >= args.warmup:
                 ts.append(time.perf_counter() - t0)
-        res[omega] = {"s": statistics.median(ts), "checks": it,
-                      "converged": s.last_info.converged,
-                      "true_rel_residual": true_rel_residual(A, x, b), "x": x}
+        return x, it, statistics.median(ts)
+
+    res = {}
+    solvers = {
+        "standard": PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000, omega="standard"),
+        "reference": PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000,
+                                     omega="reference"),
+        "mixed": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000),
+        "standard_1e-10": PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=4000,
+                                          omega="standard"),
+        "mixed_1e-10": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10,
+                                                     max_iter=4000),
+    }
+    for key, s in solvers.items():
+        mixed = key.startswith("mixed")
+        if mixed:
+            _lib.check(L.gbf_timing_enable(1, 4096))
+        x, it, t = timed(s)
+        res[key] = {"s": t, "converged": s.last_info.converged,
+                    "true_rel_residual": true_rel_residual(A, x, b), "x": x}
+        if mixed:
+            R = s.last_result
+            cnt, tot = ctypes.c_int32(0), ctypes.c_double(0.0)
+            _lib.check(L.gbf_timing_read(4, ctypes.byref(cnt), ctypes.byref(tot)))
+            _lib.check(L.gbf_timing_enable(0, 0))
+            res[key].update(inner_iterations=R.inner_iterations, fp64_updates=R.outer_updates,
+                            inner_iterations_per_s=R.inner_iterations / t,
+                            k_v_us=(tot.value * 1e3 / cnt.value) if cnt.value else None)
+        else:
+            res[key].update(checks=it, iterations=(it - 1) / 2, iterations_per_s=(it - 1) / 2 / t)
+    for key, ref in (("mixed", "standard"), ("mixed_1e-10", "standard_1e-10")):
+        res[key]["speedup_vs_fp64"] = res[ref]["s"] / res[key]["s"]
+        res[key]["x_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(res[key]["x"] - res[ref]["x"])
+                                              / torch.linalg.vector_norm(res[ref]["x"]))
     cpu = None
     if rank == 0 and not args.no_cpu:
         own = A.owner.cpu().numpy()
@@ -619,7 +652,8 @@ def run_c2(args, rank, world, local):
                            "boundary term", "n_cells": mesh.n_cells,
                "n_faces": mesh.n_internal_faces},
               {"omega_standard": res["standard"], "omega_reference": res["reference"],
-               "setup_s": t_setup}, cpu_baseline=cpu)
+               "mixed_fp32_fp64": res["mixed"], "fp64_to_1e-10": res["standard_1e-10"],
+               "mixed_to_1e-10": res["mixed_1e-10"], "setup_s": t_setup}, cpu_baseline=cpu)
 
 
 def run_c4(args, rank, world, local):

@@ -101,7 +101,8 @@ int gbf_selftest_bounded_waits(int32_t* timed_out_h);
  * launching stream; gbf_timing_read synchronises and returns, per probe,
  * the number of timed launches and their summed duration in ms.
  * Probe ids: 0 = FP64 PCG Amul+dot, 1 = mixed PCG FP32 Amul+dot,
- * 2 = PBiCGStab Amul+dot (v and t), 3 = mixed PCG FP64 true residual.     */
+ * 2 = PBiCGStab Amul+dot (v and t), 3 = mixed PCG FP64 true residual,
+ * 4 = mixed PBiCGStab FP32 Amul+dot (v = A y).                             */
 int gbf_timing_enable(int32_t enable, int32_t max_events_per_probe);
 int gbf_timing_read(int32_t probe, int32_t* launches, double* total_ms);
 
@@ -565,6 +566,22 @@ int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double*
                         const double* b, double* x, double delta, double* history, int32_t hist_cap,
                         const gbf_solve_params* P, gbf_solve_result* R, void* workspace,
                         size_t workspace_bytes, void* stream);
+/* Mixed-precision PBiCGStab: the iteration of gbf_pbicgstab_solve_f64
+ * (pbicgstab.py:103-239, the same breakdown tests) with FP32 vectors, Amul
+ * and diagonal preconditioner and the same FP64 reliable updates as
+ * gbf_mixed_pcg_solve (residual replacement keeping p, r~ and rho).
+ * Convergence on true residuals only (the FP64 solver's half-step check on
+ * s is not taken).  P->variant: 0 omega = (t.z)/(t.t) as the reference,
+ * 1 the standard (t.s)/(t.t).  coef32 = FP32 packing of the FP64 matrix;
+ * precond_d = FP64 DILU/DIC diagonal or NULL.  history / R as for
+ * gbf_mixed_pcg_solve.  Replaces PBiCGSTABSolver._solve
+ * (solvers/pbicgstab.py:103) for the momentum solve.                        */
+size_t gbf_mixed_pbicgstab_workspace_bytes(int32_t n_cells);
+int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef64, const double* diag64,
+                              const float* coef32, const double* precond_d, const double* b,
+                              double* x, double delta, double* history, int32_t hist_cap,
+                              const gbf_solve_params* P, gbf_solve_result* R, void* workspace,
+                              size_t workspace_bytes, void* stream);
 
 /* ---- batching ---------------------------------------------------------------
  * No reference counterpart.  Many independent systems solved together: the

@@ -7,10 +7,12 @@ kernels in ``libgbfoam.so`` reached through a C ABI (``include/gbfoam.h``).
 """
 
 from .core import FvMatrix, LduMatrix
-from .solvers import (DICPreconditioner, DILUPreconditioner, MixedPrecisionPCGSolver,
-                      PBiCGSTABSolver, PCGSolver, create_solver, solver_from_dict)
+from .solvers import (DICPreconditioner, DILUPreconditioner, MixedPrecisionPBiCGSTABSolver,
+                      MixedPrecisionPCGSolver, PBiCGSTABSolver, PCGSolver, create_solver,
+                      solver_from_dict)
 
-__all__ = ["LduMatrix", "FvMatrix", "PCGSolver", "PBiCGSTABSolver", "MixedPrecisionPCGSolver", "DICPreconditioner",
-           "DILUPreconditioner", "create_solver", "solver_from_dict"]
+__all__ = ["LduMatrix", "FvMatrix", "PCGSolver", "PBiCGSTABSolver", "MixedPrecisionPCGSolver",
+           "MixedPrecisionPBiCGSTABSolver", "DICPreconditioner", "DILUPreconditioner",
+           "create_solver", "solver_from_dict"]
 
 __version__ = "0.1.0"

@@ -204,6 +204,10 @@ EXPORTED: dict[str, tuple] = {
     "gbf_mixed_pcg_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp, _c_vp,
                                            _c_dbl, _c_vp, _c_i32, _P(SolveParams),
                                            _P(SolveResult), _c_vp, _c_size, _c_vp]),
+    "gbf_mixed_pbicgstab_workspace_bytes": (_c_size, [_c_i32]),
+    "gbf_mixed_pbicgstab_solve": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                                 _c_dbl, _c_vp, _c_i32, _P(SolveParams),
+                                                 _P(SolveResult), _c_vp, _c_size, _c_vp]),
     "gbf_batched_mixed_pcg_workspace_bytes": (_c_size, [_c_i32, _c_i32, _c_i32]),
     "gbf_batched_mixed_pcg_solve": (ctypes.c_int, [_L, _P(Batch), _c_vp, _c_vp, _c_vp, _c_vp,
                                                    _c_vp, _c_vp, _c_dbl, _P(SolveParams), _c_i32,

@@ -28,6 +28,7 @@ SOURCES = [
     "pcg.cu",
     "pbicgstab.cu",
     "mixed.cu",
+    "mixed_bicg.cu",
     "assemble.cu",
     "batched.cu",
     "geometry.cu",

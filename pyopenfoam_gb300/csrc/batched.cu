@@ -41,19 +41,7 @@ struct BTiles {
   const int32_t* sys_tile0;  // [n_systems + 1]
 };
 
-struct BDFAcc {
-  float hi = 0.0f, lo = 0.0f;
-  __device__ __forceinline__ void add_prod(float a, float b) {
-    const float p = __fmul_rn(a, b);
-    const float e = __fmaf_rn(a, b, -p);
-    const float s = __fadd_rn(hi, p);
-    const float bb = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(err, e));
-  }
-  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
+using BDFAcc = DFAcc;
 
 // True in every thread of the tile that finished last among its system's
 // tiles (count = number of tiles of the system); resets the ticket.

@@ -105,8 +105,14 @@ inline int wave_grid(K kernel, int block, long long work) {
 
 // Kernel timing probes (gbf_timing_enable): timing_begin returns true when
 // an event was recorded; the caller then calls timing_end after the launch.
-constexpr int kNumProbes = 4;
-enum { kProbePcgAp = 0, kProbeMixedAp = 1, kProbeBicgAmul = 2, kProbeMixedTrue = 3 };
+constexpr int kNumProbes = 5;
+enum {
+  kProbePcgAp = 0,
+  kProbeMixedAp = 1,
+  kProbeBicgAmul = 2,
+  kProbeMixedTrue = 3,
+  kProbeMixedBicgAmul = 4
+};
 bool timing_begin(int probe, cudaStream_t s);
 void timing_end(int probe, cudaStream_t s);
 int reduction_grid();  // fixed grid of the reducing kernels (SMs x 8, <= kMaxGrid)
@@ -227,5 +233,25 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+// Exact FP64 product of two FP32 values.
+__device__ __forceinline__ double dprod(float a, float b) { return (double)a * (double)b; }
+
+// Double-float accumulator: hi + lo carries the running sum of exact FP32
+// products.  Every operation is an explicitly rounded intrinsic so that the
+// compiler cannot contract or reassociate the error-free transformations.
+struct DFAcc {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);  // a*b - p exactly (TwoProduct)
+    const float s = __fadd_rn(hi, p);     // TwoSum(hi, p)
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 }  // namespace gbf

@@ -48,25 +48,6 @@ struct MixedVecs {
   MixedState* st;
 };
 
-__device__ __forceinline__ double dprod(float a, float b) { return (double)a * (double)b; }
-
-// Double-float accumulator: hi + lo carries the running sum of exact FP32
-// products.  Every operation is an explicitly rounded intrinsic so that the
-// compiler cannot contract or reassociate the error-free transformations.
-struct DFAcc {
-  float hi = 0.0f, lo = 0.0f;
-  __device__ __forceinline__ void add_prod(float a, float b) {
-    const float p = __fmul_rn(a, b);
-    const float e = __fmaf_rn(a, b, -p);  // a*b - p exactly (TwoProduct)
-    const float s = __fadd_rn(hi, p);     // TwoSum(hi, p)
-    const float bb = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(err, e));
-  }
-  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-
 // r64 = b - A64 x64 for cell c; writes r, z; returns r64.
 __device__ __forceinline__ double true_residual_cell(const gbf_layout& L,
                                                      const double* __restrict__ coef64,

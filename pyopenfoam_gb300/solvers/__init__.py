@@ -4,7 +4,7 @@ from .batched import BatchedPCGSolver
 from .diagonal import DiagonalSolver
 from .gamg import GAMGSolver
 from .linear_solver import LinearSolverBase, create_solver, register_solver, solver_from_dict
-from .mixed import MixedPrecisionPCGSolver
+from .mixed import MixedPrecisionPBiCGSTABSolver, MixedPrecisionPCGSolver
 from .pbicg import PBiCGSolver
 from .pbicgstab import PBiCGSTABSolver
 from .pcg import PCGSolver
@@ -17,7 +17,7 @@ from .smoothers import DICGSmoother, GaussSeidelSmoother, JacobiSmoother
 
 __all__ = [
     "LinearSolverBase", "create_solver", "solver_from_dict", "register_solver", "PCGSolver",
-    "PBiCGSTABSolver", "MixedPrecisionPCGSolver", "SmoothSolver", "DICPreconditioner",
+    "PBiCGSTABSolver", "MixedPrecisionPCGSolver", "MixedPrecisionPBiCGSTABSolver", "SmoothSolver", "DICPreconditioner",
     "DILUPreconditioner", "Preconditioner", "ConvergenceInfo", "ResidualMonitor",
     "BatchedPCGSolver", "assemble_pressure_equation", "solve_pressure_equation",
     "correct_velocity", "correct_face_flux", "adjust_phi", "GaussSeidelSmoother",

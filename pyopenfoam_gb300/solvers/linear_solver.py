@@ -71,7 +71,7 @@ _SOLVER_REGISTRY: dict[str, type[LinearSolverBase]] = {}
 def _register_defaults() -> None:
     if _SOLVER_REGISTRY:
         return
-    from .mixed import MixedPrecisionPCGSolver
+    from .mixed import MixedPrecisionPBiCGSTABSolver, MixedPrecisionPCGSolver
     from .pbicgstab import PBiCGSTABSolver
     from .pcg import PCGSolver
     from .diagonal import DiagonalSolver
@@ -86,6 +86,7 @@ def _register_defaults() -> None:
     _SOLVER_REGISTRY["PBICGSTAB"] = PBiCGSTABSolver
     _SOLVER_REGISTRY["SMOOTHSOLVER"] = SmoothSolver
     _SOLVER_REGISTRY["MIXEDPCG"] = MixedPrecisionPCGSolver
+    _SOLVER_REGISTRY["MIXEDPBICGSTAB"] = MixedPrecisionPBiCGSTABSolver
 
 
 def register_solver(name: str, cls: type[LinearSolverBase]) -> None:

@@ -25,7 +25,7 @@ from .linear_solver import LinearSolverBase
 from .preconditioners import DICPreconditioner, DILUPreconditioner, Preconditioner
 from .residual import ConvergenceInfo, ResidualMonitor
 
-__all__ = ["MixedPrecisionPCGSolver"]
+__all__ = ["MixedPrecisionPCGSolver", "MixedPrecisionPBiCGSTABSolver"]
 
 
 class MixedPrecisionPCGSolver(LinearSolverBase):
@@ -106,6 +106,93 @@ class MixedPrecisionPCGSolver(LinearSolverBase):
         if R.status == _lib.GBF_DEVICE_TIMEOUT:
             raise RuntimeError("gbf_mixed_pcg_solve: a bounded wait on a staged copy ran out "
                                "inside the Amul kernel; the result is invalid")
+        nh = min(R.outer_updates + 1, cap) if n > 0 else 1
+        monitor.record(hist[:nh].tolist() if n > 0 else [0.0])
+        info = monitor.build_info(converged=(R.status == _lib.GBF_CONVERGED))
+        info.iterations = R.iterations
+        info.final_residual = R.final_residual
+        return x, info
+
+
+class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
+    """PBiCGStab with FP32 inner iterations and FP64 reliable updates, for
+    the asymmetric momentum solve.
+
+    The iteration and its breakdown tests are those of ``PBiCGSTABSolver``
+    (solvers/pbicgstab.py:103-239); the vectors, the Amul and the diagonal
+    DILU/DIC preconditioner run in FP32, and the FP32 correction is folded
+    into the FP64 solution (with the residual replaced by the true
+    b - A x) whenever the iterated residual has dropped by ``delta``.
+    Convergence is checked on the true residual only, once per update, so
+    the half-step check on s is not taken.  ``omega`` (keyword only):
+    ``"standard"`` (default here) takes (t.s)/(t.t); ``"reference"`` takes
+    the reference's (t.z)/(t.t)."""
+
+    def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 1000,
+                 min_iter: int = 0, verbose: bool = False, preconditioner: str = "DILU", *,
+                 omega: str = "standard", delta: float = 0.1, check_every: int = 32) -> None:
+        super().__init__(tolerance=tolerance, rel_tol=rel_tol, max_iter=max_iter,
+                         min_iter=min_iter, verbose=verbose)
+        self._precond_type = preconditioner.upper()
+        if omega not in ("reference", "standard"):
+            raise ValueError(f"omega must be 'reference' or 'standard', got {omega!r}")
+        if not 0.0 < delta < 1.0:
+            raise ValueError(f"delta must be in (0, 1), got {delta}")
+        self._omega = omega
+        self._delta = float(delta)
+        self._check_every = int(check_every)
+        self.last_result: _lib.SolveResult | None = None
+
+    def _make_preconditioner(self, matrix: LduMatrix) -> Preconditioner | None:
+        if self._precond_type == "DILU":
+            return DILUPreconditioner(matrix)
+        if self._precond_type == "DIC":
+            return DICPreconditioner(matrix)
+        if self._precond_type == "NONE":
+            return None
+        raise ValueError(
+            f"Unknown preconditioner '{self._precond_type}'. Use 'DILU', 'DIC', or 'none'."
+        )
+
+    def _solve(self, matrix: LduMatrix, source: torch.Tensor, x0: torch.Tensor,
+               monitor: ResidualMonitor, max_iter: int) -> tuple[torch.Tensor, ConvergenceInfo]:
+        if matrix.dtype != torch.float64:
+            raise TypeError("MixedPrecisionPBiCGSTABSolver takes the float64 matrix and makes "
+                            f"its own FP32 copy (got {matrix.dtype})")
+        dev = matrix.device
+        n = matrix.n_cells
+        if source.shape[0] != n or x0.shape[0] != n:
+            raise ValueError(f"source/x0 have {source.shape[0]}/{x0.shape[0]} elements, "
+                             f"expected {n}")
+        b = source.to(device=dev, dtype=torch.float64).contiguous()
+        x = x0.to(device=dev, dtype=torch.float64).clone().contiguous()
+        precond = self._make_preconditioner(matrix)
+        pd = None if precond is None else precond.precond_diag
+        topo = matrix.topology()
+        coef64 = matrix.packed()
+        coef32 = matrix.packed(dtype=torch.float32)
+        L = _lib.lib()
+        cap = 4096
+        hist = torch.zeros(cap, device=dev, dtype=torch.float64)
+        ws = torch.empty(max(int(L.gbf_mixed_pbicgstab_workspace_bytes(n)), 1), device=dev,
+                         dtype=torch.uint8)
+        P = _lib.SolveParams(float(monitor.tolerance), float(monitor.rel_tol), int(max_iter),
+                             int(monitor.min_iter), self._check_every,
+                             1 if self._omega == "standard" else 0)
+        R = _lib.SolveResult()
+        _lib.check(
+            L.gbf_mixed_pbicgstab_solve(topo.layout_ref, coef64.data_ptr(),
+                                        matrix.diag.data_ptr(), coef32.data_ptr(),
+                                        None if pd is None else pd.data_ptr(), b.data_ptr(),
+                                        x.data_ptr(), self._delta, hist.data_ptr(), cap,
+                                        ctypes.byref(P), ctypes.byref(R), ws.data_ptr(),
+                                        ws.numel(), _lib.stream_ptr(dev)),
+            "gbf_mixed_pbicgstab_solve",
+        )
+        self.last_result = R
+        if R.status == _lib.GBF_DEVICE_TIMEOUT:
+            raise RuntimeError("gbf_mixed_pbicgstab_solve: a bounded wait on a staged copy ran "
+                               "out inside the Amul kernel; the result is invalid")
         nh = min(R.outer_updates + 1, cap) if n > 0 else 1
         monitor.record(hist[:nh].tolist() if n > 0 else [0.0])
         info = monitor.build_info(converged=(R.status == _lib.GBF_CONVERGED))
