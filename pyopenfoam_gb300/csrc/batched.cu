@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(BS)
     v.Ap[c] = y;
     a.add_prod(pc, y);
   }
-  const double acc = block_sum(a.value(), sh);
+  const double acc = block_sum_df(a, sh);
   if (threadIdx.x == 0) v.partials[tile] = acc;
   const int t0 = __ldg(T.sys_tile0 + s), t1 = __ldg(T.sys_tile0 + s + 1);
   if (last_tile_of_system(&st->ticket[1], t1 - t0)) {
@@ -181,8 +181,8 @@ __global__ void __launch_bounds__(BS)
     arr.add_prod(r, r);
     arz.add_prod(r, z);
   }
-  const double rr = block_sum(arr.value(), sh);
-  const double rz = block_sum(arz.value(), sh);
+  const double rr = block_sum_df(arr, sh);
+  const double rz = block_sum_df(arz, sh);
   if (threadIdx.x == 0) {
     v.partials[tile] = rr;
     v.partials[T.n_tiles + tile] = rz;

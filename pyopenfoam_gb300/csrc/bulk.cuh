@@ -241,14 +241,18 @@ inline bool hex_stream_aligned(const void* coef, const void* x, const void* d,
           15u) == 0;
 }
 
-// Runs f(c, y, xc) for every cell of the full tiles assigned to this block
-// (tiles blockIdx.x, blockIdx.x + gridDim.x, ...).  Returns false if a wait
-// ran out (the block then stops streaming after draining its copies).
-template <typename A, bool NEI_FIRST, bool SYM, typename F>
-__device__ __forceinline__ bool hex_stream_tiles(HexRing<SYM>& R, int n_tiles, const float* coef,
-                                                 const float* x, const float* d,
-                                                 const int* slot_dm, const int8_t* slot_mirror,
-                                                 F&& f) {
+// Runs f(c, y, xc, pre(c)) for every cell of the full tiles assigned to this
+// block (tiles blockIdx.x, blockIdx.x + gridDim.x, ...).  pre(c) -- a load of
+// another per-cell operand the epilogue needs -- is issued before the wait
+// on the tile's copies, so that its latency overlaps the wait and the
+// gather instead of following them.  Returns false if a wait ran out (the
+// block then stops streaming after draining its copies).
+template <typename A, bool NEI_FIRST, bool SYM, typename PRE, typename F>
+__device__ __forceinline__ bool hex_stream_tiles_pre(HexRing<SYM>& R, int n_tiles,
+                                                     const float* coef, const float* x,
+                                                     const float* d, const int* slot_dm,
+                                                     const int8_t* slot_mirror, PRE&& pre,
+                                                     F&& f) {
   const int tid = threadIdx.x;
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) mbar_init(&R.bar[s], 1);
@@ -269,13 +273,14 @@ __device__ __forceinline__ bool hex_stream_tiles(HexRing<SYM>& R, int n_tiles, c
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++k) {
     const int s = k % kStages;
     const unsigned parity = (unsigned)(k / kStages) & 1u;
+    const int c = t * kTileCells + tid;
+    const auto aux = pre(c);
     const bool got = mbar_wait(&R.bar[s], parity);
     if (__syncthreads_or(!got)) {
       ok = false;
       break;
     }
-    const int c = t * kTileCells + tid;
-    f(c, hex_cell<A, NEI_FIRST>(R.stage[s], tid, coef, x, c), R.stage[s].x[tid]);
+    f(c, hex_cell<A, NEI_FIRST>(R.stage[s], tid, coef, x, c), R.stage[s].x[tid], aux);
     __syncthreads();  // every thread is done with stage s
     if (tid == 0) {
       const int tn = t + kStages * gridDim.x;
@@ -291,6 +296,17 @@ __device__ __forceinline__ bool hex_stream_tiles(HexRing<SYM>& R, int n_tiles, c
   }
   __syncthreads();
   return ok;
+}
+
+// f(c, y, xc) for every cell of the block's full tiles (no extra operand).
+template <typename A, bool NEI_FIRST, bool SYM, typename F>
+__device__ __forceinline__ bool hex_stream_tiles(HexRing<SYM>& R, int n_tiles, const float* coef,
+                                                 const float* x, const float* d,
+                                                 const int* slot_dm, const int8_t* slot_mirror,
+                                                 F&& f) {
+  return hex_stream_tiles_pre<A, NEI_FIRST, SYM>(
+      R, n_tiles, coef, x, d, slot_dm, slot_mirror, [](int) { return 0; },
+      [&](int c, A y, float xc, int) { f(c, y, xc); });
 }
 
 }  // namespace gbf

@@ -254,4 +254,51 @@ struct DFAcc {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// (hi, lo) += (bhi, blo) in double-float arithmetic: TwoSum of the high
+// parts, low parts and rounding error added into lo.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float bhi, float blo) {
+  const float s = __fadd_rn(hi, bhi);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bhi, bb));
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(blo, err));
+}
+
+__device__ __forceinline__ void df_warp_sum(float& hi, float& lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_down_sync(0xffffffffu, hi, o);
+    const float l = __shfl_down_sync(0xffffffffu, lo, o);
+    df_add(hi, lo, h, l);
+  }
+}
+
+// Sum over the block of the threads' double-float accumulators, as a double
+// in thread 0 (0.0 elsewhere).  The whole tree -- shuffles within each warp,
+// then over the warps -- stays in double-float arithmetic on the FP32 pipes
+// and only thread 0 converts to FP64: GB300's FP64 rate is a small fraction
+// of its FP32 rate, and a per-thread conversion plus an FP64 shuffle tree
+// made the reduction, not memory, the bound of the vector kernels when each
+// thread holds only a few cells.  Fixed order, so deterministic.  `sh`
+// holds blockDim/32 doubles (used as float pairs).
+__device__ __forceinline__ double block_sum_df(const DFAcc& a, double* sh) {
+  float2* s2 = reinterpret_cast<float2*>(sh);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float hi = a.hi, lo = a.lo;
+  df_warp_sum(hi, lo);
+  __syncthreads();  // sh may still be read by a previous call
+  if (lane == 0) s2[wid] = make_float2(hi, lo);
+  __syncthreads();
+  double t = 0.0;
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    const float2 e = (lane < nw) ? s2[lane] : make_float2(0.0f, 0.0f);
+    hi = e.x;
+    lo = e.y;
+    df_warp_sum(hi, lo);
+    if (lane == 0) t = (double)hi + (double)lo;
+  }
+  return t;
+}
+
 }  // namespace gbf

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kBlock)
     v.Ap[c] = y;
     a.add_prod(pc, y);
   }
-  const double acc = block_sum(a.value(), sh);
+  const double acc = block_sum_df(a, sh);
   if (threadIdx.x == 0) v.partials[blockIdx.x] = acc;
   if (last_block_done(&v.st->ticket[1])) {
     const double pAp = reduce_partials(v.partials, G, sh);
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(kTileCells, 8)
     }
   }
   if (!ok && threadIdx.x == 0) atomicExch(&v.st->fault, 1);
-  const double acc = block_sum(a.value(), sh);
+  const double acc = block_sum_df(a, sh);
   if (threadIdx.x == 0) v.partials[blockIdx.x] = acc;
   if (last_block_done(&v.st->ticket[1])) {
     const double pAp = reduce_partials(v.partials, G, sh);
@@ -261,8 +261,8 @@ __global__ void __launch_bounds__(kBlock)
     arr.add_prod(r, r);
     arz.add_prod(r, z);
   }
-  const double rr = block_sum(arr.value(), sh);
-  const double rz = block_sum(arz.value(), sh);
+  const double rr = block_sum_df(arr, sh);
+  const double rz = block_sum_df(arz, sh);
   if (threadIdx.x == 0) {
     v.partials[blockIdx.x] = rr;
     v.partials[G + blockIdx.x] = rz;

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kBlock)
     a.add_prod(r, r);
   }
   rr = block_sum(rr, sh);
-  const double rho = block_sum(a.value(), sh);
+  const double rho = block_sum_df(a, sh);
   if (threadIdx.x == 0) {
     v.partials[blockIdx.x] = rr;
     v.partials[G + blockIdx.x] = rho;
@@ -113,18 +113,30 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// The second operand of the Amul kernels' dot products for cell c: r~[c]
+// (PH 0) or, for the standard omega, s[c] (PH 1; the reference's t.z uses
+// the multiplied vector itself).
+template <int PH>
+__device__ __forceinline__ float mb_amul_aux(const MbVecs& v, int c, int standard_omega) {
+  if constexpr (PH == 0)
+    return __ldg(v.rt + c);
+  else
+    return standard_omega ? __ldg(v.s + c) : 0.0f;
+}
+
 // Epilogue of the two Amul kernels, cell c: PH 0 stores v and accumulates
 // r~.v; PH 1 stores t and accumulates t.t and t.s (standard) or t.z.
 template <int PH>
 __device__ __forceinline__ void mb_amul_cell(const MbVecs& v, int c, float yv, float xc,
-                                             int standard_omega, DFAcc& a0, DFAcc& a1) {
+                                             float aux, int standard_omega, DFAcc& a0,
+                                             DFAcc& a1) {
   if constexpr (PH == 0) {
     v.v[c] = yv;
-    a0.add_prod(__ldg(v.rt + c), yv);
+    a0.add_prod(aux, yv);
   } else {
     v.t[c] = yv;
     a0.add_prod(yv, yv);
-    a1.add_prod(yv, standard_omega ? __ldg(v.s + c) : xc);
+    a1.add_prod(yv, standard_omega ? aux : xc);
   }
 }
 
@@ -133,9 +145,9 @@ template <int PH>
 __device__ __forceinline__ void mb_amul_finish(const MbVecs& v, const DFAcc& a0,
                                                const DFAcc& a1, double* sh) {
   const int G = gridDim.x;
-  const double s0 = block_sum(a0.value(), sh);
+  const double s0 = block_sum_df(a0, sh);
   double s1 = 0.0;
-  if constexpr (PH == 1) s1 = block_sum(a1.value(), sh);
+  if constexpr (PH == 1) s1 = block_sum_df(a1, sh);
   if (threadIdx.x == 0) {
     v.partials[blockIdx.x] = s0;
     if constexpr (PH == 1) v.partials[G + blockIdx.x] = s1;
@@ -177,9 +189,10 @@ __global__ void __launch_bounds__(kBlock)
   DFAcc a0, a1;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells;
        c += gridDim.x * blockDim.x) {
+    const float aux = mb_amul_aux<PH>(v, c, standard_omega);
     const float xc = __ldg(src + c);
     const float yv = cell_amul_k<KIND, float, float, false>(L, coef32, v.d32, src, c, xc);
-    mb_amul_cell<PH>(v, c, yv, xc, standard_omega, a0, a1);
+    mb_amul_cell<PH>(v, c, yv, xc, aux, standard_omega, a0, a1);
   }
   mb_amul_finish<PH>(v, a0, a1, sh);
 }
@@ -200,15 +213,19 @@ __global__ void __launch_bounds__(kTileCells, 8)
   __shared__ double sh[kTileCells / 32];
   const float* __restrict__ src = PH == 0 ? v.y : v.z;
   DFAcc a0, a1;
-  const bool ok = hex_stream_tiles<float, false, false>(
+  const bool ok = hex_stream_tiles_pre<float, false, false>(
       ring, n_tiles, coef32, src, v.d32, L.slot_dm, nullptr,
-      [&](int c, float yv, float xc) { mb_amul_cell<PH>(v, c, yv, xc, standard_omega, a0, a1); });
+      [&](int c) { return mb_amul_aux<PH>(v, c, standard_omega); },
+      [&](int c, float yv, float xc, float aux) {
+        mb_amul_cell<PH>(v, c, yv, xc, aux, standard_omega, a0, a1);
+      });
   if (blockIdx.x == n_tiles % gridDim.x) {
     const int c = n_tiles * kTileCells + threadIdx.x;
     if (c < L.n_cells) {
+      const float aux = mb_amul_aux<PH>(v, c, standard_omega);
       const float xc = __ldg(src + c);
       const float yv = cell_amul_fixed<float, float, false, 3, 3>(L, coef32, v.d32, src, c, xc);
-      mb_amul_cell<PH>(v, c, yv, xc, standard_omega, a0, a1);
+      mb_amul_cell<PH>(v, c, yv, xc, aux, standard_omega, a0, a1);
     }
   }
   if (!ok && threadIdx.x == 0) atomicExch(&v.st->fault, 1);
@@ -322,8 +339,8 @@ __global__ void __launch_bounds__(kBlock)
     arr.add_prod(r, r);
     artr.add_prod(__ldg(v.rt + c), r);
   }
-  const double rr = block_sum(arr.value(), sh);
-  const double rtr = block_sum(artr.value(), sh);
+  const double rr = block_sum_df(arr, sh);
+  const double rtr = block_sum_df(artr, sh);
   if (threadIdx.x == 0) {
     v.partials[blockIdx.x] = rr;
     v.partials[G + blockIdx.x] = rtr;
@@ -376,7 +393,7 @@ __global__ void __launch_bounds__(kBlock)
     artr.add_prod(__ldg(v.rt + c), r);
   }
   rr = block_sum(rr, sh);
-  const double rtr = block_sum(artr.value(), sh);
+  const double rtr = block_sum_df(artr, sh);
   if (threadIdx.x == 0) {
     v.partials[blockIdx.x] = rr;
     v.partials[G + blockIdx.x] = rtr;
