@@ -21,6 +21,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspa
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "reference_outputs.npz")
 JITTER_FIXTURE = os.path.join(HERE, "jitter6_inputs.npz")
+C2SIZE_FIXTURE = os.path.join(HERE, "reference_c2size.npz")
 
 
 def sha(a: np.ndarray) -> str:

@@ -9,6 +9,7 @@ Run in a checkout that has the reference project next to it:
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --smooth
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --gamg
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --pbicg
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --c2size
 
 It imports the reference's own classes (``pyfoam.core.ldu_matrix``,
 ``pyfoam.solvers.*``, ``pyfoam.discretisation.operators.fvm``,
@@ -489,6 +490,57 @@ def gamg(ref_root: str) -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def c2size(ref_root: str) -> None:
+    """Config-2 size (128^3 hex topology, 2,097,152 cells, 6,242,304 faces):
+    Ax, Ax_T, FP32 Ax, the DIC and DILU factorised diagonals
+    (core/ldu_matrix.py:172-258, solvers/preconditioners.py:88-133,228-272)
+    and PBiCGStab+DILU (solvers/pbicgstab.py:103-239) on a seeded random LDU
+    system whose coefficients are exact draws of default_rng (bit-identical
+    on every machine) -> reference_c2size.npz.  Bitwise results as SHA-256;
+    the solve as its iteration count, residual history and every 97th entry
+    of x."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    import time
+
+    import torch
+    from pyfoam.core.ldu_matrix import LduMatrix
+    from pyfoam.solvers.pbicgstab import PBiCGSTABSolver
+    from pyfoam.solvers.preconditioners import DICPreconditioner, DILUPreconditioner
+    from pyfoam.solvers.residual import ResidualMonitor
+
+    torch.set_num_threads(8)
+    t = torch.from_numpy
+    out = {}
+    c = random_ldu(128, seed=5)
+    m = LduMatrix(c["n"], t(c["owner"]), t(c["neighbour"]))
+    m.diag, m.lower, m.upper = t(c["diag"]), t(c["lower"]), t(c["upper"])
+    out["coeff_sha"] = sha(np.concatenate([c["diag"], c["lower"], c["upper"], c["x"], c["r"]]))
+    x = t(c["x"])
+    out["Ax_sha"] = sha(m.Ax(x).numpy())
+    out["AxT_sha"] = sha(m.Ax_T(x).numpy())
+    m32 = LduMatrix(c["n"], t(c["owner"]), t(c["neighbour"]), dtype=torch.float32)
+    m32.diag, m32.lower, m32.upper = t(c["diag"]), t(c["lower"]), t(c["upper"])
+    out["Ax_f32_sha"] = sha(m32.Ax(x.float()).numpy())
+    print("Ax done", flush=True)
+    t0 = time.time()
+    out["dic_sha"] = sha(DICPreconditioner(m)._precond_diag.numpy())
+    print("DIC build", time.time() - t0, flush=True)
+    t0 = time.time()
+    out["dilu_sha"] = sha(DILUPreconditioner(m)._precond_diag.numpy())
+    print("DILU build", time.time() - t0, flush=True)
+    t0 = time.time()
+    mon = ResidualMonitor(tolerance=0.0, rel_tol=1e-10, min_iter=0)
+    solver = PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=200, preconditioner="DILU")
+    xs, info = solver._solve(m, t(c["r"]), torch.zeros(c["n"], dtype=torch.float64), mon, 200)
+    out["bicg_iterations"] = np.int64(info.iterations)
+    out["bicg_history"] = np.array(info.residual_history)
+    out["bicg_x97"] = xs.numpy()[::97].copy()
+    print("PBiCGStab", info.iterations, info.converged, time.time() - t0, flush=True)
+    path = os.path.join(HERE, "reference_c2size.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else os.environ.get("PYFOAM_REFERENCE", "")
@@ -504,5 +556,7 @@ if __name__ == "__main__":
         gamg(root)
     elif "--pbicg" in sys.argv:
         pbicg(root)
+    elif "--c2size" in sys.argv:
+        c2size(root)
     else:
         main(root)
