@@ -27,6 +27,8 @@
 // stops streaming; the host turns the fault into GBF_DEVICE_TIMEOUT.
 #pragma once
 
+#include <stddef.h>
+
 #include "amul.cuh"
 
 namespace gbf {
@@ -43,6 +45,8 @@ struct __align__(128) HexStage {
   float d[kTileCells];
   int2 dm[kTileSlices * kHexW];
 };
+static_assert(offsetof(HexStage, dm) % 16 == 0 && (kHexW * sizeof(int2)) % 16 == 0,
+              "a slice's offset entries are read as 128-bit words");
 constexpr unsigned kStageBytes = sizeof(float) * (kTileSlices * kHexW * 32 + 2 * kTileCells) +
                                  sizeof(int2) * kTileSlices * kHexW;
 static_assert(kStageBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
@@ -156,11 +160,16 @@ __device__ __forceinline__ A hex_cell_from_stage(const HexStage& S, int tid,
   bool on[kHexW];
 #pragma unroll
   for (int k = 0; k < kHexW; ++k) a[k] = S.coef[(sl * kHexW + k) * 32 + lane];
+  // the slice's six {delta, mask} entries: three 128-bit shared loads
+  // (48 B per slice, 16-byte aligned in the stage)
+  const int4* __restrict__ dm4 = reinterpret_cast<const int4*>(S.dm) + 3 * sl;
 #pragma unroll
-  for (int k = 0; k < kHexW; ++k) {
-    const int2 e = S.dm[sl * kHexW + k];
-    on[k] = ((unsigned)e.y >> lane) & 1u;
-    xv[k] = on[k] ? __ldg(x + c + e.x) : 0.0f;
+  for (int q = 0; q < kHexW / 2; ++q) {
+    const int4 e = dm4[q];
+    on[2 * q] = ((unsigned)e.y >> lane) & 1u;
+    on[2 * q + 1] = ((unsigned)e.w >> lane) & 1u;
+    xv[2 * q] = on[2 * q] ? __ldg(x + c + e.x) : 0.0f;
+    xv[2 * q + 1] = on[2 * q + 1] ? __ldg(x + c + e.z) : 0.0f;
   }
   A so = (A)0, sn = (A)0;
   if (on[0]) so = first_term((A)__fmul_rn(a[0], xv[0]));
@@ -275,7 +284,10 @@ __device__ __forceinline__ bool hex_stream_tiles_pre(HexRing<SYM>& R, int n_tile
     const unsigned parity = (unsigned)(k / kStages) & 1u;
     const int c = t * kTileCells + tid;
     const auto aux = pre(c);
-    const bool got = mbar_wait(&R.bar[s], parity);
+    // one thread polls the stage's barrier; the block barrier then orders
+    // the completed copies before every thread's reads of the stage
+    bool got = true;
+    if (tid == 0) got = mbar_wait(&R.bar[s], parity);
     if (__syncthreads_or(!got)) {
       ok = false;
       break;
