@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kBlock)
 // last, partial tile are computed from global memory by one block.
 // SYM: coef is the owner-side half of a symmetric matrix (pack_sym_kernel).
 template <typename A, bool NEI_FIRST, bool SYM>
-__global__ void __launch_bounds__(kTileCells, 8)
+__global__ void __launch_bounds__(kTileCells, kStreamBlocksPerSM)
     amul_stream_kernel(gbf_layout L, const float* __restrict__ coef,
                        const float* __restrict__ diag, const float* __restrict__ x,
                        A* __restrict__ y, int n_tiles) {
@@ -217,7 +217,7 @@ extern "C" int gbf_amul_sym_f32(const gbf_layout* L, const float* coef_own, cons
   GBF_REQUIRE(layout_sym_ok(*L), "amul_sym: needs a hex 3+3 layout with a mirror table");
   GBF_REQUIRE(diag && x && y && coef_own, "amul_sym: NULL pointer");
   cudaStream_t s = as_stream(stream);
-  if (hex_stream_aligned(coef_own, x, diag, L->slot_dm) &&
+  if (kSymStaged && hex_stream_aligned(coef_own, x, diag, L->slot_dm) &&
       (reinterpret_cast<uintptr_t>(L->slot_mirror) & 15u) == 0) {
     launch_amul_stream<float, false, true>(L, coef_own, diag, x, y, s);
   } else {

@@ -33,9 +33,18 @@
 
 namespace gbf {
 
-constexpr int kTileCells = 256;
+// Cells per tile = threads per block of the staged kernels.
+#ifndef GBF_TILE_CELLS
+#define GBF_TILE_CELLS 256
+#endif
+constexpr int kTileCells = GBF_TILE_CELLS;
 constexpr int kTileSlices = kTileCells / 32;
 constexpr int kHexW = 6;
+// resident blocks per SM the staged kernels are compiled for (2048 threads)
+constexpr int kStreamBlocksPerSM = 2048 / kTileCells;
+// the symmetric form copies kTileSlices * kHexW mirror bytes per tile,
+// which a bulk copy can move only in multiples of 16 bytes
+constexpr bool kSymStaged = (kTileSlices * kHexW) % 16 == 0;
 constexpr int kStages = 3;
 constexpr int kWaitPolls = 1 << 20;
 
@@ -61,7 +70,7 @@ struct __align__(128) HexStageSym {
 constexpr unsigned kStageBytesSym = sizeof(float) * (kTileSlices * 3 * 32 + 2 * kTileCells) +
                                     sizeof(int2) * kTileSlices * kHexW +
                                     sizeof(int8_t) * kTileSlices * kHexW;
-static_assert(kStageBytesSym % 16 == 0, "bulk copies move multiples of 16 bytes");
+static_assert(!kSymStaged || kStageBytesSym % 16 == 0, "bulk copies move multiples of 16 bytes");
 
 template <bool SYM>
 struct HexStageOf {

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kBlock)
 // A wait that runs out records st->fault, which the last block turns into
 // GBF_DEVICE_TIMEOUT once every block has arrived.
 template <bool SYM>
-__global__ void __launch_bounds__(kTileCells, 8)
+__global__ void __launch_bounds__(kTileCells, kStreamBlocksPerSM)
     mp_ap_stream_kernel(gbf_layout L, const float* __restrict__ coef32, MixedVecs v,
                         int n_tiles) {
   pdl_wait();
@@ -427,7 +427,8 @@ extern "C" int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64,
   // staged K_ap: hex layout, 16-byte aligned coefficient / vector streams
   // (the workspace vectors are 256-byte aligned)
   const bool staged = hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm) &&
-                      (!sym || (reinterpret_cast<uintptr_t>(L->slot_mirror) & 15u) == 0);
+                      (!sym || (kSymStaged &&
+                                (reinterpret_cast<uintptr_t>(L->slot_mirror) & 15u) == 0));
   const int n_tiles = n / kTileCells;
   const long long tile_work = (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells;
   const int Ga = staged ? (sym ? wave_grid(mp_ap_stream_kernel<true>, kTileCells, tile_work)

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kBlock)
 // come from global memory.  A wait that runs out records st->fault, which
 // the last block turns into GBF_DEVICE_TIMEOUT.
 template <int PH>
-__global__ void __launch_bounds__(kTileCells, 8)
+__global__ void __launch_bounds__(kTileCells, kStreamBlocksPerSM)
     mb_amul_stream_kernel(gbf_layout L, const float* __restrict__ coef32, MbVecs v,
                           int n_tiles, int standard_omega) {
   pdl_wait();
