@@ -847,7 +847,11 @@ def run_next(args, rank, world, local):
                    device=dev)
     mm.diag, mm.lower, mm.upper = (torch.as_tensor(sd[k]) for k in ("diag", "lower", "upper"))
     b = torch.as_tensor(sd["b"]).to(dev)
-    g = GAMGSolver(tolerance=0.0, rel_tol=1e-3, max_iter=200)
+    # a fixed number of V-cycles: the reference's GAMG (aggregation, smoother,
+    # restriction -- reproduced here bit for bit) reduces the residual slowly
+    # on this system (run on the CPU: 60 cycles reach 1.2e-3 at 8^3 and
+    # 7.2e-3 at 16^3), so the leg reports time per cycle and the reduction
+    g = GAMGSolver(tolerance=0.0, rel_tol=0.0, max_iter=50)
     t0 = time.perf_counter()
     g(mm, b, torch.zeros_like(b))
     torch.cuda.synchronize()
@@ -856,9 +860,13 @@ def run_next(args, rank, world, local):
     x, it, res = g(mm, b, torch.zeros_like(b))
     torch.cuda.synchronize()
     t_g = time.perf_counter() - t0
+    h = g.last_info.residual_history
     out["gamg"] = {"n_cells": sd["n"], "levels": [lv.n_cells for lv in g.last_levels],
-                   "v_cycles": it, "converged": g.last_info.converged, "solve_s": t_g,
-                   "s_per_v_cycle": t_g / max(it, 1), "first_solve_incl_hierarchy_s": t_first}
+                   # the monitor's first check follows the first cycle (as the reference's)
+                   "v_cycles": it, "residual_reduction_after_cycle1": h[-1] / h[0],
+                   "reduction_per_cycle": (h[-1] / h[0]) ** (1.0 / max(len(h) - 1, 1)),
+                   "solve_s": t_g, "s_per_v_cycle": t_g / max(it, 1),
+                   "first_solve_incl_hierarchy_s": t_first}
     sm = SmoothSolver(tolerance=0.0, rel_tol=0.0, max_iter=5, smoother="GaussSeidel",
                       n_sweeps=2)
     sm(mm, b, torch.zeros_like(b))
