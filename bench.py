@@ -193,7 +193,7 @@ def design_bytes_ap(n: int, F: int, n_slices: int, sym: bool) -> int:
 # DRAM bytes (read + write) per launch of the FP32 K_ap at 256^3, from the
 # ncu launch list committed in profiles/mixed_pcg_256cube_launch_list.md
 # (dram__bytes_read.sum + dram__bytes_write.sum, mean over its 100 launches).
-NCU_TRAFFIC_AP_256 = {"sym": 494.1e6, "full": 629.0e6}
+NCU_TRAFFIC_AP_256 = {"sym": 494.1e6, "full": 626.1e6}
 
 
 def load_peaks() -> dict:
