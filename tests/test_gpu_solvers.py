@@ -307,3 +307,21 @@ def test_breakdown_and_nan_follow_the_reference(launch):
     assert not s.last_info.converged and not o.converged
     assert it == o.iterations
     assert np.isnan(res) and not torch.isfinite(x).all()
+
+
+def test_pbicgstab_fp64_x_within_1e12_of_oracle_when_converged_to_1e14():
+    """The FP64 path's x against the oracle's on an upwind convection-diffusion
+    system: at 1e-8 the two solves stop on different trajectories (their dot
+    products round in different orders), so x agrees only to ~cond * 1e-8;
+    both driven to 1e-14 converge to the same x within 1e-12 relative."""
+    from pyopenfoam_gb300.mesh.poisson import convection_diffusion
+
+    d = convection_diffusion(40, seed=1)
+    args = (d["owner"], d["neighbour"], d["diag"], d["lower"], d["upper"])
+    m = mat(d["n"], *args)
+    s = PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-14, max_iter=4000, omega="standard")
+    x, it, _ = s(m, torch.as_tensor(d["b"]), torch.zeros(d["n"], dtype=f64))
+    o = O.pbicgstab(*args, d["b"], np.zeros(d["n"]), O.dilu_build(*args), 0.0, 1e-14, 4000,
+                    threads=8, omega="standard")
+    assert s.last_info.converged and o.converged
+    assert relerr(x.cpu().numpy(), o.x) < 1e-12
