@@ -154,21 +154,16 @@ __global__ void __launch_bounds__(BS)
   }
 }
 
-template <int BS>
-__global__ void __launch_bounds__(BS)
-    bmp_update_kernel(BTiles T, double* __restrict__ x, BVecs v, double delta,
-                      gbf_solve_params P) {
-  const int tile = blockIdx.x;
-  const int s = __ldg(T.tile_sys + tile);
-  BState* st = v.st + s;
-  if (st->status != GBF_RUNNING) return;
-  __shared__ double sh[BS / 32];
-  const float alpha = (float)st->alpha;
-  const bool fold = st->fold_pending != 0;
-  BDFAcc arr, arz;
+// The cell loop of the batched K_upd for one tile.  FOLD is a template
+// parameter, not a branch inside the loop: a branch there is predicated, and
+// its FP64 conversion and add then issue on every cell of every iteration.
+template <int BS, bool FOLD>
+__device__ __forceinline__ void bmp_update_cells(const BTiles& T, int tile,
+                                                 double* __restrict__ x, const BVecs& v,
+                                                 float alpha, BDFAcc& arr, BDFAcc& arz) {
   for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < __ldg(T.tile_end + tile); c += BS) {
     const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
-    if (fold) {
+    if constexpr (FOLD) {
       x[c] += (double)xl;
       v.xlo[c] = 0.0f;
     } else {
@@ -181,6 +176,24 @@ __global__ void __launch_bounds__(BS)
     arr.add_prod(r, r);
     arz.add_prod(r, z);
   }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS)
+    bmp_update_kernel(BTiles T, double* __restrict__ x, BVecs v, double delta,
+                      gbf_solve_params P) {
+  const int tile = blockIdx.x;
+  const int s = __ldg(T.tile_sys + tile);
+  BState* st = v.st + s;
+  if (st->status != GBF_RUNNING) return;
+  __shared__ double sh[BS / 32];
+  const float alpha = (float)st->alpha;
+  const bool fold = st->fold_pending != 0;
+  BDFAcc arr, arz;
+  if (fold)
+    bmp_update_cells<BS, true>(T, tile, x, v, alpha, arr, arz);
+  else
+    bmp_update_cells<BS, false>(T, tile, x, v, alpha, arr, arz);
   const double rr = block_sum_df(arr, sh);
   const double rz = block_sum_df(arz, sh);
   if (threadIdx.x == 0) {

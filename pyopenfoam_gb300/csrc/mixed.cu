@@ -188,22 +188,17 @@ __global__ void __launch_bounds__(kTileCells, kStreamBlocksPerSM)
   }
 }
 
-// Four cells per thread with 128-bit loads and stores of the FP32 vectors
-// (the workspace vectors are 256-byte aligned); the n % 4 tail cells are
-// handled one per thread.
-__global__ void __launch_bounds__(kBlock)
-    mp_update_kernel(int n, double* __restrict__ x, MixedVecs v, double delta,
-                     gbf_solve_params P) {
-  pdl_wait();
-  pdl_launch_dependents();
-  if (v.st->status != GBF_RUNNING) return;
-  __shared__ double sh[kBlock / 32];
-  const int G = gridDim.x;
-  const float alpha = (float)v.st->alpha;
-  const bool fold = v.st->fold_pending != 0;
-  DFAcc arr, arz;
+// The cell loop of K_upd.  Four cells per thread with 128-bit loads and
+// stores of the FP32 vectors (the workspace vectors are 256-byte aligned);
+// the n % 4 tail cells one per thread.  FOLD is a template parameter, not a
+// branch inside the loop: a branch there is predicated, and its FP64
+// conversions and adds then issue on every cell of every iteration (GB300's
+// FP64 rate made that the kernel's bound).
+template <bool FOLD>
+__device__ __forceinline__ void mp_update_cells(int n, double* __restrict__ x, const MixedVecs& v,
+                                                float alpha, DFAcc& arr, DFAcc& arz) {
   const int n4 = n >> 2;
-  const int stride = G * blockDim.x;
+  const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   float4* __restrict__ xlo4 = reinterpret_cast<float4*>(v.xlo);
   float4* __restrict__ r4 = reinterpret_cast<float4*>(v.r);
@@ -218,7 +213,7 @@ __global__ void __launch_bounds__(kBlock)
     xl.y = fmaf(alpha, pp.y, xl.y);
     xl.z = fmaf(alpha, pp.z, xl.z);
     xl.w = fmaf(alpha, pp.w, xl.w);
-    if (fold) {
+    if constexpr (FOLD) {
       const int c = 4 * q;
       x[c] += (double)xl.x;
       x[c + 1] += (double)xl.y;
@@ -248,7 +243,7 @@ __global__ void __launch_bounds__(kBlock)
   }
   for (int c = 4 * n4 + tid; c < n; c += stride) {
     const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
-    if (fold) {
+    if constexpr (FOLD) {
       x[c] += (double)xl;
       v.xlo[c] = 0.0f;
     } else {
@@ -261,6 +256,23 @@ __global__ void __launch_bounds__(kBlock)
     arr.add_prod(r, r);
     arz.add_prod(r, z);
   }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    mp_update_kernel(int n, double* __restrict__ x, MixedVecs v, double delta,
+                     gbf_solve_params P) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x;
+  const float alpha = (float)v.st->alpha;
+  const bool fold = v.st->fold_pending != 0;
+  DFAcc arr, arz;
+  if (fold)
+    mp_update_cells<true>(n, x, v, alpha, arr, arz);
+  else
+    mp_update_cells<false>(n, x, v, alpha, arr, arz);
   const double rr = block_sum_df(arr, sh);
   const double rz = block_sum_df(arz, sh);
   if (threadIdx.x == 0) {

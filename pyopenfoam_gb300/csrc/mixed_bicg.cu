@@ -277,34 +277,31 @@ __global__ void __launch_bounds__(kBlock) mb_s_kernel(int n, MbVecs v) {
   }
 }
 
-// One cell of K_r: the new x32 (folded into x64 when `fold`) and r.
-__device__ __forceinline__ float mb_r_cell(double* __restrict__ x, int c, bool fold, int branch,
-                                           float omega, float s, float t, float z, float& xl) {
+// One cell of K_r: the new x32 (folded into x64 when FOLD) and r.
+template <bool FOLD>
+__device__ __forceinline__ float mb_r_cell(double* __restrict__ x, int c, int branch, float omega,
+                                           float s, float t, float z, float& xl) {
   float r = s;
   if (branch == 0) {
     xl = fmaf(omega, z, xl);
     r = fmaf(-omega, t, s);
   }
-  if (fold) {
+  if constexpr (FOLD) {
     x[c] += (double)xl;
     xl = 0.0f;
   }
   return r;
 }
 
-__global__ void __launch_bounds__(kBlock)
-    mb_r_kernel(int n, double* __restrict__ x, MbVecs v, double delta, gbf_solve_params P) {
-  pdl_wait();
-  pdl_launch_dependents();
-  if (v.st->status != GBF_RUNNING) return;
-  __shared__ double sh[kBlock / 32];
-  const int G = gridDim.x;
-  const int branch = v.st->branch;
-  const float omega = (float)v.st->omega;
-  const bool fold = v.st->fold_pending != 0;
-  DFAcc arr, artr;
+// The cell loop of K_r, four cells per thread with 128-bit accesses, then
+// the n % 4 tail.  FOLD is a template parameter, not a branch inside the
+// loop: a branch there is predicated, and its FP64 conversions and adds then
+// issue on every cell of every iteration (measured: FP64 pipe 62 % busy).
+template <bool FOLD>
+__device__ __forceinline__ void mb_r_cells(int n, double* __restrict__ x, const MbVecs& v,
+                                           int branch, float omega, DFAcc& arr, DFAcc& artr) {
   const int n4 = n >> 2;
-  const int stride = G * blockDim.x;
+  const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const float4* __restrict__ s4 = reinterpret_cast<const float4*>(v.s);
   const float4* __restrict__ t4 = reinterpret_cast<const float4*>(v.t);
@@ -316,10 +313,10 @@ __global__ void __launch_bounds__(kBlock)
     const float4 s = s4[q], t = t4[q], z = z4[q], rt = __ldg(rt4 + q);
     float4 xl = x4[q], r;
     const int c = 4 * q;
-    r.x = mb_r_cell(x, c, fold, branch, omega, s.x, t.x, z.x, xl.x);
-    r.y = mb_r_cell(x, c + 1, fold, branch, omega, s.y, t.y, z.y, xl.y);
-    r.z = mb_r_cell(x, c + 2, fold, branch, omega, s.z, t.z, z.z, xl.z);
-    r.w = mb_r_cell(x, c + 3, fold, branch, omega, s.w, t.w, z.w, xl.w);
+    r.x = mb_r_cell<FOLD>(x, c, branch, omega, s.x, t.x, z.x, xl.x);
+    r.y = mb_r_cell<FOLD>(x, c + 1, branch, omega, s.y, t.y, z.y, xl.y);
+    r.z = mb_r_cell<FOLD>(x, c + 2, branch, omega, s.z, t.z, z.z, xl.z);
+    r.w = mb_r_cell<FOLD>(x, c + 3, branch, omega, s.w, t.w, z.w, xl.w);
     r4[q] = r;
     x4[q] = xl;
     arr.add_prod(r.x, r.x);
@@ -333,12 +330,29 @@ __global__ void __launch_bounds__(kBlock)
   }
   for (int c = 4 * n4 + tid; c < n; c += stride) {
     float xl = v.xlo[c];
-    const float r = mb_r_cell(x, c, fold, branch, omega, v.s[c], v.t[c], v.z[c], xl);
+    const float r = mb_r_cell<FOLD>(x, c, branch, omega, v.s[c], v.t[c], v.z[c], xl);
     v.r[c] = r;
     v.xlo[c] = xl;
     arr.add_prod(r, r);
     artr.add_prod(__ldg(v.rt + c), r);
   }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    mb_r_kernel(int n, double* __restrict__ x, MbVecs v, double delta, gbf_solve_params P) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ double sh[kBlock / 32];
+  const int G = gridDim.x;
+  const int branch = v.st->branch;
+  const float omega = (float)v.st->omega;
+  const bool fold = v.st->fold_pending != 0;
+  DFAcc arr, artr;
+  if (fold)
+    mb_r_cells<true>(n, x, v, branch, omega, arr, artr);
+  else
+    mb_r_cells<false>(n, x, v, branch, omega, arr, artr);
   const double rr = block_sum_df(arr, sh);
   const double rtr = block_sum_df(artr, sh);
   if (threadIdx.x == 0) {
