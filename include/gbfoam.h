@@ -221,27 +221,39 @@ int gbf_amul_sym_f32(const gbf_layout* L, const float* coef_own, const float* di
                      const float* x, float* y, void* stream);
 
 /* ---- preconditioners -----------------------------------------------------
- * DICPreconditioner._build, solvers/preconditioners.py:88-133: level-
- * scheduled, one launch per wavefront level, each cell's subtractions in the
- * reference's face order; then d = clamp(|d|, 1e-30).  slot_coef must be the
- * (lower, upper) packing (the neighbour-side slots carry upper[f]).
- * level_ptr / level_cells are DEVICE copies of gbf_dic_schedule's output.  */
+ * Level-scheduled wavefronts (factorisations, apply_full sweeps and the
+ * Gauss-Seidel sweeps below) take `barrier`: device memory of
+ * gbf_wavefront_barrier_bytes() bytes, any contents (the call zeroes it).
+ * With it the whole schedule runs in one cooperative launch, levels
+ * separated by a bounded grid barrier; with NULL (or a device without
+ * cooperative launch) one kernel runs per level.  Same bits either way.  If
+ * a barrier wait runs out (2 s) the output is overwritten with NaN and
+ * gbf_wavefront_fault reports 1 (it synchronises the stream).  Calls must
+ * not share one barrier buffer while in flight.                           */
+size_t gbf_wavefront_barrier_bytes(void);
+int gbf_wavefront_fault(const void* barrier, int32_t* fault_h, void* stream);
+/* DICPreconditioner._build, solvers/preconditioners.py:88-133: level-
+ * scheduled, each cell's subtractions in the reference's face order; then
+ * d = clamp(|d|, 1e-30).  slot_coef must be the (lower, upper) packing (the
+ * neighbour-side slots carry upper[f]).  level_ptr / level_cells are DEVICE
+ * copies of gbf_dic_schedule's output.                                     */
 int gbf_dic_build_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
                       const int32_t* level_ptr, const int32_t* level_cells, int32_t n_levels,
-                      int32_t max_level_size, double* d_out, void* stream);
+                      int32_t max_level_size, double* d_out, void* barrier, void* stream);
 /* DILUPreconditioner._build, solvers/preconditioners.py:228-272, per face
  * level; lower/upper in face order.                                        */
 int gbf_dilu_build_f64(const gbf_layout* L, const double* lower, const double* upper,
                        const double* diag, const int32_t* level_ptr,
                        const int32_t* level_faces, int32_t n_levels, int32_t max_level_size,
-                       double* d_out, void* stream);
+                       double* d_out, void* barrier, void* stream);
 /* DIC/DILU apply(): z = r / d (preconditioners.py:151, :288).               */
 /* One triangular sweep of apply_full: for the faces of each level,
  * res[W] -= (coef[f] * res[R]) / d[R] if |d[R]| > 1e-30 (coef in face order:
  * upper for the forward sweeps, upper (DIC) or lower (DILU) backward).     */
 int gbf_sweep_f64(const gbf_layout* L, const double* coef, const double* d,
                   const int32_t* level_ptr, const int32_t* level_faces, int32_t n_levels,
-                  int32_t max_level_size, int32_t reverse, double* res, void* stream);
+                  int32_t max_level_size, int32_t reverse, double* res, void* barrier,
+                  void* stream);
 int gbf_diag_apply_f64(int32_t n, const double* r, const double* d, double* z, void* stream);
 
 /* ---- Krylov solvers --------------------------------------------------------
@@ -410,7 +422,7 @@ int gbf_gs_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
 int gbf_gauss_seidel_f64(const gbf_layout* L, const double* slot_coef, const double* diag,
                          const double* b, const int32_t* level_ptr, const int32_t* level_cells,
                          const int32_t* level_ptr_h, int32_t n_levels, double omega,
-                         int32_t relax, double* x, void* stream);
+                         int32_t relax, double* x, void* barrier, void* stream);
 /* r = b - A x, A x bitwise LduMatrix.Ax (core/ldu_matrix.py:172-217); the
  * residual of every smoother and of the smoothing solvers.                 */
 int gbf_residual_f64(const gbf_layout* L, const double* slot_coef, const double* diag,

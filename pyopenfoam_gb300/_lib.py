@@ -137,7 +137,7 @@ EXPORTED: dict[str, tuple] = {
     "gbf_gs_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp,
                                        _P(_c_i32), _P(_c_i32)]),
     "gbf_gauss_seidel_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32,
-                                            _c_dbl, _c_i32, _c_vp, _c_vp]),
+                                            _c_dbl, _c_i32, _c_vp, _c_vp, _c_vp]),
     "gbf_residual_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_relax_f64": (ctypes.c_int, [_c_i32, _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_norm2_workspace_bytes": (_c_size, []),
@@ -163,7 +163,7 @@ EXPORTED: dict[str, tuple] = {
     "gbf_sweep_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
                                           _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_sweep_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_i32,
-                                     _c_vp, _c_vp]),
+                                     _c_vp, _c_vp, _c_vp]),
     "gbf_boundary_lists": (ctypes.c_int, [_c_i32, _c_i32, _c_i32, _c_vp, _c_vp, _c_vp]),
     "gbf_laplacian_assemble_f64": (ctypes.c_int, [_L, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                                   _c_i32, _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp,
@@ -192,8 +192,12 @@ EXPORTED: dict[str, tuple] = {
     "gbf_amul_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
     "gbf_amul_f32_f64out": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
     "gbf_amul_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
-    "gbf_dic_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp, _c_vp]),
-    "gbf_dilu_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp, _c_vp]),
+    "gbf_wavefront_barrier_bytes": (_c_size, []),
+    "gbf_wavefront_fault": (ctypes.c_int, [_c_vp, _P(_c_i32), _c_vp]),
+    "gbf_dic_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
+                                         _c_vp, _c_vp]),
+    "gbf_dilu_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32,
+                                          _c_vp, _c_vp, _c_vp]),
     "gbf_diag_apply_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pcg_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_pcg_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
@@ -260,3 +264,20 @@ def ptr(t: torch.Tensor | None) -> int | None:
 def stream_ptr(device: torch.device) -> int:
     """cudaStream_t of torch's current stream on ``device``."""
     return torch.cuda.current_stream(device).cuda_stream
+
+
+def wavefront_barrier(device) -> torch.Tensor:
+    """Device memory for the grid barrier of one cooperative wavefront call
+    (gbf_wavefront_barrier_bytes; the call zeroes it)."""
+    return torch.empty(int(lib().gbf_wavefront_barrier_bytes()), dtype=torch.uint8,
+                       device=device)
+
+
+def check_wavefront(barrier, what: str, device) -> None:
+    """Raises if the cooperative wavefront call that used `barrier` gave up
+    on a grid-barrier wait (synchronises the stream)."""
+    fault = ctypes.c_int32(0)
+    check(lib().gbf_wavefront_fault(barrier.data_ptr(), ctypes.byref(fault), stream_ptr(device)),
+          "gbf_wavefront_fault")
+    if fault.value:
+        raise RuntimeError(f"{what}: a grid-barrier wait ran out; the result is invalid")

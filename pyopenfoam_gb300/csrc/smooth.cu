@@ -20,20 +20,15 @@
 #include <math.h>
 
 #include "amul.cuh"
+#include "wavefront.cuh"
 
 namespace gbf {
 
 template <bool RELAX>
-__global__ void __launch_bounds__(kBlock)
-    gs_level_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
-                    const double* __restrict__ b, const int32_t* __restrict__ level_ptr,
-                    const int32_t* __restrict__ level_cells, int level, double omega,
-                    double* x) {
-  const int start = __ldg(level_ptr + level);
-  const int count = __ldg(level_ptr + level + 1) - start;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const int c = __ldg(level_cells + start + t);
+__device__ __forceinline__ void gs_cell(const gbf_layout& L, const double* __restrict__ coef,
+                                        const double* __restrict__ diag,
+                                        const double* __restrict__ b, int c, double omega,
+                                        double* x) {
   const double dc = __ldg(diag + c);
   const double xc = __ldcg(x + c);
   double row = __dmul_rn(dc, xc);
@@ -62,6 +57,31 @@ __global__ void __launch_bounds__(kBlock)
     const double nv = __ddiv_rn(__dsub_rn(__ldg(b + c), off), dc);
     x[c] = RELAX ? __dadd_rn(xc, __dmul_rn(omega, __dsub_rn(nv, xc))) : nv;
   }
+}
+
+template <bool RELAX>
+__global__ void __launch_bounds__(kBlock)
+    gs_level_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
+                    const double* __restrict__ b, const int32_t* __restrict__ level_ptr,
+                    const int32_t* __restrict__ level_cells, int level, double omega,
+                    double* x) {
+  const int start = __ldg(level_ptr + level);
+  const int count = __ldg(level_ptr + level + 1) - start;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) gs_cell<RELAX>(L, coef, diag, b, __ldg(level_cells + start + t), omega, x);
+}
+
+// A whole Gauss-Seidel sweep in one cooperative launch (wavefront.cuh).
+template <bool RELAX>
+__global__ void __launch_bounds__(kBlock)
+    gs_coop_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
+                   const double* __restrict__ b, const int32_t* __restrict__ level_ptr,
+                   const int32_t* __restrict__ level_cells, int n_levels, double omega,
+                   double* x, GridBarrier* bar) {
+  if (!run_levels(bar, level_ptr, n_levels, [&](int i) {
+        gs_cell<RELAX>(L, coef, diag, b, __ldg(level_cells + i), omega, x);
+      }))
+    poison(x, L.n_cells);
 }
 
 // r = b - A x with A x in the reference's order (cell_amul).
@@ -172,7 +192,7 @@ extern "C" int gbf_gauss_seidel_f64(const gbf_layout* L, const double* coef, con
                                     const double* b, const int32_t* level_ptr,
                                     const int32_t* level_cells, const int32_t* level_ptr_h,
                                     int32_t n_levels, double omega, int32_t relax, double* x,
-                                    void* stream) {
+                                    void* barrier, void* stream) {
   ::gbf::NvtxScope nvtx_("gbf_gauss_seidel_f64");
   int rc = check_layout(L);
   if (rc) return rc;
@@ -181,6 +201,22 @@ extern "C" int gbf_gauss_seidel_f64(const gbf_layout* L, const double* coef, con
                   (L->n_faces == 0 || coef),
               "gauss_seidel: NULL pointer or bad level count");
   cudaStream_t s = as_stream(stream);
+  int max_level = 0;
+  for (int l = 0; l < n_levels; ++l) {
+    const int cnt = level_ptr_h[l + 1] - level_ptr_h[l];
+    if (cnt > max_level) max_level = cnt;
+  }
+  const void* coop = relax ? (const void*)gs_coop_kernel<true> : (const void*)gs_coop_kernel<false>;
+  const int gc = (barrier && n_levels > 0) ? wavefront_grid(coop, kBlock, max_level, 2) : 0;
+  if (gc > 0) {
+    gbf_layout Lc = *L;
+    int nl = n_levels;
+    GridBarrier* bar = static_cast<GridBarrier*>(barrier);
+    void* args[] = {&Lc, (void*)&coef, (void*)&diag, (void*)&b, (void*)&level_ptr,
+                    (void*)&level_cells, &nl, &omega, &x, &bar};
+    GBF_CHECK_CUDA(launch_wavefront(coop, gc, args, barrier, s));
+    return GBF_OK;
+  }
   for (int l = 0; l < n_levels; ++l) {
     const int cnt = level_ptr_h[l + 1] - level_ptr_h[l];
     if (cnt <= 0) continue;

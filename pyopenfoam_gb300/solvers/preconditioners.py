@@ -97,13 +97,15 @@ class DICPreconditioner(_DiagonalFactor):
             return d.to(self._dtype)
         sched = topo.dic_schedule()
         coef = m64.packed()
+        bar = _lib.wavefront_barrier(self._device)
         _lib.check(
             _lib.lib().gbf_dic_build_f64(topo.layout_ref, coef.data_ptr(), diag.data_ptr(),
                                          sched.ptr.data_ptr(), sched.items.data_ptr(),
                                          sched.n_levels, sched.max_level_size, d.data_ptr(),
-                                         _lib.stream_ptr(self._device)),
+                                         bar.data_ptr(), _lib.stream_ptr(self._device)),
             "gbf_dic_build_f64",
         )
+        _lib.check_wavefront(bar, "gbf_dic_build_f64", self._device)
         return d.to(self._dtype)
 
     def apply_full(self, r: torch.Tensor) -> torch.Tensor:
@@ -126,14 +128,16 @@ class DILUPreconditioner(_DiagonalFactor):
         if self._matrix.n_cells == 0:
             return d.to(self._dtype)
         sched = topo.dilu_schedule()
+        bar = _lib.wavefront_barrier(self._device)
         _lib.check(
             _lib.lib().gbf_dilu_build_f64(topo.layout_ref, lower.data_ptr(), upper.data_ptr(),
                                           diag.data_ptr(), sched.ptr.data_ptr(),
                                           sched.items.data_ptr(), sched.n_levels,
-                                          sched.max_level_size, d.data_ptr(),
+                                          sched.max_level_size, d.data_ptr(), bar.data_ptr(),
                                           _lib.stream_ptr(self._device)),
             "gbf_dilu_build_f64",
         )
+        _lib.check_wavefront(bar, "gbf_dilu_build_f64", self._device)
         return d.to(self._dtype)
 
     def apply_full(self, r: torch.Tensor) -> torch.Tensor:

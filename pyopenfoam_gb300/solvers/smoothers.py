@@ -79,7 +79,8 @@ def gs_sweep(matrix: LduMatrix, x: torch.Tensor, b: torch.Tensor, reverse: bool 
     _lib.check(_lib.lib().gbf_gauss_seidel_f64(
         topo.layout_ref, coef.data_ptr(), matrix.diag.data_ptr(), b.data_ptr(), sch.ptr.data_ptr(),
         sch.cells.data_ptr(), sch.ptr_h.ctypes.data, sch.n_levels, float(omega), int(relax),
-        x.data_ptr(), _lib.stream_ptr(matrix.device)), "gbf_gauss_seidel_f64")
+        x.data_ptr(), _lib.wavefront_barrier(matrix.device).data_ptr(),
+        _lib.stream_ptr(matrix.device)), "gbf_gauss_seidel_f64")
 
 
 def residual(matrix: LduMatrix, b: torch.Tensor, x: torch.Tensor,

@@ -30,15 +30,19 @@ def _apply_full(pre, r: torch.Tensor, lower_only: bool, back_coef: torch.Tensor)
     if m.n_cells == 0:
         return z
     fwd = topo.sweep_schedule(False, lower_only)
+    # one barrier buffer per sweep: the two sweeps are stream-ordered, but a
+    # buffer is never shared between calls that could be in flight together
     _lib.check(L.gbf_sweep_f64(topo.layout_ref, m.upper.data_ptr(), d.data_ptr(),
                                fwd.ptr.data_ptr(), fwd.items.data_ptr(), fwd.n_levels,
-                               fwd.max_level_size, 0, z.data_ptr(), st), "gbf_sweep_f64")
+                               fwd.max_level_size, 0, z.data_ptr(),
+                               _lib.wavefront_barrier(m.device).data_ptr(), st), "gbf_sweep_f64")
     _lib.check(L.gbf_diag_apply_f64(m.n_cells, z.data_ptr(), d.data_ptr(), z.data_ptr(), st),
                "gbf_diag_apply_f64")
     bwd = topo.sweep_schedule(True, lower_only)
     _lib.check(L.gbf_sweep_f64(topo.layout_ref, back_coef.data_ptr(), d.data_ptr(),
                                bwd.ptr.data_ptr(), bwd.items.data_ptr(), bwd.n_levels,
-                               bwd.max_level_size, 1, z.data_ptr(), st), "gbf_sweep_f64")
+                               bwd.max_level_size, 1, z.data_ptr(),
+                               _lib.wavefront_barrier(m.device).data_ptr(), st), "gbf_sweep_f64")
     return z
 
 
