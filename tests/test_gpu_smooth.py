@@ -71,3 +71,75 @@ def test_smooth_solver_converges_and_factory():
     assert isinstance(create_solver("smoothsolver", smoother="DIC"), SmoothSolver)
     with pytest.raises(ValueError):
         SmoothSolver(smoother="Jacobi")(m, b, torch.zeros_like(b))
+
+
+@pytest.mark.parametrize("N,perm", [(24, True), (40, False)])
+def test_wavefront_single_launch_matches_per_level_launches(N, perm):
+    """The cooperative single-launch wavefronts (barrier memory given) and
+    the per-level launches (NULL) give the same bits: DIC and DILU
+    factorisations, both apply_full sweeps, Gauss-Seidel forward and
+    backward (plain and relaxed)."""
+    from pyopenfoam_gb300 import _lib
+    from pyopenfoam_gb300.solvers.smoothers import _gs_schedule
+
+    c = random_ldu(N, seed=17, permute_faces=perm)
+    m = LduMatrix(c["n"], torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(k) for k in (c["diag"], c["lower"], c["upper"]))
+    L = _lib.lib()
+    topo, coef, st = m.topology(), m.packed(), _lib.stream_ptr(m.device)
+    n = m.n_cells
+
+    def both(fn):
+        out = []
+        for bar in (None, _lib.wavefront_barrier(m.device)):
+            out.append(fn(None if bar is None else bar.data_ptr()))
+            if bar is not None:
+                _lib.check_wavefront(bar, "wavefront", m.device)
+        return out
+
+    def dic(b):
+        d = torch.empty(n, dtype=torch.float64, device="cuda")
+        s = topo.dic_schedule()
+        _lib.check(L.gbf_dic_build_f64(topo.layout_ref, coef.data_ptr(), m.diag.data_ptr(),
+                                       s.ptr.data_ptr(), s.items.data_ptr(), s.n_levels,
+                                       s.max_level_size, d.data_ptr(), b, st))
+        return d.cpu().numpy()
+
+    def dilu(b):
+        d = torch.empty(n, dtype=torch.float64, device="cuda")
+        s = topo.dilu_schedule()
+        _lib.check(L.gbf_dilu_build_f64(topo.layout_ref, m.lower.data_ptr(), m.upper.data_ptr(),
+                                        m.diag.data_ptr(), s.ptr.data_ptr(), s.items.data_ptr(),
+                                        s.n_levels, s.max_level_size, d.data_ptr(), b, st))
+        return d.cpu().numpy()
+
+    for fn in (dic, dilu):
+        a, b = both(fn)
+        assert _eq(a, b), fn.__name__
+    pd = torch.as_tensor(dilu(None)).cuda()
+    for reverse in (0, 1):
+        for lower_only in (True, False):
+            def sweep(b, reverse=reverse, lower_only=lower_only):
+                s = topo.sweep_schedule(bool(reverse), lower_only)
+                res = torch.as_tensor(c["r"]).cuda().clone()
+                _lib.check(L.gbf_sweep_f64(topo.layout_ref, m.upper.data_ptr(), pd.data_ptr(),
+                                           s.ptr.data_ptr(), s.items.data_ptr(), s.n_levels,
+                                           s.max_level_size, reverse, res.data_ptr(), b, st))
+                return res.cpu().numpy()
+            a, b = both(sweep)
+            assert _eq(a, b), ("sweep", reverse, lower_only)
+    rhs = torch.as_tensor(c["r"]).cuda()
+    for reverse in (False, True):
+        for relax, omega in ((0, 1.0), (1, 0.8)):
+            def gs(b, reverse=reverse, relax=relax, omega=omega):
+                sch = _gs_schedule(m, reverse)
+                x = torch.as_tensor(c["x"]).cuda().clone()
+                _lib.check(L.gbf_gauss_seidel_f64(topo.layout_ref, coef.data_ptr(),
+                                                  m.diag.data_ptr(), rhs.data_ptr(),
+                                                  sch.ptr.data_ptr(), sch.cells.data_ptr(),
+                                                  sch.ptr_h.ctypes.data, sch.n_levels, omega,
+                                                  relax, x.data_ptr(), b, st))
+                return x.cpu().numpy()
+            a, b = both(gs)
+            assert _eq(a, b), ("gs", reverse, relax)
