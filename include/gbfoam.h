@@ -560,7 +560,7 @@ int gbf_face_interp_f64(int32_t n_faces, int32_t n_internal, const int32_t* owne
                         double* delta, void* stream);
 
 /* ---- mixed precision -------------------------------------------------------
- * No reference counterpart (the north-star's precision pattern): PCG whose
+ * No reference counterpart (FP32 inner iterations, FP64 outer accuracy): PCG whose
  * Krylov recurrence, Amul (coef32 = FP32 packing of the FP64 matrix; with
  * coef32_sym = 1 the owner-side half of a symmetric matrix from
  * gbf_pack_sym_f64_to_f32, which needs L->slot_mirror and a hex 3+3 layout

@@ -1,8 +1,8 @@
 // Mixed-precision PCG: FP32 inner iterations with FP64 reliable updates.
 //
-// No reference counterpart: this is the precision pattern of the north-star
-// (FP32 Amul / preconditioner / vectors, FP64 outer residual r = b - A x,
-// FP64 solution update and FP64 dot-product reductions).  It follows the
+// No reference counterpart: the precision pattern of this solver is FP32
+// Amul / preconditioner / vectors, with an FP64 outer residual r = b - A x,
+// FP64 solution update and FP64 dot-product reductions.  It follows the
 // reliable-update scheme of Sleijpen & van der Vorst ("Reliable updated
 // residuals in hybrid Bi-CG methods", Computing 56, 1996), in the mixed
 // precision form of Clark et al. (2010): the Krylov recurrence runs in
