@@ -72,14 +72,16 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
-    p.add_argument("--workload", choices=["c3", "c1", "c2", "c4", "c5", "next"], default="c3",
-                   help="c3 (default, the headline): 256^3 mixed vs FP64 PCG; c1: 32^3 "
-                        "PCG+DIC to 1e-6; c2: 128^3 jittered convection-diffusion with "
-                        "PBiCGStab+DILU; c5: adjoint gradient of 20 implicit steps at 96^3; "
+    p.add_argument("--workload", choices=["poisson256", "poisson32", "convdiff128", "batch64",
+                                          "adjoint96", "next"], default="poisson256",
+                   help="poisson256 (default, the headline): 256^3 mixed vs FP64 PCG; "
+                        "poisson32: 32^3 PCG+DIC to 1e-6; convdiff128: 128^3 jittered "
+                        "convection-diffusion with PBiCGStab+DILU; batch64: 64 uneven Poisson "
+                        "systems, batched; adjoint96: adjoint gradient of 20 implicit steps at 96^3; "
                         "next: geometry, correctors, GAMG and smoothers")
-    p.add_argument("--c2-solvers", default="standard,reference,mixed,standard_1e-10,mixed_1e-10",
-                   help="c2: comma-separated solver legs to run")
-    p.add_argument("--fd-faces", type=int, default=32, help="c5: faces checked by central "
+    p.add_argument("--convdiff-legs", default="standard,reference,mixed,standard_1e-10,mixed_1e-10",
+                   help="convdiff128: comma-separated solver legs to run")
+    p.add_argument("--fd-faces", type=int, default=32, help="adjoint96: faces checked by central "
                                                             "differences")
     return p.parse_args()
 
@@ -495,7 +497,7 @@ def _line(args, world, metric, value, unit, hib, workload, extra, **kw):
     print(json.dumps(d), flush=True)
 
 
-def run_c1(args, rank, world, local):
+def run_poisson32(args, rank, world, local):
     """32^3 Poisson, PCG+DIC to 1e-6 relative (the reference's CPU case)."""
     from oracle import oracle as O
     from pyopenfoam_gb300 import PCGSolver
@@ -525,7 +527,7 @@ def run_c1(args, rank, world, local):
         o = O.pcg(own, nei, sysd["diag"], sysd["lower"], sysd["upper"], sysd["b"],
                   np.zeros(sysd["n"]), pd, 0.0, 1e-6, 1000, threads=len(os.sched_getaffinity(0)))
         cpu = time.perf_counter() - t0
-        _line(args, world, "config 1: 32^3 Poisson PCG+DIC to 1e-6 relative residual, time",
+        _line(args, world, "32^3 Poisson PCG+DIC to 1e-6 relative residual, time",
               gpu, "s", False,
               {"workload": "32^3 Poisson (unit-cube hex, x0 fixed value), PCG+DIC to 1e-6",
                "n_cells": sysd["n"]},
@@ -536,8 +538,8 @@ def run_c1(args, rank, world, local):
                             "kind": "port", "sample": "full solve"})
 
 
-def c2_system(N: int, dev):
-    """Config 2: N^3 hex mesh with +-20 % jitter (seed 1), face diffusivity
+def convdiff_system(N: int, dev):
+    """The convection-diffusion system: N^3 hex mesh with +-20 % jitter (seed 1), face diffusivity
     LogNormal(0, 1), upwind convection of u = (1, 0.5, 0.25) scaled to a cell
     Peclet number of ~10, fixed value on x = 0.  The flux uses the nominal
     (unjittered) face areas, so it is positive on every internal face and
@@ -570,7 +572,7 @@ def c2_system(N: int, dev):
     return mesh, A, torch.as_tensor(b).to(dev)
 
 
-def run_c2(args, rank, world, local):
+def run_convdiff128(args, rank, world, local):
     """128^3 jittered convection-diffusion, PBiCGStab+DILU to 1e-8."""
     import ctypes
 
@@ -580,7 +582,7 @@ def run_c2(args, rank, world, local):
     dev = torch.device("cuda", local)
     N = 128 if args.n == 256 else args.n
     t0 = time.perf_counter()
-    mesh, A, b = c2_system(N, dev)
+    mesh, A, b = convdiff_system(N, dev)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     L = _lib.lib()
@@ -608,10 +610,10 @@ def run_c2(args, rank, world, local):
         "mixed_1e-10": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10,
                                                      max_iter=4000),
     }
-    wanted = [k for k in args.c2_solvers.split(",") if k]
+    wanted = [k for k in args.convdiff_legs.split(",") if k]
     for key in wanted:
         if key not in solvers:
-            raise SystemExit(f"--c2-solvers: unknown leg {key!r} (known: {', '.join(solvers)})")
+            raise SystemExit(f"--convdiff-legs: unknown leg {key!r} (known: {', '.join(solvers)})")
     for key, s in solvers.items():
         if key not in wanted:
             continue
@@ -673,7 +675,7 @@ def run_c2(args, rank, world, local):
                  "mixed_1e-10": "mixed_to_1e-10"}
         extra = {names[k]: v for k, v in res.items()}
         extra["setup_s"] = t_setup
-        _line(args, world, f"config 2: 128^3 jittered convection-diffusion, PBiCGStab+DILU "
+        _line(args, world, f"128^3 jittered convection-diffusion, PBiCGStab+DILU "
               f"({head} leg) to 1e-{10 if head.endswith('1e-10') else 8} relative, time",
               res[head]["s"], "s", False,
               {"workload": f"{N}^3 hex, +-20% jitter, log-normal gamma, upwind Pe~10, outflow "
@@ -681,7 +683,7 @@ def run_c2(args, rank, world, local):
                "n_faces": mesh.n_internal_faces}, extra, cpu_baseline=cpu)
 
 
-def run_c4(args, rank, world, local):
+def run_batch64(args, rank, world, local):
     """64 independent Poisson systems (sides U{16..96}, seed 3), mixed
     FP32/FP64 refined PCG+DIC to 1e-8: one batched solve vs 64 sequential
     single-system solves."""
@@ -722,7 +724,7 @@ def run_c4(args, rank, world, local):
     torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
     if rank == 0:
-        _line(args, world, "config 4: 64 uneven Poisson systems, batched mixed PCG+DIC to 1e-8, "
+        _line(args, world, "64 uneven Poisson systems, batched mixed PCG+DIC to 1e-8, "
               "time", t_batch, "s", False,
               {"workload": "64 uniform hex Poisson systems, sides U{16..96} (seed 3), gamma "
                            "LogNormal(0,0.5), mixed FP32/FP64 refined to 1e-8",
@@ -735,7 +737,7 @@ def run_c4(args, rank, world, local):
                "setup_s": t_setup, "first_solve_incl_autotune_s": t_tune})
 
 
-def run_c5(args, rank, world, local):
+def run_adjoint96(args, rank, world, local):
     """Adjoint gradient through 20 implicit diffusion steps at 96^3."""
     from pyopenfoam_gb300 import PCGSolver
     from pyopenfoam_gb300.differentiable.unrolled import UnrolledImplicitDiffusion
@@ -773,7 +775,7 @@ def run_c5(args, rank, world, local):
     t_fd = time.perf_counter() - t0
     f_s, b_s = statistics.median(fw), statistics.median(bw)
     if rank == 0:
-        _line(args, world, "config 5: adjoint gradient of 20 implicit steps (96^3), "
+        _line(args, world, "adjoint gradient of 20 implicit steps (96^3), "
               "forward + backward time", f_s + b_s, "s", False,
               {"workload": f"{N}^3 uniform hex, dt=1e-3, 20 steps, gamma ~ LogNormal(0,1) "
                            "per face, checkpoint every 5", "n_cells": mesh.n_cells,
@@ -903,14 +905,14 @@ def main():
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
-    elif args.workload == "c1":
-        run_c1(args, rank, world, local)
-    elif args.workload == "c2":
-        run_c2(args, rank, world, local)
-    elif args.workload == "c4":
-        run_c4(args, rank, world, local)
-    elif args.workload == "c5":
-        run_c5(args, rank, world, local)
+    elif args.workload == "poisson32":
+        run_poisson32(args, rank, world, local)
+    elif args.workload == "convdiff128":
+        run_convdiff128(args, rank, world, local)
+    elif args.workload == "batch64":
+        run_batch64(args, rank, world, local)
+    elif args.workload == "adjoint96":
+        run_adjoint96(args, rank, world, local)
     elif args.workload == "next":
         run_next(args, rank, world, local)
     else:

@@ -2,7 +2,7 @@
 
 Every generator is deterministic across platforms: indices are integer
 arithmetic, random values come from ``numpy.random.default_rng`` (PCG64), and
-the config-1 coefficients are exact powers of two.  The jittered-mesh case
+the 32^3 Poisson coefficients are exact powers of two.  The jittered-mesh case
 stores its geometry in the fixture, so no test depends on floating-point
 geometry being bit-identical across machines.
 """
@@ -21,7 +21,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspa
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "reference_outputs.npz")
 JITTER_FIXTURE = os.path.join(HERE, "jitter6_inputs.npz")
-C2SIZE_FIXTURE = os.path.join(HERE, "reference_c2size.npz")
+LDU128_FIXTURE = os.path.join(HERE, "reference_ldu128.npz")
 
 
 def sha(a: np.ndarray) -> str:
@@ -57,7 +57,7 @@ def random_ldu(N: int, seed: int = 5, permute_faces: bool = False) -> dict:
 
 
 def c1_poisson(N: int = 32, seed: int = 0) -> dict:
-    """Config-1 system (see pyopenfoam_gb300.mesh.poisson.hex_poisson)."""
+    """The 32^3 Poisson system (see pyopenfoam_gb300.mesh.poisson.hex_poisson)."""
     return hex_poisson(N, seed)
 
 
@@ -116,7 +116,7 @@ def jitter_case(N: int = 6, seed: int = 1, store: bool = True):
 
 
 def unroll_case(N: int = 10, dt: float = 1e-3, steps: int = 20, seed: int = 4) -> dict:
-    """Config-5 structure at a small size: uniform N^3 mesh (fixed value on
+    """The 96^3 adjoint workload's structure at a small size: uniform N^3 mesh (fixed value on
     x0), per-face diffusivity gamma ~ LogNormal(0, 1), x0 ~ U[0, 1], and a
     target produced by the same 20 implicit steps with a second draw gamma'
     (computed here with the oracle restatement: fvm.laplacian + PCG)."""

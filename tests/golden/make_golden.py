@@ -9,7 +9,7 @@ Run in a checkout that has the reference project next to it:
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --smooth
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --gamg
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --pbicg
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --c2size
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --ldu128
 
 It imports the reference's own classes (``pyfoam.core.ldu_matrix``,
 ``pyfoam.solvers.*``, ``pyfoam.discretisation.operators.fvm``,
@@ -77,7 +77,7 @@ def main(ref_root: str) -> None:
             out[f"{name}_dilu_full_sha"] = sha(DILUPreconditioner(m).apply_full(r).numpy())
         print(name, "done", flush=True)
 
-    # ---- 2. Config-1 Poisson (32^3, Dirichlet x=0), PCG+DIC to rel 1e-6
+    # ---- 2. 32^3 Poisson (Dirichlet x=0), PCG+DIC to rel 1e-6
     c1 = c1_poisson(32)
     m = ldu(c1["n"], c1["owner"], c1["neighbour"], c1["diag"], c1["lower"], c1["upper"])
     out["c1_coeff_sha"] = sha(np.concatenate([c1["diag"], c1["lower"], c1["upper"]]))
@@ -490,13 +490,13 @@ def gamg(ref_root: str) -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
-def c2size(ref_root: str) -> None:
-    """Config-2 size (128^3 hex topology, 2,097,152 cells, 6,242,304 faces):
+def ldu128(ref_root: str) -> None:
+    """128^3 hex topology (2,097,152 cells, 6,242,304 faces):
     Ax, Ax_T, FP32 Ax, the DIC and DILU factorised diagonals
     (core/ldu_matrix.py:172-258, solvers/preconditioners.py:88-133,228-272)
     and PBiCGStab+DILU (solvers/pbicgstab.py:103-239) on a seeded random LDU
     system whose coefficients are exact draws of default_rng (bit-identical
-    on every machine) -> reference_c2size.npz.  Bitwise results as SHA-256;
+    on every machine) -> reference_ldu128.npz.  Bitwise results as SHA-256;
     the solve as its iteration count, residual history and every 97th entry
     of x."""
     sys.path.insert(0, os.path.join(ref_root, "src"))
@@ -536,7 +536,7 @@ def c2size(ref_root: str) -> None:
     out["bicg_history"] = np.array(info.residual_history)
     out["bicg_x97"] = xs.numpy()[::97].copy()
     print("PBiCGStab", info.iterations, info.converged, time.time() - t0, flush=True)
-    path = os.path.join(HERE, "reference_c2size.npz")
+    path = os.path.join(HERE, "reference_ldu128.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
 
@@ -556,7 +556,7 @@ if __name__ == "__main__":
         gamg(root)
     elif "--pbicg" in sys.argv:
         pbicg(root)
-    elif "--c2size" in sys.argv:
-        c2size(root)
+    elif "--ldu128" in sys.argv:
+        ldu128(root)
     else:
         main(root)

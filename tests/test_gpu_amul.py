@@ -126,7 +126,7 @@ def test_argument_errors_like_reference():
 
 @pytest.mark.parametrize("N", [128, 256])
 def test_full_size_bitwise_against_oracle(N):
-    """Config-2/3 sizes: every cell of A x equals the oracle's (threaded
+    """128^3 and 256^3: every cell of A x equals the oracle's (threaded
     per-cell gather in reference order) bit for bit."""
     n, own, nei = hex_faces(N)
     rng = np.random.default_rng(N)

@@ -1,5 +1,5 @@
-"""Config-2 size (128^3 hex topology, 2,097,152 cells, 6,242,304 faces)
-against the reference's own outputs (tests/golden/reference_c2size.npz,
+"""128^3 hex topology (2,097,152 cells, 6,242,304 faces)
+against the reference's own outputs (tests/golden/reference_ldu128.npz,
 made by running the reference on the same seeded system): Amul, Ax_T and
 FP32 Amul bitwise, the DIC and DILU factorised diagonals bitwise, and
 PBiCGStab+DILU against the reference's residual checks, check count and
@@ -11,11 +11,11 @@ import torch
 
 from pyopenfoam_gb300 import (DICPreconditioner, DILUPreconditioner, LduMatrix,
                               PBiCGSTABSolver)
-from tests.golden.cases import C2SIZE_FIXTURE, random_ldu, sha
-from tests.test_oracle_pins import check_c2size_bicgstab
+from tests.golden.cases import LDU128_FIXTURE, random_ldu, sha
+from tests.test_oracle_pins import check_ldu128_bicgstab
 
 pytestmark = pytest.mark.gpu
-R = np.load(C2SIZE_FIXTURE)
+R = np.load(LDU128_FIXTURE)
 
 
 @pytest.fixture(scope="module")
@@ -49,6 +49,6 @@ def test_pbicgstab_dilu_against_reference(case):
     m = mat(case)
     s = PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=200, preconditioner="DILU")
     x, it, res = s(m, torch.as_tensor(case["r"]), torch.zeros(case["n"], dtype=torch.float64))
-    # the bar and why it is not bitwise: check_c2size_bicgstab's docstring
-    check_c2size_bicgstab(s.last_info.converged, it, s.last_info.residual_history,
+    # the bar and why it is not bitwise: check_ldu128_bicgstab's docstring
+    check_ldu128_bicgstab(s.last_info.converged, it, s.last_info.residual_history,
                           x.cpu().numpy(), R)

@@ -131,7 +131,7 @@ def test_pcg_matches_oracle_iteration_counts(pre):
 
 
 def test_pcg_config1_against_reference():
-    """Config 1: 32^3 Poisson, PCG+DIC to 1e-6 relative: same iteration count
+    """32^3 Poisson, PCG+DIC to 1e-6 relative: same iteration count
     as the reference (198, counting the iteration-0 check); x within 1e-8 of
     the reference's x (the reference's own thread-dependent dot products
     move its x by ~1e-9 at this depth), and within 1e-11 after 50 iterations."""

@@ -7,7 +7,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.golden.cases import (
-    C2SIZE_FIXTURE, DLAP_CASES, DLAP_FIXTURE, FIXTURE, c1_poisson, dlap_case, jitter_case,
+    LDU128_FIXTURE, DLAP_CASES, DLAP_FIXTURE, FIXTURE, c1_poisson, dlap_case, jitter_case,
     random_ldu, sha,
 )
 
@@ -197,11 +197,11 @@ def test_oracle_pressure_equation_against_reference():
     np.testing.assert_allclose(r.x, z["p_x"], rtol=0, atol=1e-9 * np.abs(z["p_x"]).max())
 
 
-def test_oracle_at_config2_size_against_reference():
+def test_oracle_at_128cube_against_reference():
     """128^3 hex topology (2,097,152 cells, 6,242,304 faces): Amul, Ax_T,
     FP32 Amul and both factorisations bitwise, PBiCGStab+DILU with the
     reference's iteration count, residual history and solution."""
-    R = np.load(C2SIZE_FIXTURE)
+    R = np.load(LDU128_FIXTURE)
     c = random_ldu(128, seed=5)
     assert sha(np.concatenate([c["diag"], c["lower"], c["upper"], c["x"], c["r"]])) == str(
         R["coeff_sha"])
@@ -216,10 +216,10 @@ def test_oracle_at_config2_size_against_reference():
     assert sha(pd) == str(R["dilu_sha"])
     o = O.pbicgstab(*args, c["r"], np.zeros(c["n"]), pd, 0.0, 1e-10, 200,
                     threads=O.num_threads())
-    check_c2size_bicgstab(o.converged, o.iterations, o.history, o.x, R)
+    check_ldu128_bicgstab(o.converged, o.iterations, o.history, o.x, R)
 
 
-def check_c2size_bicgstab(converged, iterations, history, x, R):
+def check_ldu128_bicgstab(converged, iterations, history, x, R):
     """The reference's omega = (t.z)/(t.t) makes this trajectory chaotic:
     a rounding difference in a dot product (summation order: torch's blocked
     CPU dot, the oracle's per-thread partials, the GPU's fixed tree) grows
