@@ -853,6 +853,33 @@ def run_next(args, rank, world, local):
     out["correct_velocity"] = {"s": t_cv, "bytes": cv_bytes, "GBs": cv_bytes / t_cv / 1e9}
     out["correct_face_flux"] = {"s": t_cf, "bytes": ff_bytes, "GBs": ff_bytes / t_cf / 1e9}
     out["rhie_chow_face_flux"] = {"s": t_rc, "bytes": rc_bytes, "GBs": rc_bytes / t_rc / 1e9}
+    if rank == 0 and not args.no_cpu:
+        # the oracle's serial C restatement of the same formulas beside each
+        # kernel (one core), and the GPU result against it bit for bit
+        from oracle import oracle as O
+
+        own_h, nei_h = own.cpu().numpy(), nei.cpu().numpy()
+        S_h, dl_h, V_h, w_h = (a.cpu().numpy() for a in (S, dl, V, w))
+        p_h, A_h, H_h, phi_h = (a.cpu().numpy() for a in (p, A, HbyA, phi))
+        bits = lambda a: np.ascontiguousarray(a, np.float64).view(np.int64)  # noqa: E731
+        legs = {
+            "correct_velocity": (
+                lambda: O.correct_velocity(n, own_h, nei_h, S_h, w_h, V_h, p_h, A_h, H_h),
+                lambda: correct_velocity(HbyA, HbyA, p, A, m)),
+            "correct_face_flux": (
+                lambda: O.correct_face_flux(own_h, nei_h, phi_h, p_h, A_h, S_h, dl_h, w_h),
+                lambda: correct_face_flux(phi, p, A, m, face_weights=w)),
+            "rhie_chow_face_flux": (
+                lambda: O.face_flux(own_h, nei_h, H_h, S_h, w_h, p_h, A_h, dl_h),
+                lambda: rhie_chow.compute_face_flux(HbyA, p, A, S, dl, own, nei, ni, V, w)),
+        }
+        for key, (cpu_fn, gpu_fn) in legs.items():
+            t0 = time.perf_counter()
+            ref = cpu_fn()
+            t_c = time.perf_counter() - t0
+            out[key].update(cpu_oracle_s=t_c, cpu_cores=1, speedup_vs_cpu=t_c / out[key]["s"],
+                            bitwise_vs_oracle=bool((bits(gpu_fn().cpu().numpy())
+                                                    == bits(ref)).all()))
 
     Nm = max(N // 2, 8)
     sd = hex_poisson(Nm, seed=2)
@@ -880,6 +907,19 @@ def run_next(args, rank, world, local):
                    "reduction_per_cycle": (h[-1] / h[0]) ** (1.0 / max(len(h) - 1, 1)),
                    "solve_s": t_g, "s_per_v_cycle": t_g / max(it, 1),
                    "first_solve_incl_hierarchy_s": t_first}
+    gs_cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+
+        t0 = time.perf_counter()
+        xg = O.gauss_seidel(sd["owner"], sd["neighbour"], sd["diag"], sd["lower"], sd["upper"],
+                            sd["b"], np.zeros(sd["n"]), n_sweeps=1)
+        gs_cpu = time.perf_counter() - t0
+        from pyopenfoam_gb300.solvers.smoothers import gs_sweep
+
+        xd = torch.zeros_like(b)
+        gs_sweep(mm, xd, b)
+        gs_bitwise = bool((xd.cpu().numpy().view(np.int64) == xg.view(np.int64)).all())
     sm = SmoothSolver(tolerance=0.0, rel_tol=0.0, max_iter=5, smoother="GaussSeidel",
                       n_sweeps=2)
     sm(mm, b, torch.zeros_like(b))
@@ -888,8 +928,17 @@ def run_next(args, rank, world, local):
     sm(mm, b, torch.zeros_like(b))
     torch.cuda.synchronize()
     t_s = time.perf_counter() - t0
+    from pyopenfoam_gb300.solvers.smoothers import gs_sweep
+
+    xs = torch.zeros_like(b)
+    t_sw = _event_time(lambda: gs_sweep(mm, xs, b))
     out["smooth_gauss_seidel"] = {"n_cells": sd["n"], "sweeps": 10,
-                                  "s_per_sweep_incl_checks": t_s / 10}
+                                  "s_per_sweep_incl_checks": t_s / 10,
+                                  "gpu_s_per_forward_sweep": t_sw}
+    if gs_cpu is not None:
+        out["smooth_gauss_seidel"].update(cpu_oracle_s_per_sweep=gs_cpu, cpu_cores=1,
+                                          speedup_vs_cpu=gs_cpu / t_sw,
+                                          bitwise_vs_oracle=gs_bitwise)
     if rank == 0:
         _line(args, world, f"rows next to the solve: GPU geometry, correctors, GAMG, smoothers "
               f"({N}^3 mesh)", t_geo, "s", False,

@@ -628,6 +628,141 @@ void orc_face_grad_to_cells_f64(idx_t n, idx_t nint, idx_t nfaces, const idx_t* 
   }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Pressure correctors either side of the solve (serial):                    */
+/*   correct_velocity, solvers/pressure_equation.py:187-266:                 */
+/*     p_f = w p_P + (1-w) p_N; grad = index_add(owner, p_f S_f),            */
+/*     index_add(neighbour, -p_f S_f), index_add(owner_b, p_P S_b) (in that  */
+/*     order, faces ascending); U = HbyA - (alpha/max(|A|,1e-30)) (grad /    */
+/*     max(V,1e-30)); rows with |U| > 1e4 scaled by 1e4/|U|                  */
+/*   compute_face_flux_HbyA + rhie_chow_correction, rhie_chow.py:81-250, and */
+/*   correct_face_flux, pressure_equation.py:269-332:                        */
+/*     rc_f = ((ia_f (p_P - p_N)) |S_f|) delta_f,                            */
+/*     ia_f = w/max(|A_P|,1e-30) + (1-w)/max(|A_N|,1e-30)                    */
+/* ------------------------------------------------------------------------ */
+static double lerp_w(double w, double a, double b) { return w * a + (1.0 - w) * b; }
+
+void orc_correct_velocity_f64(idx_t n, idx_t nint, idx_t nfaces, const idx_t* own /* nfaces */,
+                              const idx_t* nei, const double* areas, const double* w,
+                              const double* V, const double* p, const double* A,
+                              const double* HbyA, double alpha, double* U) {
+  double* g = (double*)calloc((size_t)(3 * (n > 0 ? n : 1)), sizeof(double));
+  for (idx_t f = 0; f < nint; ++f) {
+    const double pf = lerp_w(w[f], p[own[f]], p[nei[f]]);
+    for (int q = 0; q < 3; ++q) g[3 * own[f] + q] = g[3 * own[f] + q] + pf * areas[3 * f + q];
+  }
+  for (idx_t f = 0; f < nint; ++f) {
+    const double pf = lerp_w(w[f], p[own[f]], p[nei[f]]);
+    for (int q = 0; q < 3; ++q)
+      g[3 * nei[f] + q] = g[3 * nei[f] + q] + (-(pf * areas[3 * f + q]));
+  }
+  for (idx_t f = nint; f < nfaces; ++f) {
+    const double pb = p[own[f]];
+    for (int q = 0; q < 3; ++q) g[3 * own[f] + q] = g[3 * own[f] + q] + pb * areas[3 * f + q];
+  }
+  for (idx_t c = 0; c < n; ++c) {
+    const double vc = V[c] < 1e-30 ? 1e-30 : V[c];
+    const double s = alpha * inv_abs(A[c]);
+    double u[3];
+    for (int q = 0; q < 3; ++q) u[q] = HbyA[3 * c + q] - s * (g[3 * c + q] / vc);
+    double m = smag3(u);
+    m = m < 1e-30 ? 1e-30 : m;
+    if (m > 1e4) {
+      const double r = 1e4 / m;
+      for (int q = 0; q < 3; ++q) u[q] = u[q] * r;
+    }
+    for (int q = 0; q < 3; ++q) U[3 * c + q] = u[q];
+  }
+  free(g);
+}
+
+static double rc_term(idx_t f, const idx_t* own, const idx_t* nei, const double* p,
+                      const double* A, const double* areas, const double* delta,
+                      const double* w) {
+  const double wf = w ? w[f] : 0.5;
+  const double ia = lerp_w(wf, inv_abs(A[own[f]]), inv_abs(A[nei[f]]));
+  const double dp = p[own[f]] - p[nei[f]];
+  return ((ia * dp) * smag3(areas + 3 * f)) * delta[f];
+}
+
+/* phi_f = (w HbyA_P + (1-w) HbyA_N) . S_f on internal faces, HbyA_P . S_f on
+ * boundary faces (dot = ((0 + x) + y) + z), plus the Rhie-Chow term when p
+ * is given (w NULL: 0.5). */
+void orc_face_flux_f64(idx_t nint, idx_t nfaces, const idx_t* own, const idx_t* nei,
+                       const double* HbyA, const double* areas, const double* w,
+                       const double* p, const double* A, const double* delta, double* phi) {
+  for (idx_t f = 0; f < nfaces; ++f) {
+    double s = 0.0;
+    if (f < nint) {
+      const double wf = w ? w[f] : 0.5;
+      for (int q = 0; q < 3; ++q)
+        s = s + lerp_w(wf, HbyA[3 * own[f] + q], HbyA[3 * nei[f] + q]) * areas[3 * f + q];
+      if (p) s = s + rc_term(f, own, nei, p, A, areas, delta, w);
+    } else {
+      for (int q = 0; q < 3; ++q) s = s + HbyA[3 * own[f] + q] * areas[3 * f + q];
+      if (p) s = s + 0.0;
+    }
+    phi[f] = s;
+  }
+}
+
+/* correct_face_flux: phi_out = phi + rc on internal faces, phi on boundary. */
+void orc_correct_face_flux_f64(idx_t nint, idx_t nfaces, const idx_t* own, const idx_t* nei,
+                               const double* phi, const double* p, const double* A,
+                               const double* areas, const double* delta, const double* w,
+                               double* out) {
+  for (idx_t f = 0; f < nfaces; ++f)
+    out[f] = f < nint ? phi[f] + rc_term(f, own, nei, p, A, areas, delta, w) : phi[f];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Gauss-Seidel sweeps: SmoothSolver._solve_gauss_seidel,                    */
+/* solvers/smooth_solver.py:133-187 (relax = 0), and GaussSeidelSmoother,    */
+/* solvers/smoothers.py:63-149 (relax = 1: x_c + omega (new - x_c)).  Cells  */
+/* ascending (reverse: descending); a row's off-diagonal sum runs over the   */
+/* cell's faces in ascending face order: lower[f] x[nei] where the cell owns */
+/* the face, upper[f] x[own] where it is the neighbour.  The per-cell face   */
+/* lists are built once per call (counting sort keeps faces ascending).      */
+/* ------------------------------------------------------------------------ */
+void orc_gauss_seidel_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                          const double* diag, const double* lower, const double* upper,
+                          const double* b, int n_sweeps, int reverse, int relax, double omega,
+                          double* x) {
+  idx_t* ptr = (idx_t*)calloc((size_t)(n + 1), sizeof(idx_t));
+  idx_t* fl = (idx_t*)malloc(sizeof(idx_t) * (size_t)(2 * (nf > 0 ? nf : 1)));
+  for (idx_t f = 0; f < nf; ++f) { ptr[own[f] + 1]++; ptr[nei[f] + 1]++; }
+  for (idx_t c = 0; c < n; ++c) ptr[c + 1] += ptr[c];
+  idx_t* cur = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n > 0 ? n : 1));
+  for (idx_t c = 0; c < n; ++c) cur[c] = ptr[c];
+  for (idx_t f = 0; f < nf; ++f) {
+    fl[cur[own[f]]++] = f;
+    if (nei[f] != own[f]) fl[cur[nei[f]]++] = f;
+  }
+  for (int sweep = 0; sweep < n_sweeps; ++sweep) {
+    for (idx_t k = 0; k < n; ++k) {
+      const idx_t c = reverse ? n - 1 - k : k;
+      const double xc = x[c];
+      double row = diag[c] * xc;
+      for (idx_t i = ptr[c]; i < cur[c]; ++i) {
+        const idx_t f = fl[i];
+        if (own[f] == c)
+          row = row + lower[f] * x[nei[f]];
+        else
+          row = row + upper[f] * x[own[f]];
+      }
+      const double off = row - diag[c] * xc;
+      const double d = diag[c];
+      if (fabs(d) > 1e-30) {
+        const double nv = (b[c] - off) / d;
+        x[c] = relax ? xc + omega * (nv - xc) : nv;
+      }
+    }
+  }
+  free(cur);
+  free(fl);
+  free(ptr);
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

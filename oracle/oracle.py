@@ -284,5 +284,64 @@ def face_grad_to_cells(n_cells, owner_all, neighbour, g_face):
     return out
 
 
+def correct_velocity(n_cells, owner_all, neighbour, face_areas, weights, volumes, p, A_p, HbyA,
+                     alpha=1.0):
+    """``correct_velocity`` (solvers/pressure_equation.py:187-266), serial."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    fa, w, V = _f(face_areas).reshape(-1, 3), _f(weights), _f(volumes)
+    pp, A, H = _f(p), _f(A_p), _f(HbyA).reshape(-1, 3)
+    U = np.empty((n_cells, 3))
+    lib().orc_correct_velocity_f64(ctypes.c_int64(n_cells), ctypes.c_int64(nei.shape[0]),
+                                   ctypes.c_int64(own.shape[0]), _p(own), _p(nei), _p(fa),
+                                   _p(w), _p(V), _p(pp), _p(A), _p(H), ctypes.c_double(alpha),
+                                   _p(U))
+    return U
+
+
+def face_flux(owner_all, neighbour, HbyA, face_areas, weights=None, p=None, A_p=None,
+              delta=None):
+    """``compute_face_flux_HbyA`` (rhie_chow.py:81-133) and, with p,
+    ``compute_face_flux`` = that + ``rhie_chow_correction`` (rhie_chow.py:
+    136-250); weights None means 0.5."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    H, fa = _f(HbyA).reshape(-1, 3), _f(face_areas).reshape(-1, 3)
+    w = None if weights is None else _f(weights)
+    pp = None if p is None else _f(p)
+    A = None if A_p is None else _f(A_p)
+    dl = None if delta is None else _f(delta)
+    phi = np.empty(own.shape[0])
+    lib().orc_face_flux_f64(ctypes.c_int64(nei.shape[0]), ctypes.c_int64(own.shape[0]),
+                            _p(own), _p(nei), _p(H), _p(fa), None if w is None else _p(w),
+                            None if pp is None else _p(pp), None if A is None else _p(A),
+                            None if dl is None else _p(dl), _p(phi))
+    return phi
+
+
+def correct_face_flux(owner_all, neighbour, phi, p, A_p, face_areas, delta, weights):
+    """``correct_face_flux`` (solvers/pressure_equation.py:269-332)."""
+    own, nei = _i64(owner_all), _i64(neighbour)
+    ph, pp, A = _f(phi), _f(p), _f(A_p)
+    fa, dl, w = _f(face_areas).reshape(-1, 3), _f(delta), _f(weights)
+    out = np.empty(own.shape[0])
+    lib().orc_correct_face_flux_f64(ctypes.c_int64(nei.shape[0]), ctypes.c_int64(own.shape[0]),
+                                    _p(own), _p(nei), _p(ph), _p(pp), _p(A), _p(fa), _p(dl),
+                                    _p(w), _p(out))
+    return out
+
+
+def gauss_seidel(owner, neighbour, diag, lower, upper, b, x0, n_sweeps=1, reverse=False,
+                 relax=False, omega=1.0):
+    """``n_sweeps`` Gauss-Seidel sweeps from x0 (smooth_solver.py:133-187;
+    ``relax``: GaussSeidelSmoother's x_c + omega (new - x_c),
+    smoothers.py:63-149); returns x."""
+    own, nei = _i64(owner), _i64(neighbour)
+    x = _f(x0).copy()
+    lib().orc_gauss_seidel_f64(ctypes.c_int64(x.shape[0]), ctypes.c_int64(own.shape[0]),
+                               _p(own), _p(nei), _p(_f(diag)), _p(_f(lower)), _p(_f(upper)),
+                               _p(_f(b)), ctypes.c_int(n_sweeps), ctypes.c_int(int(reverse)),
+                               ctypes.c_int(int(relax)), ctypes.c_double(omega), _p(x))
+    return x
+
+
 def num_threads() -> int:
     return int(lib().orc_num_threads())

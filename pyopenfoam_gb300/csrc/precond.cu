@@ -16,13 +16,31 @@ __device__ __forceinline__ void dic_cell(const gbf_layout& L, const double* __re
   double dc = __ldg(diag + c);
   if (L.n_faces > 0) {
     const CellSlots cs = cell_slots(L, c);
-    for (int k = 0; k < cs.wn; ++k) {
-      const int i = cs.base + 32 * (cs.wo + k);
-      const int j = __ldg(L.slot_col + i);
-      if (j < 0) continue;
-      const double a = __ldg(coef + i);
-      const double dj = (j < c) ? __ldcg(d + j) : __ldg(diag + j);
-      if (fabs(dj) > 1e-30) dc = __dsub_rn(dc, __ddiv_rn(__dmul_rn(a, a), dj));
+    if (cs.wn <= 4) {
+      // the slots' columns, coefficients and d values loaded at once, then
+      // the subtractions in slot (= face) order
+      int j[4];
+      double a[4], dj[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int i = cs.base + 32 * (cs.wo + k);
+        j[k] = k < cs.wn ? __ldg(L.slot_col + i) : -1;
+        a[k] = j[k] >= 0 ? __ldg(coef + i) : 0.0;
+        dj[k] = j[k] < 0 ? 0.0 : (j[k] < c ? __ldcg(d + j[k]) : __ldg(diag + j[k]));
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (j[k] >= 0 && fabs(dj[k]) > 1e-30)
+          dc = __dsub_rn(dc, __ddiv_rn(__dmul_rn(a[k], a[k]), dj[k]));
+    } else {
+      for (int k = 0; k < cs.wn; ++k) {
+        const int i = cs.base + 32 * (cs.wo + k);
+        const int jk = __ldg(L.slot_col + i);
+        if (jk < 0) continue;
+        const double ak = __ldg(coef + i);
+        const double djk = (jk < c) ? __ldcg(d + jk) : __ldg(diag + jk);
+        if (fabs(djk) > 1e-30) dc = __dsub_rn(dc, __ddiv_rn(__dmul_rn(ak, ak), djk));
+      }
     }
   }
   d[c] = dc;
@@ -69,25 +87,6 @@ __device__ __forceinline__ void clamp_abs(double* d, int c) {
 __global__ void clamp_abs_kernel(int n, double* d) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) clamp_abs(d, c);
-}
-
-// The whole DIC factorisation in one cooperative launch: the levels, then
-// the clamp.
-__global__ void __launch_bounds__(kBlock)
-    dic_coop_kernel(gbf_layout L, const double* __restrict__ coef,
-                    const double* __restrict__ diag, const int32_t* __restrict__ level_ptr,
-                    const int32_t* __restrict__ level_cells, int n_levels, double* d,
-                    GridBarrier* bar) {
-  const bool ok =
-      run_levels(bar, level_ptr, n_levels,
-                 [&](int i) { dic_cell(L, coef, diag, __ldg(level_cells + i), d); }) &&
-      grid_barrier(bar, gridDim.x);
-  if (!ok) {
-    poison(d, L.n_cells);
-    return;
-  }
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells; c += gridDim.x * blockDim.x)
-    clamp_abs(d, c);
 }
 
 // The whole DILU factorisation in one cooperative launch: d = diag, the face
@@ -153,18 +152,11 @@ extern "C" int gbf_dic_build_f64(const gbf_layout* L, const double* coef, const 
   GBF_REQUIRE(n_levels >= 1 && max_level_size >= 1 && max_level_size <= n,
               "dic_build: bad schedule (levels=%d, max size=%d)", n_levels, max_level_size);
   cudaStream_t s = as_stream(stream);
-  const int gc = barrier ? wavefront_grid((const void*)dic_coop_kernel, kBlock,
-                                          max_level_size > n ? max_level_size : n, 2)
-                         : 0;
-  if (gc > 0) {
-    gbf_layout Lc = *L;
-    int nl = n_levels;
-    GridBarrier* bar = static_cast<GridBarrier*>(barrier);
-    void* args[] = {&Lc, (void*)&coef, (void*)&diag, (void*)&level_ptr, (void*)&level_cells,
-                    &nl, &d_out, &bar};
-    GBF_CHECK_CUDA(launch_wavefront((const void*)dic_coop_kernel, gc, args, barrier, s));
-    return GBF_OK;
-  }
+  // One launch per cell level: with each cell's slots loaded at once this is
+  // faster than the cooperative form for DIC (measured 6.6 vs 7.4 ms at
+  // 256^3, 3.0 vs 3.3 ms at 128^3), so `barrier` is not used here; its
+  // fault word stays 0.
+  if (barrier) GBF_CHECK_CUDA(cudaMemsetAsync(barrier, 0, sizeof(GridBarrier), s));
   const int grid = (max_level_size + kBlock - 1) / kBlock;
   for (int lv = 0; lv < n_levels; ++lv) {
     dic_level_kernel<<<grid, kBlock, 0, s>>>(*L, coef, diag, level_ptr, level_cells, lv, d_out);

@@ -32,7 +32,44 @@ __device__ __forceinline__ void gs_cell(const gbf_layout& L, const double* __res
   const double dc = __ldg(diag + c);
   const double xc = __ldcg(x + c);
   double row = __dmul_rn(dc, xc);
+  bool merged = false;
   if (L.n_faces > 0) {
+    const CellSlots cs = cell_slots(L, c);
+    if (cs.wo <= 4 && cs.wn <= 4) {
+      // Every slot's face, coefficient and x value loaded at once; when the
+      // cell's neighbour-side faces all precede its owner-side faces (always
+      // on a mesh in upper-triangular face order), ascending face order is
+      // the neighbour-side slots followed by the owner-side slots.
+      int fk[8];
+      double a[8], xv[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const bool use = k < 4 ? k < cs.wo : (k - 4) < cs.wn;
+        const int slot_k = k < 4 ? k : cs.wo + (k - 4);
+        const int slot = cs.base + 32 * slot_k;
+        fk[k] = use ? __ldg(L.slot_face + slot) : -1;
+        const int col = use ? slot_column(L, cs.e0 + slot_k, slot, c) : -1;
+        a[k] = use ? __ldg(coef + slot) : 0.0;
+        xv[k] = (use && col >= 0) ? __ldcg(x + col) : 0.0;
+      }
+      int max_nei = -1, min_own = INT_MAX;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (fk[k] >= 0 && fk[k] < min_own) min_own = fk[k];
+        if (fk[4 + k] > max_nei) max_nei = fk[4 + k];
+      }
+      if (max_nei < min_own) {
+#pragma unroll
+        for (int k = 4; k < 8; ++k)
+          if (fk[k] >= 0) row = __dadd_rn(row, __dmul_rn(a[k], xv[k]));
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (fk[k] >= 0) row = __dadd_rn(row, __dmul_rn(a[k], xv[k]));
+        merged = true;
+      }
+    }
+  }
+  if (L.n_faces > 0 && !merged) {
     const CellSlots cs = cell_slots(L, c);
     int i = 0, j = 0;
     while (true) {

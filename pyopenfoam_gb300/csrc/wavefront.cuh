@@ -44,8 +44,8 @@ __device__ __forceinline__ void poison(double* out, int n) {
 // no more than needed for the largest level and at most `per_sm_max` per SM
 // (fewer blocks make a cheaper barrier, more hide more latency of the
 // items' dependent loads; a level larger than the grid is looped over).
-// Measured on GB300: the cell levels (DIC, Gauss-Seidel) are fastest with
-// two blocks per SM, the many small face levels (DILU, sweeps) with one.
+// Measured on GB300: the Gauss-Seidel cell levels are fastest with two
+// blocks per SM, the many small face levels (DILU, sweeps) with one.
 // 0 when the device cannot launch cooperatively.
 inline int wavefront_grid(const void* kernel, int block, long long max_level_items,
                           int per_sm_max) {
