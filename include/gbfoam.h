@@ -95,6 +95,11 @@ int gbf_device_sm_count(int32_t* n_sm);
  * [1] = 1 if the mbarrier wait gave up, [2] = the barrier's fault word.
  * Allocates and frees a few bytes of device memory; synchronises.          */
 int gbf_selftest_bounded_waits(int32_t* timed_out_h);
+/* Self-test of the cooperative wavefronts' failure path: a two-level
+ * wavefront whose grid barrier can never complete (1000-poll limit).
+ * result_h[0] = the barrier's fault word (1 expected), result_h[1] = 1 if
+ * the output was overwritten with NaN.  No GPU fault is involved.          */
+int gbf_selftest_wavefront_fault(int32_t* result_h);
 /* Kernel timing probes (no reference counterpart; used by the benchmark to
  * time the dominant kernel inside a solve).  While enabled, the solvers
  * bracket the launches of their Amul kernels with CUDA events on the

@@ -12,8 +12,11 @@
 //     ever posted.
 // Nothing faults, traps or spins without bound; the whole test takes well
 // under a millisecond of GPU time.
+#include <string.h>
+
 #include "barrier.cuh"
 #include "bulk.cuh"
+#include "wavefront.cuh"
 
 namespace gbf {
 
@@ -37,9 +40,61 @@ __global__ void mbarrier_timeout_kernel(int polls, int* out) {
   }
 }
 
+// A two-level wavefront whose grid barrier can never complete: the arrival
+// counter starts far past the block count, so no arrival is the last one.
+// The waits run out, the fault word is set and every block overwrites the
+// output with NaN -- the failure path of every cooperative wavefront.
+__global__ void wavefront_timeout_kernel(const int32_t* level_ptr, GridBarrier* bar,
+                                         long long polls, double* out, int n) {
+  const bool ok = run_levels(bar, level_ptr, 2, [&](int i) { out[i] = 1.0; }, polls);
+  if (!ok) poison(out, n);
+}
+
 }  // namespace gbf
 
 using namespace gbf;
+
+extern "C" int gbf_selftest_wavefront_fault(int32_t* result_h) {
+  GBF_REQUIRE(result_h, "selftest: NULL pointer");
+  int dev = 0, coop = 0;
+  GBF_CHECK_CUDA(cudaGetDevice(&dev));
+  GBF_CHECK_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  GBF_REQUIRE(coop, "selftest: the device has no cooperative launch");
+  constexpr int n = 64;
+  struct Buf {
+    GridBarrier bar;
+    int32_t level_ptr[4];
+    double out[n];
+  };
+  Buf h0;
+  memset(&h0, 0, sizeof(h0));
+  h0.bar.count = 1u << 30;  // never reaches the block count
+  h0.level_ptr[0] = 0;
+  h0.level_ptr[1] = n / 2;
+  h0.level_ptr[2] = n;
+  Buf* d = nullptr;
+  GBF_CHECK_CUDA(cudaMalloc(&d, sizeof(Buf)));
+  cudaError_t e = cudaMemcpy(d, &h0, sizeof(Buf), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    const int32_t* lp = d->level_ptr;
+    GridBarrier* bar = &d->bar;
+    long long polls = 1000;  // ~0.1 ms
+    double* out = d->out;
+    int nn = n;
+    void* args[] = {(void*)&lp, &bar, &polls, &out, &nn};
+    e = cudaLaunchCooperativeKernel((const void*)wavefront_timeout_kernel, dim3(2), dim3(32),
+                                    args, 0, nullptr);
+  }
+  Buf h;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(Buf), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  GBF_CHECK_CUDA(e);
+  int all_nan = 1;
+  for (int i = 0; i < n; ++i) all_nan &= (h.out[i] != h.out[i]) ? 1 : 0;
+  result_h[0] = h.bar.fault;
+  result_h[1] = all_nan;
+  return GBF_OK;
+}
 
 extern "C" int gbf_selftest_bounded_waits(int32_t* timed_out_h) {
   GBF_REQUIRE(timed_out_h, "selftest: NULL pointer");

@@ -23,13 +23,14 @@ namespace gbf {
 // a barrier wait ran out.
 template <typename F>
 __device__ __forceinline__ bool run_levels(GridBarrier* bar, const int32_t* __restrict__ level_ptr,
-                                           int n_levels, F&& body) {
+                                           int n_levels, F&& body,
+                                           long long max_polls = kBarrierPolls) {
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   for (int lv = 0; lv < n_levels; ++lv) {
     const int start = __ldg(level_ptr + lv), end = __ldg(level_ptr + lv + 1);
     for (int i = start + tid; i < end; i += stride) body(i);
-    if (lv + 1 < n_levels && !grid_barrier(bar, gridDim.x)) return false;
+    if (lv + 1 < n_levels && !grid_barrier(bar, gridDim.x, max_polls)) return false;
   }
   return true;
 }

@@ -274,6 +274,29 @@ def test_bounded_waits_give_up_instead_of_hanging():
     assert it > 1 and torch.isfinite(x).all()
 
 
+def test_wavefront_barrier_timeout_poisons_the_output():
+    """The cooperative wavefronts' failure path, without a GPU fault: a
+    barrier that can never complete runs out after its poll limit, sets the
+    fault word and the output becomes NaN; the context stays usable (a DIC
+    factorisation and a Gauss-Seidel sweep afterwards still work)."""
+    import ctypes
+
+    from pyopenfoam_gb300 import _lib
+    from pyopenfoam_gb300.solvers.smoothers import gs_sweep
+
+    out = (ctypes.c_int32 * 2)()
+    _lib.check(_lib.lib().gbf_selftest_wavefront_fault(out))
+    assert list(out) == [1, 1]
+    c = c1_poisson(8)
+    m = LduMatrix(c["n"], torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(k) for k in (c["diag"], c["lower"], c["upper"]))
+    assert torch.isfinite(DICPreconditioner(m).precond_diag).all()
+    x = torch.zeros(c["n"], dtype=torch.float64, device="cuda")
+    gs_sweep(m, x, torch.as_tensor(c["b"]).cuda())
+    assert torch.isfinite(x).all() and torch.count_nonzero(x) > 0
+
+
 @pytest.mark.parametrize("launch", ["single", "kernels"])
 def test_breakdown_and_nan_follow_the_reference(launch):
     """Failure modes of the reference solvers, reproduced (no exception, no
