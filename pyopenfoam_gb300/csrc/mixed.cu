@@ -206,6 +206,7 @@ __device__ __forceinline__ void mp_update_cells(int n, double* __restrict__ x, c
   const float4* __restrict__ p4 = reinterpret_cast<const float4*>(v.p);
   const float4* __restrict__ ap4 = reinterpret_cast<const float4*>(v.Ap);
   const float4* __restrict__ rd4 = reinterpret_cast<const float4*>(v.rD);
+#pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
     const float4 pp = p4[q], ap = ap4[q], rd = __ldg(rd4 + q);
     float4 xl = xlo4[q], r = r4[q], z;
@@ -363,6 +364,7 @@ __global__ void __launch_bounds__(kBlock) mp_p_kernel(int n, MixedVecs v) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   float4* __restrict__ p4 = reinterpret_cast<float4*>(v.p);
   const float4* __restrict__ z4 = reinterpret_cast<const float4*>(v.z);
+#pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
     float4 p = p4[q];
     const float4 z = z4[q];

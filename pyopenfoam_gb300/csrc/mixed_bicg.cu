@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(kBlock) mb_s_kernel(int n, MbVecs v) {
   float4* __restrict__ s4 = reinterpret_cast<float4*>(v.s);
   float4* __restrict__ z4 = reinterpret_cast<float4*>(v.z);
   float4* __restrict__ x4 = reinterpret_cast<float4*>(v.xlo);
+#pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
     const float4 r = r4[q], vv = v4[q], y = y4[q], rd = __ldg(rd4 + q);
     float4 xl = x4[q], s, z;
@@ -309,6 +310,7 @@ __device__ __forceinline__ void mb_r_cells(int n, double* __restrict__ x, const 
   const float4* __restrict__ rt4 = reinterpret_cast<const float4*>(v.rt);
   float4* __restrict__ r4 = reinterpret_cast<float4*>(v.r);
   float4* __restrict__ x4 = reinterpret_cast<float4*>(v.xlo);
+#pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
     const float4 s = s4[q], t = t4[q], z = z4[q], rt = __ldg(rt4 + q);
     float4 xl = x4[q], r;
@@ -453,6 +455,7 @@ __global__ void __launch_bounds__(kBlock) mb_p_kernel(int n, MbVecs v) {
   const float4* __restrict__ rd4 = reinterpret_cast<const float4*>(v.rD);
   float4* __restrict__ p4 = reinterpret_cast<float4*>(v.p);
   float4* __restrict__ y4 = reinterpret_cast<float4*>(v.y);
+#pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
     const float4 r = r4[q], vv = v4[q], rd = __ldg(rd4 + q);
     float4 p = p4[q], y;
