@@ -113,6 +113,13 @@ static void launch_amul(const gbf_layout* L, const T* coef, const T* diag, const
 int check_layout(const gbf_layout* L) {
   GBF_REQUIRE(L != nullptr, "layout is NULL");
   GBF_REQUIRE(L->n_cells >= 0 && L->n_faces >= 0, "negative layout size");
+  // The kernels index cells, faces and slots with 32-bit integers, and a
+  // grid-stride loop may step up to kMaxGrid * 1024 past the last item.
+  constexpr int64_t kIndexLimit = (int64_t)INT_MAX - (int64_t)kMaxGrid * 1024;
+  GBF_REQUIRE(L->n_cells <= kIndexLimit && L->n_faces <= kIndexLimit && L->n_slots >= 0 &&
+                  L->n_slots <= kIndexLimit,
+              "layout too large for 32-bit indices: %d cells, %d faces, %lld slots (limit %lld)",
+              L->n_cells, L->n_faces, (long long)L->n_slots, (long long)kIndexLimit);
   GBF_REQUIRE(L->n_slices == (L->n_cells + 31) / 32, "layout n_slices does not match n_cells");
   if (L->n_cells > 0)
     GBF_REQUIRE(L->slice_off && L->slice_w && L->slot_col && L->slot_face,

@@ -151,6 +151,19 @@ def test_topology_rejects_bad_addressing():
     assert rc == 4 and b"owner == neighbour" in L.gbf_last_error()
 
 
+def test_layout_beyond_32bit_indices_is_refused():
+    """A 1024^3 mesh has more slots than the kernels' 32-bit indices reach:
+    the C ABI refuses it with an argument error before any CUDA call (the
+    pointers below are never dereferenced)."""
+    L = _lib.lib()
+    n = 1 << 30
+    lay = _lib.Layout(n_cells=n, n_faces=n, n_slices=(n + 31) // 32, max_width=6,
+                      uniform_wo=3, uniform_wn=3, all_uniform=1, n_slots=6 * n,
+                      slice_off=16, slice_w=16, slot_col=16, slot_face=16)
+    rc = L.gbf_amul_f64(ctypes.byref(lay), 16, 16, 16, 16, 0, None)
+    assert rc == 1 and b"32-bit" in L.gbf_last_error()
+
+
 def test_python_surface_errors_without_gpu():
     import torch
 
