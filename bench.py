@@ -905,12 +905,25 @@ def run_next(args, rank, world, local):
     torch.cuda.synchronize()
     t_g = time.perf_counter() - t0
     h = g.last_info.residual_history
+    gamg_cpu = {}
+    if rank == 0 and not args.no_cpu:
+        # the oracle's serial restatement: hierarchy + the same 50 V-cycles
+        from oracle import oracle as O
+
+        t0 = time.perf_counter()
+        xo, _, _ = O.gamg(sd["owner"], sd["neighbour"], sd["diag"], sd["lower"], sd["upper"],
+                          sd["b"], np.zeros(sd["n"]), 50)
+        t_o = time.perf_counter() - t0
+        gamg_cpu = {"cpu_oracle_s_incl_hierarchy": t_o, "cpu_cores": 1,
+                    "speedup_vs_cpu": t_o / t_first,
+                    "bitwise_vs_oracle": bool((x.cpu().numpy().view(np.int64)
+                                               == xo.view(np.int64)).all())}
     out["gamg"] = {"n_cells": sd["n"], "levels": [lv.n_cells for lv in g.last_levels],
                    # the monitor's first check follows the first cycle (as the reference's)
                    "v_cycles": it, "residual_reduction_after_cycle1": h[-1] / h[0],
                    "reduction_per_cycle": (h[-1] / h[0]) ** (1.0 / max(len(h) - 1, 1)),
                    "solve_s": t_g, "s_per_v_cycle": t_g / max(it, 1),
-                   "first_solve_incl_hierarchy_s": t_first}
+                   "first_solve_incl_hierarchy_s": t_first, **gamg_cpu}
     gs_cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O

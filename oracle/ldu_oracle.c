@@ -763,6 +763,208 @@ void orc_gauss_seidel_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
   free(ptr);
 }
 
+/* ------------------------------------------------------------------------ */
+/* GAMG, solvers/gamg.py:104-585 (serial).                                   */
+/*   aggregation (:166-240): adjacency lists in face order (owner gets the   */
+/*     neighbour, the neighbour the owner); cells ascending, an unaggregated */
+/*     cell seeds a new aggregate and takes its unaggregated neighbours; at  */
+/*     the target count the remaining cells join their first aggregated     */
+/*     neighbour's aggregate (else aggregate 0);                            */
+/*   coarse matrix (:242-335): diag = scatter_add of the fine diagonal; a   */
+/*     fine face between two aggregates adds to the coarse face of the      */
+/*     pair, numbered at its first occurrence with that face's orientation, */
+/*     lower/upper = first value + the others in face order;                */
+/*   V-cycle (:440-493): Jacobi x + (1/max(|d|,1e-30)) (b - A x), restrict  */
+/*     by scatter_add, coarse correction from zero, injection, 50 sweeps on */
+/*     the coarsest level.                                                   */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  idx_t n, nf;
+  idx_t *own, *nei; /* [nf] */
+  double *diag, *lower, *upper;
+  idx_t* f2c; /* [n], map to the next level (NULL on the coarsest) */
+  idx_t n_coarse;
+} orc_level;
+
+static idx_t gamg_aggregate(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei,
+                            idx_t target, idx_t* f2c) {
+  idx_t* ptr = (idx_t*)calloc((size_t)(n + 1), sizeof(idx_t));
+  idx_t* adj = (idx_t*)malloc(sizeof(idx_t) * (size_t)(2 * (nf > 0 ? nf : 1)));
+  idx_t* cur = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n > 0 ? n : 1));
+  for (idx_t f = 0; f < nf; ++f) { ptr[own[f] + 1]++; ptr[nei[f] + 1]++; }
+  for (idx_t c = 0; c < n; ++c) ptr[c + 1] += ptr[c];
+  for (idx_t c = 0; c < n; ++c) cur[c] = ptr[c];
+  for (idx_t f = 0; f < nf; ++f) {
+    adj[cur[own[f]]++] = nei[f];
+    adj[cur[nei[f]]++] = own[f];
+  }
+  for (idx_t c = 0; c < n; ++c) f2c[c] = -1;
+  idx_t na = 0;
+  for (idx_t c = 0; c < n; ++c) {
+    if (f2c[c] >= 0) continue;
+    const idx_t id = na++;
+    f2c[c] = id;
+    for (idx_t k = ptr[c]; k < ptr[c + 1]; ++k)
+      if (f2c[adj[k]] < 0) f2c[adj[k]] = id;
+    if (na >= target) {
+      for (idx_t r = 0; r < n; ++r) {
+        if (f2c[r] >= 0) continue;
+        int assigned = 0;
+        for (idx_t k = ptr[r]; k < ptr[r + 1]; ++k)
+          if (f2c[adj[k]] >= 0) { f2c[r] = f2c[adj[k]]; assigned = 1; break; }
+        if (!assigned) f2c[r] = 0;
+      }
+      break;
+    }
+  }
+  for (idx_t c = 0; c < n; ++c)
+    if (f2c[c] < 0) f2c[c] = 0;
+  free(cur);
+  free(adj);
+  free(ptr);
+  return na;
+}
+
+/* Coarse level of `fine` under fine->f2c (n_coarse cells).  The pair ->
+ * coarse-face map is an open-addressing hash on (min, max). */
+static void gamg_coarse(const orc_level* fine, orc_level* c) {
+  const idx_t nc = fine->n_coarse;
+  c->n = nc;
+  c->diag = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+  for (idx_t i = 0; i < fine->n; ++i) c->diag[fine->f2c[i]] = c->diag[fine->f2c[i]] + fine->diag[i];
+  idx_t cap = 16;
+  while (cap < 4 * (fine->nf + 1)) cap *= 2;
+  idx_t* hkey = (idx_t*)malloc(sizeof(idx_t) * (size_t)cap);
+  idx_t* hval = (idx_t*)malloc(sizeof(idx_t) * (size_t)cap);
+  for (idx_t i = 0; i < cap; ++i) hkey[i] = -1;
+  idx_t nfc = 0;
+  idx_t m = fine->nf > 0 ? fine->nf : 1;
+  c->own = (idx_t*)malloc(sizeof(idx_t) * (size_t)m);
+  c->nei = (idx_t*)malloc(sizeof(idx_t) * (size_t)m);
+  c->lower = (double*)malloc(sizeof(double) * (size_t)m);
+  c->upper = (double*)malloc(sizeof(double) * (size_t)m);
+  for (idx_t f = 0; f < fine->nf; ++f) {
+    const idx_t cp = fine->f2c[fine->own[f]], cn = fine->f2c[fine->nei[f]];
+    if (cp == cn) continue;
+    const idx_t lo = cp < cn ? cp : cn, hi = cp < cn ? cn : cp;
+    const idx_t key = lo * nc + hi;
+    idx_t h = (idx_t)(((uint64_t)key * 0x9E3779B97F4A7C15ull) >> 20) & (cap - 1);
+    while (hkey[h] >= 0 && hkey[h] != key) h = (h + 1) & (cap - 1);
+    if (hkey[h] == key) {
+      const idx_t i = hval[h];
+      c->lower[i] = c->lower[i] + fine->lower[f];
+      c->upper[i] = c->upper[i] + fine->upper[f];
+    } else {
+      hkey[h] = key;
+      hval[h] = nfc;
+      c->own[nfc] = cp;
+      c->nei[nfc] = cn;
+      c->lower[nfc] = fine->lower[f];
+      c->upper[nfc] = fine->upper[f];
+      ++nfc;
+    }
+  }
+  c->nf = nfc;
+  c->f2c = NULL;
+  c->n_coarse = 0;
+  free(hkey);
+  free(hval);
+}
+
+/* r = b - A x on a level (the reference's Ax order), work = 2n doubles. */
+static void gamg_residual(const orc_level* L, const double* b, const double* x, double* r,
+                          double* y, double* work) {
+  orc_amul_f64(L->n, L->nf, L->own, L->nei, L->diag, L->lower, L->upper, x, y, 0, work);
+  for (idx_t c = 0; c < L->n; ++c) r[c] = b[c] - y[c];
+}
+
+static void gamg_jacobi(const orc_level* L, double* x, const double* b, int n_it) {
+  const idx_t n = L->n;
+  double* r = (double*)malloc(sizeof(double) * (size_t)(4 * (n > 0 ? n : 1)));
+  for (int it = 0; it < n_it; ++it) {
+    gamg_residual(L, b, x, r, r + n, r + 2 * n);
+    for (idx_t c = 0; c < n; ++c) x[c] = x[c] + inv_abs(L->diag[c]) * r[c];
+  }
+  free(r);
+}
+
+static void gamg_vcycle(const orc_level* lv, int n_levels, int i, double* x, const double* b,
+                        int n_pre, int n_post) {
+  const orc_level* L = &lv[i];
+  if (i == n_levels - 1) {
+    gamg_jacobi(L, x, b, 50);
+    return;
+  }
+  gamg_jacobi(L, x, b, n_pre);
+  const idx_t n = L->n, nc = L->n_coarse;
+  double* r = (double*)malloc(sizeof(double) * (size_t)(4 * (n > 0 ? n : 1)));
+  gamg_residual(L, b, x, r, r + n, r + 2 * n);
+  double* rc = (double*)calloc((size_t)(2 * (nc > 0 ? nc : 1)), sizeof(double));
+  double* ec = rc + nc;
+  for (idx_t c = 0; c < n; ++c) rc[L->f2c[c]] = rc[L->f2c[c]] + r[c];
+  gamg_vcycle(lv, n_levels, i + 1, ec, rc, n_pre, n_post);
+  for (idx_t c = 0; c < n; ++c) x[c] = x[c] + ec[L->f2c[c]];
+  free(rc);
+  free(r);
+  gamg_jacobi(L, x, b, n_post);
+}
+
+/* n_cycles V-cycles from x (in place); hist[k] = |b - A x| after cycle k
+ * (summed in cell order); level_sizes[0..*n_levels) = the hierarchy's cell
+ * counts (at most max_levels + 1 entries). */
+void orc_gamg_f64(idx_t n, idx_t nf, const idx_t* own, const idx_t* nei, const double* diag,
+                  const double* lower, const double* upper, const double* b, double* x,
+                  int n_cycles, int n_pre, int n_post, int max_levels, int min_cells_coarse,
+                  double* hist, idx_t* level_sizes, int* n_levels_out) {
+  orc_level* lv = (orc_level*)calloc((size_t)(max_levels + 1), sizeof(orc_level));
+  lv[0].n = n;
+  lv[0].nf = nf;
+  lv[0].own = (idx_t*)own;
+  lv[0].nei = (idx_t*)nei;
+  lv[0].diag = (double*)diag;
+  lv[0].lower = (double*)lower;
+  lv[0].upper = (double*)upper;
+  int nl = 1;
+  for (int k = 0; k < max_levels; ++k) {
+    orc_level* cur = &lv[nl - 1];
+    if (cur->n <= min_cells_coarse) break;
+    idx_t target = cur->n / 2;
+    if (target < min_cells_coarse) target = min_cells_coarse;
+    cur->f2c = (idx_t*)malloc(sizeof(idx_t) * (size_t)(cur->n > 0 ? cur->n : 1));
+    cur->n_coarse = gamg_aggregate(cur->n, cur->nf, cur->own, cur->nei, target, cur->f2c);
+    if (cur->n_coarse >= cur->n) {
+      free(cur->f2c);
+      cur->f2c = NULL;
+      cur->n_coarse = 0;
+      break;
+    }
+    gamg_coarse(cur, &lv[nl]);
+    ++nl;
+  }
+  double* r = (double*)malloc(sizeof(double) * (size_t)(4 * (n > 0 ? n : 1)));
+  for (int k = 0; k < n_cycles; ++k) {
+    gamg_vcycle(lv, nl, 0, x, b, n_pre, n_post);
+    gamg_residual(&lv[0], b, x, r, r + n, r + 2 * n);
+    double ss = 0.0;
+    for (idx_t c = 0; c < n; ++c) ss = ss + r[c] * r[c];
+    hist[k] = sqrt(ss);
+  }
+  free(r);
+  for (int k = 0; k < nl; ++k) {
+    level_sizes[k] = lv[k].n;
+    free(lv[k].f2c);
+    if (k > 0) {
+      free(lv[k].own);
+      free(lv[k].nei);
+      free(lv[k].diag);
+      free(lv[k].lower);
+      free(lv[k].upper);
+    }
+  }
+  *n_levels_out = nl;
+  free(lv);
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

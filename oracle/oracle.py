@@ -343,5 +343,22 @@ def gauss_seidel(owner, neighbour, diag, lower, upper, b, x0, n_sweeps=1, revers
     return x
 
 
+def gamg(owner, neighbour, diag, lower, upper, b, x0, n_cycles, n_pre_smooth=2, n_post_smooth=2,
+         max_levels=10, min_cells_coarse=10):
+    """``n_cycles`` V-cycles of GAMGSolver (solvers/gamg.py:104-585) from x0,
+    serial; returns (x, residual norm after each cycle, level cell counts)."""
+    own, nei = _i64(owner), _i64(neighbour)
+    x = _f(x0).copy()
+    hist = np.empty(max(n_cycles, 1))
+    sizes = np.empty(max_levels + 1, np.int64)
+    nl = ctypes.c_int(0)
+    lib().orc_gamg_f64(ctypes.c_int64(x.shape[0]), ctypes.c_int64(own.shape[0]), _p(own),
+                       _p(nei), _p(_f(diag)), _p(_f(lower)), _p(_f(upper)), _p(_f(b)), _p(x),
+                       ctypes.c_int(n_cycles), ctypes.c_int(n_pre_smooth),
+                       ctypes.c_int(n_post_smooth), ctypes.c_int(max_levels),
+                       ctypes.c_int(min_cells_coarse), _p(hist), _p(sizes), ctypes.byref(nl))
+    return x, hist[:n_cycles], sizes[: nl.value]
+
+
 def num_threads() -> int:
     return int(lib().orc_num_threads())
