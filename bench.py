@@ -73,7 +73,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     p.add_argument("--workload", choices=["poisson256", "poisson32", "convdiff128", "batch64",
-                                          "adjoint96", "next"], default="poisson256",
+                                          "adjoint96", "next", "assembly"],
+                   default="poisson256",
                    help="poisson256 (default, the headline): 256^3 mixed vs FP64 PCG; "
                         "poisson32: 32^3 PCG+DIC to 1e-6; convdiff128: 128^3 jittered "
                         "convection-diffusion with PBiCGStab+DILU; batch64: 64 uneven Poisson "
@@ -966,6 +967,121 @@ def run_next(args, rank, world, local):
                                            "mesh (the reference's Python loops take hours)"})
 
 
+def run_assembly(args, rank, world, local):
+    """The operators on the path around the solve, each timed on the GPU
+    (CUDA events) beside the oracle's serial C restatement of the same
+    formulas (one core), with the GPU result compared bit for bit, on the
+    jittered N^3 mesh (default 128^3): fvm.laplacian, fvm.div (upwind), the
+    pressure-equation assembly, the DIC and DILU factorisations, the
+    DifferentiableLaplacian forward + backward and the DifferentiableLinear-
+    Solve gradient kernel.  Bytes are the arrays each operator reads and
+    writes once."""
+    from oracle import oracle as O
+    from pyopenfoam_gb300 import DICPreconditioner, DILUPreconditioner, LduMatrix
+    from pyopenfoam_gb300.differentiable import DifferentiableLaplacian, dls_grads
+    from pyopenfoam_gb300.discretisation import fvm
+    from pyopenfoam_gb300.mesh import HexMesh
+    from pyopenfoam_gb300.solvers import assemble_pressure_equation
+
+    dev = torch.device("cuda", local)
+    N = 128 if args.n == 256 else args.n
+    h = HexMesh(N, jitter=0.2, seed=1)
+    m = h.to(dev)
+    n, nf, ni = h.n_cells, h.n_faces, h.n_internal_faces
+    own, nei = h.numpy("owner"), h.numpy("neighbour")
+    S, dl, V = h.numpy("face_areas"), h.numpy("delta_coefficients"), h.numpy("cell_volumes")
+    rng = np.random.default_rng(1)
+    gamma = rng.lognormal(0.0, 1.0, nf)
+    nominal = HexMesh(N)
+    u = np.array([1.0, 0.5, 0.25])
+    flux = (nominal.numpy("face_areas") * u).sum(axis=1) * (10.0 * N / np.linalg.norm(u))
+    A_p = rng.uniform(0.5, 3.0, n)
+    phiHbyA = rng.normal(0.0, 1.0, nf)
+    w = O.centre_weights(own, nei, h.numpy("cell_centres"), h.numpy("face_centres"))
+    phi_c, g_c = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    T = lambda a: torch.as_tensor(a).to(dev)  # noqa: E731
+    bits = lambda a: np.ascontiguousarray(a, np.float64).view(np.int64)  # noqa: E731
+    out = {"n_cells": n, "n_faces": nf, "n_internal_faces": ni}
+
+    def leg(name, gpu_fn, cpu_fn, nbytes):
+        t_g = _event_time(gpu_fn, reps=5, warmup=2)
+        got = gpu_fn()
+        rec = {"gpu_s": t_g, "bytes": nbytes, "GBs": nbytes / t_g / 1e9}
+        if rank == 0 and not args.no_cpu:
+            t0 = time.perf_counter()
+            ref = cpu_fn()
+            t_c = time.perf_counter() - t0
+            same = all(bool((bits(a.detach().cpu().numpy()) == bits(b)).all())
+                       for a, b in zip(got, ref))
+            rec.update(cpu_oracle_s=t_c, cpu_cores=1, speedup_vs_cpu=t_c / t_g,
+                       bitwise_vs_oracle=same)
+        out[name] = rec
+
+    gam = T(gamma)
+    lap = lambda: fvm.laplacian(gam, torch.zeros(1), mesh=m)  # noqa: E731
+    leg("fvm_laplacian", lambda: (lambda A: (A.lower, A.upper, A.diag))(lap()),
+        lambda: O.laplacian(n, own, nei, S, dl, gamma, V),
+        nf * (24 + 8 + 8 + 8) + ni * (8 + 8 + 16) + n * (8 + 8))
+    fl = T(flux)
+    leg("fvm_div_upwind",
+        lambda: (lambda A: (A.lower, A.upper, A.diag))(fvm.div(fl, torch.zeros(1),
+                                                                "Gauss upwind", mesh=m)),
+        lambda: O.div_upwind(n, own[:ni], nei, flux[:ni], V),
+        ni * (8 + 8 + 16 + 16) + n * (8 + 8))
+    Ap, ph, wt = T(A_p), T(phiHbyA), T(w)
+    leg("pressure_assembly",
+        lambda: (lambda P: (P.lower, P.upper, P.diag, P.source))(
+            assemble_pressure_equation(ph, Ap, m, face_weights=wt)),
+        lambda: O.pressure_assemble(n, own, nei, S, dl, w, A_p, V, phiHbyA),
+        nf * (24 + 8 + 8 + 8 + 8) + ni * (8 + 8 + 16 + 16) + n * (8 + 8 + 16))
+
+    A = lap()
+    own_i = own[:ni]
+    lo_h, up_h, dg_h = (t.cpu().numpy() for t in (A.lower, A.upper, A.diag))
+    def fresh(mat, cls):
+        # drop the cached factorisation (kept per matrix) so that every call builds it
+        for k in [k for k in mat._csr_cache if k[0] == cls.kind]:
+            del mat._csr_cache[k]
+        return (cls(mat).precond_diag,)
+
+    leg("dic_factorisation", lambda: fresh(A, DICPreconditioner),
+        lambda: (O.dic_build(own_i, nei, dg_h, up_h),), 16 * n + 16 * ni)
+    D = fvm.div(fl, torch.zeros(1), "Gauss upwind", mesh=m)
+    M = LduMatrix(n, A.owner, A.neighbour, device=dev)
+    M.diag, M.lower, M.upper = A.diag - D.diag, A.lower - D.lower, A.upper - D.upper
+    md, ml, mu = (t.cpu().numpy() for t in (M.diag, M.lower, M.upper))
+    leg("dilu_factorisation", lambda: fresh(M, DILUPreconditioner),
+        lambda: (O.dilu_build(own_i, nei, md, ml, mu),), 16 * n + 48 * ni)
+
+    def dlap():
+        p_ = T(phi_c).requires_grad_(True)
+        d_ = T(gamma).requires_grad_(True)
+        y = DifferentiableLaplacian.apply(p_, d_, m)
+        (y * T(g_c)).sum().backward()
+        return y.detach(), p_.grad, d_.grad
+
+    leg("differentiable_laplacian_fwd_bwd", dlap,
+        lambda: (O.explicit_laplacian(n, own, nei, S, dl, gamma, V, phi_c),
+                 O.explicit_laplacian(n, own, nei, S, dl, gamma, V, g_c),
+                 O.explicit_laplacian_grad_d(own, nei, S, dl, V, phi_c, g_c)),
+        3 * (nf * (24 + 8 + 8 + 16) + ni * 16) + n * 48)
+    lam_h, x_h = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    lam, xx = T(lam_h), T(x_h)
+    leg("dls_gradients", lambda: dls_grads(M, lam, xx),
+        lambda: O.dls_grads(own_i, nei, lam_h, x_h), 24 * n + 48 * ni)
+    if rank == 0:
+        _line(args, world, f"operators around the solve on the {N}^3 jittered mesh: "
+              f"fvm.laplacian time", out["fvm_laplacian"]["gpu_s"], "s", False,
+              {"workload": f"{N}^3 hex, +-20% jitter: fvm.laplacian, fvm.div, pressure "
+                           "assembly, DIC / DILU factorisation, DifferentiableLaplacian, "
+                           "DLS gradients", "n_cells": n},
+              out, cpu_baseline={"value": out["fvm_laplacian"].get("cpu_oracle_s"),
+                                 "unit": "s", "cores": 1, "kind": "port",
+                                 "sample": "the oracle's serial C restatement of each "
+                                           "operator, same inputs (per-operator times in "
+                                           "extra)"})
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup()
@@ -981,6 +1097,8 @@ def main():
         run_adjoint96(args, rank, world, local)
     elif args.workload == "next":
         run_next(args, rank, world, local)
+    elif args.workload == "assembly":
+        run_assembly(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:
