@@ -232,11 +232,9 @@ int gbf_amul_sym_f32(const gbf_layout* L, const float* coef_own, const float* di
  * With it the whole schedule runs in one cooperative launch, levels
  * separated by a bounded grid barrier; with NULL (or a device without
  * cooperative launch) one kernel runs per level.  Same bits either way.
- * gbf_dic_build_f64 always launches per level (measured faster for its
- * cell levels) and only zeroes the barrier memory it is given.  If
- * a barrier wait runs out (2 s) the output is overwritten with NaN and
- * gbf_wavefront_fault reports 1 (it synchronises the stream).  Calls must
- * not share one barrier buffer while in flight.                           */
+ * If a barrier wait runs out (a few seconds) the output is overwritten
+ * with NaN and gbf_wavefront_fault reports 1 (it synchronises the stream).
+ * Calls must not share one barrier buffer while in flight.                */
 size_t gbf_wavefront_barrier_bytes(void);
 int gbf_wavefront_fault(const void* barrier, int32_t* fault_h, void* stream);
 /* DICPreconditioner._build, solvers/preconditioners.py:88-133: level-

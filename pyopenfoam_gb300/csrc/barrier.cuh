@@ -1,11 +1,19 @@
 // Software grid barrier for cooperative (all blocks resident) launches.
 //
-// Thread 0 of each block arrives on a counter; the last to arrive resets it
-// and advances a generation word that the others poll.  Every wait is
-// bounded: after `max_polls` polls (100 ns sleep each) the block records a
-// fault and returns false; blocks that reach a barrier after a fault return
-// false at once.  Callers return from the kernel on false, and the host turns
-// the fault word into an error status, so a lost block never hangs the GPU.
+// The arrival counter only grows within a launch: thread 0 of each block adds
+// one with release semantics at GPU scope (publishing the block's writes,
+// ordered before it by __syncthreads), which also tells it which barrier it
+// is at -- all arrivals at barrier k return values in [k*G, (k+1)*G) for G
+// blocks, since no block passes barrier k before all G have arrived -- and
+// then polls the counter with acquire loads until it reaches (k+1)*G.  So the
+// critical path is one atomic and one load; there is no reset, no separate
+// generation word and no full fence.
+//
+// Every wait is bounded: after `max_polls` polls the block records a fault
+// and returns false, and a waiting block that sees the fault word (checked
+// every 16 polls) gives up at once.  Callers return from the kernel on false,
+// and the host turns the fault word into an error status, so a lost block
+// never hangs the GPU.
 #pragma once
 
 #include "common.cuh"
@@ -13,11 +21,23 @@
 namespace gbf {
 
 struct GridBarrier {
-  unsigned int count, gen;
+  unsigned long long count;
   int fault, pad;
 };
 
-constexpr long long kBarrierPolls = 1LL << 24;  // ~2 s with the 100 ns sleeps
+constexpr long long kBarrierPolls = 1LL << 22;  // a few seconds of polling
+
+__device__ __forceinline__ unsigned long long barrier_arrive(unsigned long long* c) {
+  unsigned long long old;
+  asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(old) : "l"(c) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ unsigned long long barrier_load(const unsigned long long* c) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(c) : "memory");
+  return v;
+}
 
 __device__ __forceinline__ bool grid_barrier(GridBarrier* bar, unsigned int nblocks,
                                              long long max_polls = kBarrierPolls) {
@@ -25,27 +45,18 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* bar, unsigned int nblo
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned int* vgen = &bar->gen;
-    volatile int* vfault = &bar->fault;
-    const unsigned int g = *vgen;
-    __threadfence();
-    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
-      atomicExch(&bar->count, 0u);
-      __threadfence();
-      atomicAdd(&bar->gen, 1u);
-    } else {
-      long long polls = 0;
-      while (*vgen == g) {
-        if (*vfault != 0 || ++polls > max_polls) {
-          atomicExch(&bar->fault, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(100);
+    const unsigned long long old = barrier_arrive(&bar->count);
+    const unsigned long long target = (old / nblocks + 1) * nblocks;
+    long long polls = 0;
+    while (barrier_load(&bar->count) < target) {
+      ++polls;
+      if (polls > max_polls || ((polls & 15) == 0 && *(volatile int*)&bar->fault != 0)) {
+        atomicExch(&bar->fault, 1);
+        ok = 0;
+        break;
       }
+      __nanosleep(32);
     }
-    __threadfence();
-    if (*vfault != 0) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

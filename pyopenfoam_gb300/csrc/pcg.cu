@@ -185,9 +185,9 @@ __global__ void __launch_bounds__(kBlock) pcg_p_kernel(int n, PcgVecs v) {
 // three-kernel form.  Vectors that other blocks rewrite during the launch
 // (p, and the partials) are read from L2 (__ldcg), never through L1.
 //
-// Every barrier wait is bounded: after kBarrierPolls polls (with a 100 ns
-// sleep each, ~2 s) the block records a fault and returns; blocks that reach
-// a barrier after a fault return at once.  The host turns a fault into
+// Every barrier wait is bounded: after kBarrierPolls polls (a few seconds)
+// the block records a fault and returns; a block waiting at a barrier that
+// sees the fault returns within 16 polls.  The host turns a fault into
 // GBF_DEVICE_TIMEOUT.
 // ---------------------------------------------------------------------------
 template <int KIND, bool PREC>

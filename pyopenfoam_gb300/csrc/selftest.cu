@@ -40,12 +40,13 @@ __global__ void mbarrier_timeout_kernel(int polls, int* out) {
   }
 }
 
-// A two-level wavefront whose grid barrier can never complete: the arrival
-// counter starts far past the block count, so no arrival is the last one.
-// The waits run out, the fault word is set and every block overwrites the
-// output with NaN -- the failure path of every cooperative wavefront.
+// A two-level wavefront whose grid barrier can never complete: block 1
+// never arrives.  Block 0's wait runs out, the fault word is set and block 0
+// overwrites the whole output with NaN -- the failure path of every
+// cooperative wavefront.
 __global__ void wavefront_timeout_kernel(const int32_t* level_ptr, GridBarrier* bar,
                                          long long polls, double* out, int n) {
+  if (blockIdx.x == 1) return;  // the participant that never arrives
   const bool ok = run_levels(bar, level_ptr, 2, [&](int i) { out[i] = 1.0; }, polls);
   if (!ok) poison(out, n);
 }
@@ -68,7 +69,6 @@ extern "C" int gbf_selftest_wavefront_fault(int32_t* result_h) {
   };
   Buf h0;
   memset(&h0, 0, sizeof(h0));
-  h0.bar.count = 1u << 30;  // never reaches the block count
   h0.level_ptr[0] = 0;
   h0.level_ptr[1] = n / 2;
   h0.level_ptr[2] = n;
