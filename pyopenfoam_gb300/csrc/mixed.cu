@@ -16,11 +16,15 @@
 // Per inner iteration (four launches; K_true returns at once unless an
 // update is due):
 //   K_ap   : Ap = A32 p, p.Ap                       -> alpha
-//   K_upd  : x32 += alpha p (or fold x64 += x32 + alpha p, x32 = 0),
-//            r -= alpha Ap, z = rD r, r.r, r.z      -> beta, update decision
+//   K_upd  : r -= alpha Ap, z = rD r, r.r, r.z      -> beta, update decision
+//            (when an update is due, also fold x64 += x32 + alpha p, x32 = 0)
 //   K_true : r64 = b - A64 x64 (reference-order Amul), r = (float) r64,
 //            z = rD r, |r64|, r.z                   -> convergence, beta
-//   K_p    : p = z + beta p
+//   K_p    : x32 += alpha p (unless K_upd folded), p = z + beta p
+// The FP32 solution update sits in K_p, which reads p anyway, so K_upd reads
+// neither p nor x32 on the iterations without an update (4 bytes per cell
+// per iteration less); each x32 element sees the same fmaf sequence as it
+// would in K_upd.
 // Dot products of FP32 vectors are accumulated per thread in double-float
 // arithmetic on the FP32 pipes -- each product split exactly into p + e with
 // a fused multiply-add (Dekker's TwoProduct), summed with Knuth's TwoSum --
@@ -38,7 +42,7 @@ enum { MP_NORMAL = 0, MP_TRUE_RESIDUAL = 1 };
 
 struct MixedState {
   double rz, alpha, beta, res0, res, rmax, target, pAp;
-  int inner, status, n_hist, phase, fold_pending, updates, fault, pad1;
+  int inner, status, n_hist, phase, fold_pending, updates, fault, x_deferred;
   unsigned int ticket[8];
 };
 
@@ -208,21 +212,22 @@ __device__ __forceinline__ void mp_update_cells(int n, double* __restrict__ x, c
   const float4* __restrict__ rd4 = reinterpret_cast<const float4*>(v.rD);
 #pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
-    const float4 pp = p4[q], ap = ap4[q], rd = __ldg(rd4 + q);
-    float4 xl = xlo4[q], r = r4[q], z;
-    xl.x = fmaf(alpha, pp.x, xl.x);
-    xl.y = fmaf(alpha, pp.y, xl.y);
-    xl.z = fmaf(alpha, pp.z, xl.z);
-    xl.w = fmaf(alpha, pp.w, xl.w);
+    const float4 ap = ap4[q], rd = __ldg(rd4 + q);
+    float4 r = r4[q], z;
     if constexpr (FOLD) {
+      const float4 pp = p4[q];
+      float4 xl = xlo4[q];
+      xl.x = fmaf(alpha, pp.x, xl.x);
+      xl.y = fmaf(alpha, pp.y, xl.y);
+      xl.z = fmaf(alpha, pp.z, xl.z);
+      xl.w = fmaf(alpha, pp.w, xl.w);
       const int c = 4 * q;
       x[c] += (double)xl.x;
       x[c + 1] += (double)xl.y;
       x[c + 2] += (double)xl.z;
       x[c + 3] += (double)xl.w;
-      xl = make_float4(0.f, 0.f, 0.f, 0.f);
+      xlo4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    xlo4[q] = xl;
     r.x = fmaf(-alpha, ap.x, r.x);
     r.y = fmaf(-alpha, ap.y, r.y);
     r.z = fmaf(-alpha, ap.z, r.z);
@@ -243,12 +248,9 @@ __device__ __forceinline__ void mp_update_cells(int n, double* __restrict__ x, c
     arz.add_prod(r.w, z.w);
   }
   for (int c = 4 * n4 + tid; c < n; c += stride) {
-    const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
     if constexpr (FOLD) {
-      x[c] += (double)xl;
+      x[c] += (double)fmaf(alpha, v.p[c], v.xlo[c]);
       v.xlo[c] = 0.0f;
-    } else {
-      v.xlo[c] = xl;
     }
     const float r = fmaf(-alpha, v.Ap[c], v.r[c]);
     const float z = __ldg(v.rD + c) * r;
@@ -288,6 +290,7 @@ __global__ void __launch_bounds__(kBlock)
       st->inner += 1;
       const double res = sqrt(trr);
       st->res = res;
+      st->x_deferred = fold ? 0 : 1;  // K_p adds alpha p to x32
       if (fold) {
         st->fold_pending = 0;
         st->phase = MP_TRUE_RESIDUAL;  // K_true replaces r and sets beta
@@ -354,27 +357,51 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
-__global__ void __launch_bounds__(kBlock) mp_p_kernel(int n, MixedVecs v) {
-  pdl_wait();
-  pdl_launch_dependents();
-  if (v.st->status != GBF_RUNNING) return;
+// p = z + beta p, after x32 += alpha p with the old p when X (the update
+// K_upd left to this kernel).
+template <bool X>
+__device__ __forceinline__ void mp_p_cells(int n, const MixedVecs& v) {
   const float beta = (float)v.st->beta;
+  const float alpha = (float)v.st->alpha;
   const int n4 = n >> 2;
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   float4* __restrict__ p4 = reinterpret_cast<float4*>(v.p);
+  float4* __restrict__ xlo4 = reinterpret_cast<float4*>(v.xlo);
   const float4* __restrict__ z4 = reinterpret_cast<const float4*>(v.z);
 #pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
     float4 p = p4[q];
     const float4 z = z4[q];
+    if constexpr (X) {
+      float4 xl = xlo4[q];
+      xl.x = fmaf(alpha, p.x, xl.x);
+      xl.y = fmaf(alpha, p.y, xl.y);
+      xl.z = fmaf(alpha, p.z, xl.z);
+      xl.w = fmaf(alpha, p.w, xl.w);
+      xlo4[q] = xl;
+    }
     p.x = fmaf(beta, p.x, z.x);
     p.y = fmaf(beta, p.y, z.y);
     p.z = fmaf(beta, p.z, z.z);
     p.w = fmaf(beta, p.w, z.w);
     p4[q] = p;
   }
-  for (int c = 4 * n4 + tid; c < n; c += stride) v.p[c] = fmaf(beta, v.p[c], v.z[c]);
+  for (int c = 4 * n4 + tid; c < n; c += stride) {
+    const float pc = v.p[c];
+    if constexpr (X) v.xlo[c] = fmaf(alpha, pc, v.xlo[c]);
+    v.p[c] = fmaf(beta, pc, v.z[c]);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) mp_p_kernel(int n, MixedVecs v) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (v.st->status != GBF_RUNNING) return;
+  if (v.st->x_deferred)
+    mp_p_cells<true>(n, v);
+  else
+    mp_p_cells<false>(n, v);
 }
 
 // Folds any remaining FP32 correction into x (breakdown / iteration limit;
