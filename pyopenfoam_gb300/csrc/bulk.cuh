@@ -135,15 +135,30 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
+// bulk_g2s with an L2 evict-first policy: for streams read once per pass
+// (coefficients, diagonal), so that their lines are the first to go and the
+// vectors the surrounding kernels reuse stay in L2 longer.
+__device__ __forceinline__ void bulk_g2s_stream(void* dst, const void* src, unsigned bytes,
+                                                unsigned long long* bar) {
+  unsigned long long policy;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1], %2, [%3], %4;" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
 // Issues the copies of tile t into stage s (one thread).
 __device__ __forceinline__ void hex_issue(HexRing<false>& R, int s, int t, const float* coef,
                                           const float* x, const float* d, const int* slot_dm,
                                           const int8_t*) {
   HexStage& S = R.stage[s];
   mbar_arrive_expect_tx(&R.bar[s], kStageBytes);
-  bulk_g2s(S.coef, coef + (size_t)t * (kTileSlices * kHexW * 32), sizeof(S.coef), &R.bar[s]);
+  bulk_g2s_stream(S.coef, coef + (size_t)t * (kTileSlices * kHexW * 32), sizeof(S.coef),
+                  &R.bar[s]);
   bulk_g2s(S.x, x + (size_t)t * kTileCells, sizeof(S.x), &R.bar[s]);
-  bulk_g2s(S.d, d + (size_t)t * kTileCells, sizeof(S.d), &R.bar[s]);
+  bulk_g2s_stream(S.d, d + (size_t)t * kTileCells, sizeof(S.d), &R.bar[s]);
   bulk_g2s(S.dm, slot_dm + (size_t)t * (2 * kTileSlices * kHexW), sizeof(S.dm), &R.bar[s]);
 }
 
