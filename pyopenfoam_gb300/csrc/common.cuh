@@ -37,6 +37,43 @@ __device__ __forceinline__ void pdl_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// L2 eviction priority for streams.  Each inner iteration of the mixed
+// solvers moves ~20x the L2's size; what pays to keep is the vector one
+// kernel writes and the next reads (Ap, z, p).  Loads and stores of data that
+// is dead after the access, or not read again until a later iteration, carry
+// an evict-first policy so that those hand-over vectors are the lines that
+// stay.  Hints only: the values are the same either way.
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+  unsigned long long policy;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+  return policy;
+}
+
+// Read-only (for this kernel) float4 with an L2 cache policy.
+__device__ __forceinline__ float4 ld_nc_hint(const float4* p, unsigned long long policy) {
+  float4 v;
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p), "l"(policy));
+  return v;
+}
+
+// float4 that this thread also writes (after reading it), with an L2 cache
+// policy.  The caller's own store of the same address depends on the value,
+// so it cannot move before this load.
+__device__ __forceinline__ float4 ld_hint(const float4* p, unsigned long long policy) {
+  float4 v;
+  asm("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p), "l"(policy));
+  return v;
+}
+
+__device__ __forceinline__ void st_hint(float4* p, float4 v, unsigned long long policy) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p),
+               "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(policy));
+}
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
                               Args&&... args) {

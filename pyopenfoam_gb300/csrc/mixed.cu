@@ -210,10 +210,13 @@ __device__ __forceinline__ void mp_update_cells(int n, double* __restrict__ x, c
   const float4* __restrict__ p4 = reinterpret_cast<const float4*>(v.p);
   const float4* __restrict__ ap4 = reinterpret_cast<const float4*>(v.Ap);
   const float4* __restrict__ rd4 = reinterpret_cast<const float4*>(v.rD);
+  const unsigned long long ef = l2_evict_first();
 #pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
-    const float4 ap = ap4[q], rd = __ldg(rd4 + q);
-    float4 r = r4[q], z;
+    // Ap and rD are dead until a later kernel or iteration, r is next read
+    // by the next iteration: evict first, keep z (read by K_p next)
+    const float4 ap = ld_nc_hint(ap4 + q, ef), rd = ld_nc_hint(rd4 + q, ef);
+    float4 r = ld_hint(r4 + q, ef), z;
     if constexpr (FOLD) {
       const float4 pp = p4[q];
       float4 xl = xlo4[q];
@@ -236,7 +239,7 @@ __device__ __forceinline__ void mp_update_cells(int n, double* __restrict__ x, c
     z.y = rd.y * r.y;
     z.z = rd.z * r.z;
     z.w = rd.w * r.w;
-    r4[q] = r;
+    st_hint(r4 + q, r, ef);
     z4[q] = z;
     arr.add_prod(r.x, r.x);
     arr.add_prod(r.y, r.y);
@@ -369,17 +372,20 @@ __device__ __forceinline__ void mp_p_cells(int n, const MixedVecs& v) {
   float4* __restrict__ p4 = reinterpret_cast<float4*>(v.p);
   float4* __restrict__ xlo4 = reinterpret_cast<float4*>(v.xlo);
   const float4* __restrict__ z4 = reinterpret_cast<const float4*>(v.z);
+  const unsigned long long ef = l2_evict_first();
 #pragma unroll 2
   for (int q = tid; q < n4; q += stride) {
+    // z is dead after this kernel and x32 is next touched by the next
+    // iteration: evict first, keep p (read by the next K_ap)
     float4 p = p4[q];
-    const float4 z = z4[q];
+    const float4 z = ld_nc_hint(z4 + q, ef);
     if constexpr (X) {
-      float4 xl = xlo4[q];
+      float4 xl = ld_hint(xlo4 + q, ef);
       xl.x = fmaf(alpha, p.x, xl.x);
       xl.y = fmaf(alpha, p.y, xl.y);
       xl.z = fmaf(alpha, p.z, xl.z);
       xl.w = fmaf(alpha, p.w, xl.w);
-      xlo4[q] = xl;
+      st_hint(xlo4 + q, xl, ef);
     }
     p.x = fmaf(beta, p.x, z.x);
     p.y = fmaf(beta, p.y, z.y);
