@@ -11,8 +11,9 @@
 // converge independently; tiles of finished systems return at once
 // (per-system convergence mask).  The iteration is the reliable-update
 // mixed-precision PCG of mixed.cu (FP32 inner iterations, FP64 true
-// residuals), and a chunk of iterations is captured once into a CUDA graph
-// and replayed until every system has finished.
+// residuals; x32 += alpha p in the p kernel, the L2 evict-first policies of
+// its vector kernels), and a chunk of iterations is captured once into a
+// CUDA graph and replayed until every system has finished.
 #include <math.h>
 #include <string.h>
 
@@ -22,7 +23,7 @@ namespace gbf {
 
 struct BState {
   double rz, alpha, beta, res0, res, rmax, target, pAp;
-  int inner, status, phase, fold_pending, updates, pad0;
+  int inner, status, phase, fold_pending, updates, x_deferred;
   unsigned int ticket[6];
 };
 
@@ -161,17 +162,15 @@ template <int BS, bool FOLD>
 __device__ __forceinline__ void bmp_update_cells(const BTiles& T, int tile,
                                                  double* __restrict__ x, const BVecs& v,
                                                  float alpha, BDFAcc& arr, BDFAcc& arz) {
+  const unsigned long long ef = l2_evict_first();
   for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < __ldg(T.tile_end + tile); c += BS) {
-    const float xl = fmaf(alpha, v.p[c], v.xlo[c]);
     if constexpr (FOLD) {
-      x[c] += (double)xl;
+      x[c] += (double)fmaf(alpha, v.p[c], v.xlo[c]);
       v.xlo[c] = 0.0f;
-    } else {
-      v.xlo[c] = xl;
     }
-    const float r = fmaf(-alpha, v.Ap[c], v.r[c]);
-    const float z = __ldg(v.rD + c) * r;
-    v.r[c] = r;
+    const float r = fmaf(-alpha, ld_nc_hint(v.Ap + c, ef), ld_hint(v.r + c, ef));
+    const float z = ld_nc_hint(v.rD + c, ef) * r;
+    st_hint(v.r + c, r, ef);
     v.z[c] = z;
     arr.add_prod(r, r);
     arz.add_prod(r, z);
@@ -208,6 +207,7 @@ __global__ void __launch_bounds__(BS)
       st->inner += 1;
       const double res = sqrt(trr);
       st->res = res;
+      st->x_deferred = fold ? 0 : 1;  // bmp_p_kernel adds alpha p to x32
       if (fold) {
         st->fold_pending = 0;
         st->phase = 1;
@@ -279,8 +279,14 @@ __global__ void __launch_bounds__(BS) bmp_p_kernel(BTiles T, BVecs v) {
   const BState* st = v.st + __ldg(T.tile_sys + tile);
   if (st->status != GBF_RUNNING) return;
   const float beta = (float)st->beta;
-  for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < __ldg(T.tile_end + tile); c += BS)
-    v.p[c] = fmaf(beta, v.p[c], v.z[c]);
+  const float alpha = (float)st->alpha;
+  const bool xd = st->x_deferred != 0;
+  const unsigned long long ef = l2_evict_first();
+  for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < __ldg(T.tile_end + tile); c += BS) {
+    const float pc = v.p[c];
+    if (xd) st_hint(v.xlo + c, fmaf(alpha, pc, ld_hint(v.xlo + c, ef)), ef);
+    v.p[c] = fmaf(beta, pc, ld_nc_hint(v.z + c, ef));
+  }
 }
 
 template <int BS>

@@ -74,6 +74,23 @@ __device__ __forceinline__ void st_hint(float4* p, float4 v, unsigned long long 
                "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(policy));
 }
 
+// Scalar forms of the above.
+__device__ __forceinline__ float ld_nc_hint(const float* p, unsigned long long policy) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy));
+  return v;
+}
+
+__device__ __forceinline__ float ld_hint(const float* p, unsigned long long policy) {
+  float v;
+  asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy));
+  return v;
+}
+
+__device__ __forceinline__ void st_hint(float* p, float v, unsigned long long policy) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(policy));
+}
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
                               Args&&... args) {
