@@ -413,19 +413,23 @@ def run_ours(args, rank, world, local):
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = n * 8
     xs_host = torch.empty(n, dtype=torch.float64).pin_memory()
-    e2e_times = []
+    e2e_times, h2d_times = [], []
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        h0.record()
         m.diag = host["diag"].to(dev, non_blocking=True)
         m.lower = host["lower"].to(dev, non_blocking=True)
         m.upper = host["upper"].to(dev, non_blocking=True)
         bb = host["b"].to(dev, non_blocking=True)
+        h1.record()  # stream-ordered after the copies: their device time, no extra sync
         xe, _, _ = mixed(m, bb, x0)
         xs_host.copy_(xe, non_blocking=True)
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
+            h2d_times.append(h0.elapsed_time(h1) / 1e3)
     # median over the steps (one slow step -- a host-side stall -- moved the
     # mean by up to 10 %); the mean is reported beside it
     e2e = max_over_ranks(statistics.median(e2e_times), world) if e2e_times else None
@@ -486,7 +490,8 @@ def run_ours(args, rank, world, local):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "s", "statistic": "median of the timed steps",
                     "mean": e2e_mean, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "h2d_s_median": statistics.median(h2d_times) if h2d_times else None},
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "extra": extra,

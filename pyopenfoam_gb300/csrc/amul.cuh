@@ -135,8 +135,15 @@ __device__ __forceinline__ A cell_amul_fixed(const gbf_layout& L, const T* __res
   }
   T a[W], xv[W];
   bool on[W];
+  if constexpr (sizeof(T) == 4) {
+    // FP32 coefficients are a read-once stream per pass: L2 evict-first
+    const unsigned long long ef = l2_evict_first();
 #pragma unroll
-  for (int k = 0; k < W; ++k) a[k] = __ldg(coef + base + 32 * k);
+    for (int k = 0; k < W; ++k) a[k] = ld_nc_hint(coef + base + 32 * k, ef);
+  } else {
+#pragma unroll
+    for (int k = 0; k < W; ++k) a[k] = __ldg(coef + base + 32 * k);
+  }
 #pragma unroll
   for (int k = 0; k < W; ++k) {
     on[k] = (m[k] >> lane) & 1u;
