@@ -66,7 +66,9 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--n", type=int, default=256, help="cells per direction")
+    p.add_argument("--n", "--size", type=int, default=256, dest="n",
+                   help="cells per direction (--size under torchrun, whose own options "
+                        "--n would abbreviate)")
     p.add_argument("--rel-tol", type=float, default=1e-10)
     p.add_argument("--delta", type=float, default=0.1)
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
