@@ -415,16 +415,19 @@ def run_ours(args, rank, world, local):
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = n * 8
     xs_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    # device buffers the caller keeps across steps (as a time loop would):
+    # each step copies the host data into them and hands them to the setters
+    dbuf = {k: torch.empty_like(t, device=dev) for k, t in host.items()}
     e2e_times, h2d_times = [], []
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
         h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h0.record()
-        m.diag = host["diag"].to(dev, non_blocking=True)
-        m.lower = host["lower"].to(dev, non_blocking=True)
-        m.upper = host["upper"].to(dev, non_blocking=True)
-        bb = host["b"].to(dev, non_blocking=True)
+        m.diag = dbuf["diag"].copy_(host["diag"], non_blocking=True)
+        m.lower = dbuf["lower"].copy_(host["lower"], non_blocking=True)
+        m.upper = dbuf["upper"].copy_(host["upper"], non_blocking=True)
+        bb = dbuf["b"].copy_(host["b"], non_blocking=True)
         h1.record()  # stream-ordered after the copies: their device time, no extra sync
         xe, _, _ = mixed(m, bb, x0)
         xs_host.copy_(xe, non_blocking=True)
