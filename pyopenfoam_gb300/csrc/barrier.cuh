@@ -1,6 +1,7 @@
 // Software grid barrier for cooperative (all blocks resident) launches.
 //
-// The arrival counter only grows within a launch: thread 0 of each block adds
+// The arrival counter starts at zero (the launcher clears the barrier memory)
+// and only grows within a launch: thread 0 of each block adds
 // one with release semantics at GPU scope (publishing the block's writes,
 // ordered before it by __syncthreads), which also tells it which barrier it
 // is at -- all arrivals at barrier k return values in [k*G, (k+1)*G) for G
