@@ -37,6 +37,29 @@ def test_library_exports_every_declared_symbol():
     assert L.gbf_version() >= 1
 
 
+def _declared_arity():
+    """Parameter count of every gbf_* function the headers declare."""
+    out = {}
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        txt = open(os.path.join(ROOT, "include", fn)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        txt = re.sub(r"//[^\n]*", "", txt)
+        for m in re.finditer(r"\b(gbf_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_argument_counts_match_the_headers():
+    """Every ctypes binding passes as many arguments as its C declaration
+    takes (an ABI change in the header without the binding, or the reverse,
+    fails here rather than as a wrong call on the GPU)."""
+    arity = _declared_arity()
+    assert set(arity) == set(_lib.EXPORTED), set(arity) ^ set(_lib.EXPORTED)
+    bad = {k: (arity[k], len(v[1])) for k, v in _lib.EXPORTED.items() if len(v[1]) != arity[k]}
+    assert not bad, bad
+
+
 def _layout(n, own, nei, pad=-1):
     L = _lib.lib()
     o = np.ascontiguousarray(own, np.int32)
