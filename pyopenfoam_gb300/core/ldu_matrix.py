@@ -281,8 +281,13 @@ class LduMatrix:
         return self.Ax_sparse(x)
 
     def invalidate_cache(self) -> None:
-        """Drop derived data (kept for API parity; the cache is also keyed
-        by the coefficients' version counters)."""
+        """Drop every derived array cached on this matrix: the packed
+        FP64/FP32 coefficients and the factorised DIC/DILU diagonals all live
+        in ``_csr_cache``, so the next solve re-packs and re-factorises.  The
+        setters and in-place edits already invalidate entries through the
+        coefficients' version counters; a caller calls this to force that
+        work (a benchmark timing the whole solve, or a matrix whose storage
+        was overwritten through another alias)."""
         self._csr_cache.clear()
 
     def __repr__(self) -> str:

@@ -64,21 +64,29 @@ class ResidualMonitor:
         self._history.clear()
         self._initial_residual = None
 
+    def _ratio(self, res_norm: float) -> float:
+        """|r| / |r0|, taken as 0 while the first norm is zero or unknown."""
+        r0 = self._initial_residual
+        return res_norm / r0 if r0 else 0.0
+
+    def _log(self, label: str, k: int, res_norm: float) -> None:
+        logger.info("  %s %d: |r| %.6e, |r|/|r0| %.6e", label, k, res_norm,
+                    self._ratio(res_norm))
+
     def check(self, res_norm: float, iteration: int) -> bool:
         """Record one residual norm and apply the convergence rules
-        (residual.py:112-145)."""
+        (residual.py:112-145): from ``min_iter`` on, an absolute norm below
+        ``tolerance`` or a ratio to the first norm below ``rel_tol`` stops
+        the solve."""
         self._history.append(res_norm)
         if self._initial_residual is None:
             self._initial_residual = res_norm
         if self._verbose:
-            ratio = res_norm / self._initial_residual if self._initial_residual > 0 else 0.0
-            logger.info("  Iteration %d: residual = %.6e (ratio = %.6e)", iteration, res_norm, ratio)
-        if iteration >= self._min_iter:
-            if res_norm < self._tolerance:
-                return True
-            if self._initial_residual > 0 and res_norm / self._initial_residual < self._rel_tol:
-                return True
-        return False
+            self._log("iteration", iteration, res_norm)
+        if iteration < self._min_iter:
+            return False
+        r0 = self._initial_residual
+        return res_norm < self._tolerance or (r0 > 0 and res_norm / r0 < self._rel_tol)
 
     def update(self, residual: torch.Tensor, iteration: int) -> bool:
         return self.check(float(torch.linalg.vector_norm(residual).item()), iteration)
@@ -88,20 +96,14 @@ class ResidualMonitor:
         self._history = list(history)
         self._initial_residual = self._history[0] if self._history else None
         if self._verbose:
-            for i, r in enumerate(self._history):
-                ratio = r / self._history[0] if self._history[0] > 0 else 0.0
-                logger.info("  Check %d: residual = %.6e (ratio = %.6e)", i, r, ratio)
+            for k, res_norm in enumerate(self._history):
+                self._log("check", k, res_norm)
 
     def build_info(self, converged: bool) -> ConvergenceInfo:
-        initial = self._initial_residual or 0.0
-        final = self._history[-1] if self._history else 0.0
-        ratio = final / initial if initial > 0 else 0.0
-        return ConvergenceInfo(
-            converged=converged,
-            iterations=len(self._history),
-            final_residual=final,
-            initial_residual=initial,
-            residual_ratio=ratio,
-            tolerance=self._tolerance,
-            residual_history=list(self._history),
-        )
+        """Summary of the recorded checks: their count is the iteration
+        count, the last norm the final residual (0.0 for an empty history)."""
+        hist = list(self._history)
+        last = hist[-1] if hist else 0.0
+        first = self._initial_residual if self._initial_residual else 0.0
+        return ConvergenceInfo(converged, len(hist), last, first,
+                               self._ratio(last) if first > 0 else 0.0, self._tolerance, hist)
