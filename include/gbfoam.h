@@ -306,13 +306,17 @@ int gbf_pcg_solve_f64(const gbf_layout* L, const double* slot_coef, const double
                       size_t workspace_bytes, void* stream);
 
 /* No counterpart in the reference.  Same solve as gbf_pcg_solve_f64 for
- * callers that cannot allocate device memory when they solve (work recorded
- * into a stream capture, real-time loops that must not touch the allocator,
- * programs with a fixed device-memory budget): the scratch comes from one
- * file-scope device array of 32.1 MiB instead of a workspace, so at most
- * 1,048,576 cells (larger systems return GBF_ERR_ARG).  The first call on a
- * device looks up the array's address and should precede any stream
- * capture; calls that overlap on the GPU share the array and race.        */
+ * callers that cannot allocate device memory when they solve (real-time
+ * loops that must not touch the allocator, host codes whose device memory
+ * is owned by their own pool or a fixed budget, plugin hosts that offer no
+ * allocator): the scratch comes from one file-scope device array of 32.1 MiB
+ * instead of a workspace, so at most 1,048,576 cells (larger systems return
+ * GBF_ERR_ARG).  It always runs three kernels per iteration: P->variant 0
+ * and 1 are accepted alike, 2 (single launch required) and anything else
+ * return GBF_ERR_ARG.  The first call on a device looks up and caches the
+ * array's address there and should precede any stream capture; the cached
+ * address does not survive cudaDeviceReset.  Calls that overlap on the GPU
+ * share the array and race.                                                */
 int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* slot_coef, const double* diag,
                               const double* precond_d, const double* b, double* x,
                               double* history, const gbf_solve_params* P, gbf_solve_result* R,

@@ -476,25 +476,29 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
 // gbf_pcg_solve_f64_noalloc: the FP64 PCG solve without a caller workspace.
 //
 // Who needs it: callers that cannot allocate device memory at the moment they
-// solve.  Examples are code that records its work into a CUDA stream capture
-// (cudaMalloc and cudaFree are not allowed there, and cudaFree synchronises
-// the whole device), real-time or embedded time loops that must never wait
-// on the allocator or handle an out-of-memory error mid-step, and host
-// programs that run under a fixed device-memory budget and pass the solver
-// only their own input and output buffers.  Such a caller keeps x, b, the
-// matrix and the history buffer; everything else the solve needs (the four
-// iteration vectors r, z, p, Ap, the per-block partial sums and the state
-// block) lives in one file-scope device array of fixed size.
+// solve.  Examples are real-time or embedded time loops that must never wait
+// on the allocator or handle an out-of-memory error mid-step, host programs
+// (a C, C++ or Fortran CFD code) whose device memory is owned by their own
+// pool or runs under a fixed budget and which hand the solver only their own
+// input and output buffers, and plugin hosts that expose no allocator to the
+// library they load.  Such a caller keeps x, b, the matrix and the history
+// buffer; everything else the solve needs (the four iteration vectors r, z,
+// p, Ap, the per-block partial sums and the state block) lives in one
+// file-scope device array of fixed size.
 //
 // Limits and rules:
 //   * at most kNoAllocMaxCells (1,048,576) cells; larger systems are refused
 //     with GBF_ERR_ARG -- use gbf_pcg_solve_f64 with a workspace for them;
 //   * the array occupies 32.1 MiB on every GPU that loads the library, until
 //     the process exits;
+//   * it always runs the three-kernel-per-iteration form (variant 0 and 1
+//     alike); variant 2, which demands the single cooperative launch, is
+//     refused with GBF_ERR_ARG, as is any value outside 0..2;
 //   * the first call on a device looks up the array's device address on that
 //     device (cudaGetSymbolAddress, with the device current) and caches it;
-//     make that first call before any stream capture that includes this
-//     entry point;
+//     make that first call before any stream capture begins; the cached
+//     address does not survive cudaDeviceReset, so a process that resets a
+//     device must not call this entry point on that device afterwards;
 //   * all calls share the one array, which keeps the previous call's
 //     contents: the state block is cleared at the start of every call, and
 //     calls whose work overlaps on the GPU (different streams, or different
@@ -546,6 +550,9 @@ extern "C" int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* coef
   if (rc) return rc;
   GBF_REQUIRE(P && R, "pcg_noalloc: NULL params/result");
   GBF_REQUIRE(P->max_iter >= 0, "pcg_noalloc: negative max_iter");
+  GBF_REQUIRE(P->variant == 0 || P->variant == 1,
+              "pcg_noalloc: variant must be 0 or 1 (this entry point always runs three kernels "
+              "per iteration; the single-launch form, variant 2, needs gbf_pcg_solve_f64)");
   const int n = L->n_cells;
   GBF_REQUIRE(n <= kNoAllocMaxCells,
               "pcg_noalloc: %d cells exceed the fixed scratch limit of %d cells; use "
@@ -588,10 +595,14 @@ extern "C" int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* coef
   PcgState hs;
   GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
   GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+  const bool hex = layout_kind(*L) == kLayoutHex33;
   int launched = 0;
   while (hs.status == GBF_RUNNING && launched < P->max_iter) {
     for (int j = 0; j < chunk && launched < P->max_iter; ++j, ++launched) {
-      pcg_ap_kernel<kLayoutGeneric><<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      if (hex)
+        pcg_ap_kernel<kLayoutHex33><<<G, kBlock, 0, s>>>(*L, coef, diag, v);
+      else
+        pcg_ap_kernel<kLayoutGeneric><<<G, kBlock, 0, s>>>(*L, coef, diag, v);
       if (pd)
         pcg_update_kernel<true><<<G, kBlock, 0, s>>>(n, pd, x, v, hist, *P);
       else
