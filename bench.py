@@ -18,21 +18,23 @@ matrix coefficients and RHS are copied from pinned host memory and x is read
 back inside the timed region.
 
 ``roofline``: the dominant kernel is the FP32 Amul + p.Ap reduction of the
-inner iteration; its algorithmic bytes per launch are
-B_amul(4) = 3*4*n + 2*4*F + 8*F (diag, x, y; lower, upper; int32 owner and
-neighbour), divided by the launch durations recorded with CUDA events on the
-launching stream during the timed steps.  The kernel's layout reads neither
-per-face indices (per-slice offsets replace them) nor, for a symmetric
-matrix, the upper triangle (the owner-side half of the coefficients is
-streamed), so it moves fewer bytes than B_amul: ``design_bytes_per_launch``
-and ``design_frac`` state the bytes it does move, ``traffic`` the DRAM bytes
-ncu measured.
+inner iteration.  ``achieved`` is the bytes that kernel moves per launch in
+its own layout -- p, diagonal and Ap (4 B per cell each), the off-diagonal
+slots (4 B per slot, both sides) and the per-slice {offset, mask} entries
+(8 B per slot column); no per-face index is read, the offsets replace them
+-- divided by the launch durations recorded with CUDA events on the
+launching stream during the timed steps.  ``frac_survey_bytes`` states the
+same durations against B_amul(4) = 12n + 16F, which also counts int32
+owner and neighbour arrays this kernel never reads.  ``traffic`` is the DRAM
+bytes per launch of a small-case ncu capture of the same kernel, scaled to
+this workload by its layout bytes.
 
 ``--impl reference`` times the reference algorithm on the host cores
 instead: the CPU restatement of the reference's PCG+DIC (the reference is
-pure Python on PyTorch and cannot run here), threaded over all host cores,
-on a bounded sample (DIC factorisation + 20 iterations) extrapolated to the
-iteration count of the full solve.
+pure Python on PyTorch and cannot run here), threaded over all host cores.
+It first runs one full FP64 solve to the tolerance (its iteration count and
+time are reported), then each step is a bounded sample (DIC factorisation
++ 20 iterations) extrapolated to that iteration count.
 """
 
 from __future__ import annotations
@@ -54,10 +56,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "time to 1e-10 rel. residual: mixed-prec refined vs FP64 PCG on GPU; Amul HBM GB/s"
 WORKLOAD = "256^3 Poisson (unit-cube hex, x0 fixed value), PCG+DIC to 1e-10 relative residual"
-# Iterations of FP64 PCG+DIC to 1e-10 on this system, counted like the
-# reference (len(history)); measured with the FP64 GPU solver on GB300 and
-# used only to extrapolate the bounded CPU sample of the reference arm.
-FP64_ITERATIONS_256 = 1991
+# ncu summary of the small-case capture whose DRAM bytes per launch give
+# ``roofline.traffic`` (scaled by layout bytes to the bench's size)
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "mp_ap_stream_kernel_192cube_dram.md")
 
 
 def parse():
@@ -74,6 +75,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    p.add_argument("--ref-sample-only", action="store_true",
+                   help="--impl reference: skip the full solve that sets the iteration count")
     p.add_argument("--workload", choices=["poisson256", "poisson32", "convdiff128", "batch64",
                                           "adjoint96", "next", "assembly"],
                    default="poisson256",
@@ -186,19 +189,51 @@ def b_amul(s: int, n: int, F: int) -> int:
     return 3 * s * n + 2 * s * F + 8 * F
 
 
-def design_bytes_ap(n: int, F: int, n_slices: int, sym: bool) -> int:
+def design_bytes_ap(n: int, n_slots: int, sym: bool) -> int:
     """Bytes the staged FP32 K_ap moves in its own layout: p, diagonal and
-    Ap (4 B each per cell), the off-diagonal slots (4F for the owner-side
-    half of a symmetric matrix, 8F for both sides), the per-slice {offset,
-    mask} entries (6 x 8 B) and, for the half storage, the mirror entries
-    (6 x 1 B per slice).  No per-face index bytes: the offsets replace them."""
-    return 12 * n + (4 if sym else 8) * F + n_slices * 6 * (8 + (1 if sym else 0))
+    Ap (4 B each per cell), the off-diagonal slots (4 B per slot on both
+    sides; for the half storage of a symmetric matrix only the owner-side
+    half, plus a 1 B mirror entry per neighbour-side slot column) and one
+    8 B {offset, mask} entry per slot column of 32 slots.  No per-face index
+    bytes: the offsets replace them."""
+    cols = n_slots // 32
+    if sym:
+        return 12 * n + 2 * n_slots + cols * 8 + cols // 2
+    return 12 * n + 4 * n_slots + cols * 8
 
 
-# DRAM bytes (read + write) per launch of the FP32 K_ap at 256^3, from the
-# ncu launch list committed in profiles/mixed_pcg_256cube_launch_list.md
-# (dram__bytes_read.sum + dram__bytes_write.sum, mean over its 100 launches).
-NCU_TRAFFIC_AP_256 = {"sym": 494.1e6, "full": 626.1e6}
+def layout_bytes(s: int, n: int, n_slots: int, n_slices: int, kind: str) -> int:
+    """Bytes one Amul moves in a given layout, element size s: x, diagonal
+    and y (s B per cell each) and one coefficient per slot (s B), plus the
+    addressing the layout reads -- an 8 B {offset, mask} entry per column of
+    32 slots (offset-compressed), with the per-slice start and width (4 + 4
+    B per slice) when the width is not fixed, or an int32 column per slot
+    (explicit columns)."""
+    base = 3 * s * n + s * n_slots
+    if kind == "compressed":
+        return base + 8 * (n_slots // 32)
+    if kind == "variable_width":
+        return base + 8 * (n_slots // 32) + 8 * n_slices
+    if kind == "explicit_columns":
+        return base + 4 * n_slots + 8 * n_slices
+    raise ValueError(kind)
+
+
+def traffic_from_profile(design_bytes: int) -> dict | None:
+    """DRAM bytes per launch of K_ap from the committed small-case capture,
+    scaled to this workload by layout bytes.  The summary holds one line
+    ``traffic: <dram read+write bytes per launch> <layout bytes per launch>``."""
+    try:
+        with open(TRAFFIC_PROFILE) as f:
+            for line in f:
+                if line.startswith("traffic:"):
+                    dram, lay = (float(v) for v in line.split()[1:3])
+                    return {"bytes": dram / lay * design_bytes, "ratio_to_layout_bytes": dram / lay,
+                            "captured_dram_bytes": dram, "captured_layout_bytes": lay,
+                            "source": os.path.relpath(TRAFFIC_PROFILE, ROOT)}
+    except (OSError, ValueError):
+        pass
+    return None
 
 
 def load_peaks() -> dict:
@@ -257,8 +292,11 @@ def time_amul(m, dev, reps=20):
                                                      d32.data_ptr(), x32.data_ptr(),
                                                      y32.data_ptr(), 0, st.cuda_stream),
     }
+    kinds = {"f64": "compressed", "f32": "compressed", "f32_explicit_columns": "explicit_columns",
+             "f32_variable_width": "variable_width"}
     for name, fn in fns.items():
         s = 8 if name == "f64" else 4
+        moved = layout_bytes(s, n, topo.n_slots, topo.n_slices, kinds[name])
         for _ in range(3):
             fn()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -269,7 +307,9 @@ def time_amul(m, dev, reps=20):
         e1.record(st)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
-        out[name] = {"us": ms * 1e3, "GBs": b_amul(s, n, F) / (ms * 1e-3) / 1e9}
+        out[name] = {"us": ms * 1e3, "layout": kinds[name], "bytes": moved,
+                     "GBs": moved / (ms * 1e-3) / 1e9,
+                     "GBs_survey_bytes": b_amul(s, n, F) / (ms * 1e-3) / 1e9}
     return out
 
 
@@ -305,13 +345,32 @@ def cpu_model() -> str:
 
 
 # --------------------------------------------------------------------------
+def headline_config(args, n: int, F: int, world: int) -> dict:
+    """The workload both arms report, key for key."""
+    return {"workload": WORKLOAD.replace("256^3", f"{args.n}^3"), "n_cells": n, "n_faces": F,
+            "rel_tol": args.rel_tol, "rhs_seed": 2,
+            "l2": "no flush: resident inputs (~1.9 GB at 256^3) exceed the 129 MB L2",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args, rank, world):
+    from oracle import oracle as O
     from pyopenfoam_gb300.mesh.poisson import hex_poisson
 
     if rank != 0:
         return
     sysd = hex_poisson(args.n, seed=2)
-    iters_full = FP64_ITERATIONS_256 if args.n == 256 and FP64_ITERATIONS_256 else None
+    threads = len(os.sched_getaffinity(0))
+    full = None
+    if not args.ref_sample_only:
+        # one full FP64 solve to the tolerance: the iteration count the
+        # samples extrapolate to, and a measured total to check them against
+        t0 = time.perf_counter()
+        pd = O.dic_build(sysd["owner"], sysd["neighbour"], sysd["diag"], sysd["upper"])
+        o = O.pcg(sysd["owner"], sysd["neighbour"], sysd["diag"], sysd["lower"], sysd["upper"],
+                  sysd["b"], np.zeros(sysd["n"]), pd, 0.0, args.rel_tol, 50000, threads=threads)
+        full = {"s": time.perf_counter() - t0, "iterations": o.iterations,
+                "converged": bool(o.converged)}
     samples = []
     for i in range(args.warmup + args.steps):
         t_dic, t_it, threads = cpu_sample(sysd, iters=20)
@@ -319,27 +378,69 @@ def run_reference(args, rank, world):
             samples.append((t_dic, t_it))
     t_dic = statistics.median(s[0] for s in samples)
     t_it = statistics.median(s[1] for s in samples)
-    n_it = iters_full or 1
-    value = t_dic + t_it * n_it
+    n_it = full["iterations"] if full else None
+    value = t_dic + t_it * n_it if n_it else t_dic + t_it
     sample = (f"DIC factorisation + 20 PCG iterations of the {args.n}^3 system per step, "
-              f"extrapolated to {n_it} iterations" + ("" if iters_full else " (count unknown: 1)"))
+              + (f"extrapolated to the {n_it} iterations of one full solve of the same port "
+                 f"run first" if n_it else "not extrapolated (--ref-sample-only): one iteration"))
+    n, F = sysd["n"], int(sysd["owner"].shape[0])
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD.replace("256^3", f"{args.n}^3"), "n_cells": sysd["n"],
-                   "n_faces": int(sysd["owner"].shape[0]), "rel_tol": args.rel_tol,
-                   "rhs_seed": 2},
+        "data": "synthetic", "config": headline_config(args, n, F, world),
+        "solver": "oracle port of the reference PCG+DIC (FP64), all host cores",
+        "extrapolated": bool(n_it), "sampled_iterations": 20,
+        "timed_s_per_step": t_dic + 20 * t_it,
         "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
                          "sample": sample, "cpu": cpu_model(), "dic_build_s": t_dic,
                          "s_per_iteration": t_it},
+        "full_solve": full,
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if full:
+        line["full_solve"]["extrapolation_rel_err"] = value / full["s"] - 1.0
     print(json.dumps(line), flush=True)
 
 
+def _pinned_link_probe(dev, nbytes: int = 1 << 28, reps: int = 3) -> float:
+    """GB/s of one pinned host -> device copy of ``nbytes`` (best of
+    ``reps``), the link rate the e2e copies can reach on this machine."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    best = float("inf")
+    for _ in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        d.copy_(h, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return nbytes / best / 1e9
+
+
+def _host_placement(dev) -> dict:
+    """Where this process runs relative to the GPU: the host CPUs it may use,
+    the GPU's PCI NUMA node and the CPUs local to it (sysfs; empty where the
+    platform does not say)."""
+    out = {"cpus": len(os.sched_getaffinity(0))}
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        bus = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+        base = f"/sys/bus/pci/devices/{bus}"
+        with open(f"{base}/numa_node") as f:
+            out["gpu_numa_node"] = int(f.read())
+        with open(f"{base}/local_cpulist") as f:
+            out["gpu_local_cpulist"] = f.read().strip()
+    except (AttributeError, OSError, ValueError):
+        pass
+    return out
+
+
 def run_ours(args, rank, world, local):
+    import ctypes
+
     from pyopenfoam_gb300 import MixedPrecisionPCGSolver, PCGSolver, _lib
     from pyopenfoam_gb300.mesh.poisson import hex_poisson
 
@@ -358,26 +459,6 @@ def run_ours(args, rank, world, local):
     def step():
         m.invalidate_cache()  # re-pack + re-factorise each solve, like the reference
         return mixed(m, b, x0)
-
-    # --- FP64 comparison (same system, same API) ---
-    x64 = None
-    if not args.no_fp64:
-        fp64 = PCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
-                         preconditioner="DIC")
-        # one untimed solve (first launches, lazy module loading), then one
-        # timed like the mixed steps: packing + DIC + iterations
-        m.invalidate_cache()
-        fp64(m, b, x0)
-        m.invalidate_cache()
-        torch.cuda.synchronize()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record()
-        x64, it64, res64 = fp64(m, b, x0)
-        f1.record()
-        torch.cuda.synchronize()
-        extra["fp64_pcg_s"] = f0.elapsed_time(f1) / 1e3
-        extra["fp64_iterations"] = it64
-        extra["fp64_true_rel_residual"] = true_rel_residual(m, x64, b)
 
     for _ in range(args.warmup):
         step()
@@ -398,8 +479,6 @@ def run_ours(args, rank, world, local):
         e1.record()
         torch.cuda.synchronize()
     ms_total = e0.elapsed_time(e1)
-    import ctypes
-
     cnt, tot = ctypes.c_int32(), ctypes.c_double()
     _lib.check(L.gbf_timing_read(1, ctypes.byref(cnt), ctypes.byref(tot)))
     L.gbf_timing_enable(0, 0)
@@ -411,42 +490,73 @@ def run_ours(args, rank, world, local):
 
     # --- end to end through the public API with host buffers (right after
     # the device-timed steps, before the auxiliary measurements allocate) ---
-    host = {k: torch.as_tensor(sysd[k]).pin_memory() for k in ("diag", "lower", "upper", "b")}
+    names = ("diag", "lower", "upper", "b")
+    host = {k: torch.as_tensor(sysd[k]).pin_memory() for k in names}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = n * 8
     xs_host = torch.empty(n, dtype=torch.float64).pin_memory()
     # device buffers the caller keeps across steps (as a time loop would):
-    # each step copies the host data into them and hands them to the setters
+    # each step copies all four host arrays into them, then hands them to the
+    # setters, solves and reads x back
     dbuf = {k: torch.empty_like(t, device=dev) for k, t in host.items()}
-    e2e_times, h2d_times = [], []
+    link = None if args.no_e2e else _pinned_link_probe(dev)
+    e2e_times, h2d_times, per_copy, host_setters = [], [], {k: [] for k in names}, []
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
-        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        h0.record()
-        m.diag = dbuf["diag"].copy_(host["diag"], non_blocking=True)
-        m.lower = dbuf["lower"].copy_(host["lower"], non_blocking=True)
-        m.upper = dbuf["upper"].copy_(host["upper"], non_blocking=True)
-        bb = dbuf["b"].copy_(host["b"], non_blocking=True)
-        h1.record()  # stream-ordered after the copies: their device time, no extra sync
-        xe, _, _ = mixed(m, bb, x0)
+        ev[0].record()
+        for j, k in enumerate(names):
+            dbuf[k].copy_(host[k], non_blocking=True)
+            ev[j + 1].record()  # stream-ordered after copy j: its device time alone
+        t1 = time.perf_counter()
+        m.diag, m.lower, m.upper = dbuf["diag"], dbuf["lower"], dbuf["upper"]
+        t2 = time.perf_counter()
+        xe, _, _ = mixed(m, dbuf["b"], x0)
         xs_host.copy_(xe, non_blocking=True)
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
-            h2d_times.append(h0.elapsed_time(h1) / 1e3)
+            h2d_times.append(ev[0].elapsed_time(ev[-1]) / 1e3)
+            for j, k in enumerate(names):
+                per_copy[k].append(ev[j].elapsed_time(ev[j + 1]) / 1e3)
+            host_setters.append(t2 - t1)
     # median over the steps (one slow step -- a host-side stall -- moved the
     # mean by up to 10 %); the mean is reported beside it
     e2e = max_over_ranks(statistics.median(e2e_times), world) if e2e_times else None
     e2e_mean = max_over_ranks(statistics.mean(e2e_times), world) if e2e_times else None
 
+    # --- FP64 comparison: the same system, the same API, the same K steps ---
+    x64 = None
+    if not args.no_fp64:
+        fp64 = PCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
+                         preconditioner="DIC")
+        m.invalidate_cache()
+        fp64(m, b, x0)  # one untimed solve (first launches, lazy module loading)
+        f_times = []
+        for _ in range(args.steps):
+            m.invalidate_cache()
+            torch.cuda.synchronize()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record()
+            x64, it64, res64 = fp64(m, b, x0)
+            f1.record()
+            torch.cuda.synchronize()
+            f_times.append(f0.elapsed_time(f1) / 1e3)
+        extra["fp64_pcg_s"] = statistics.mean(f_times)
+        extra["fp64_pcg_s_min_max"] = [min(f_times), max(f_times)]
+        extra["fp64_steps"] = len(f_times)
+        extra["fp64_iterations"] = it64
+        extra["fp64_true_rel_residual"] = true_rel_residual(m, x64, b)
+
     peaks = load_peaks()
     avg_ms = tot.value / max(cnt.value, 1)
-    achieved = b_amul(4, n, F) / (avg_ms * 1e-3) / 1e9
     sym = mixed._symmetric_storage and m.packed_sym32() is not None
     topo = m.topology()
-    design = design_bytes_ap(n, F, topo.n_slices, sym)
-    traffic = NCU_TRAFFIC_AP_256["sym" if sym else "full"] if args.n == 256 else None
+    design = design_bytes_ap(n, topo.n_slots, sym)
+    achieved = design / (avg_ms * 1e-3) / 1e9
+    survey = b_amul(4, n, F) / (avg_ms * 1e-3) / 1e9
+    traffic = traffic_from_profile(design)
     extra["iterations"] = iters[-1]
     extra["inner_iterations_per_s"] = iters[-1] / sec
     extra["outer_updates"] = mixed.last_result.outer_updates
@@ -458,45 +568,57 @@ def run_ours(args, rank, world, local):
         extra["fp64_iterations_per_s"] = extra["fp64_iterations"] / extra["fp64_pcg_s"]
     extra["amul"] = time_amul(m, dev)
 
-
     cpu = None
     if rank == 0 and world >= 1 and not args.no_cpu:
         t_dic, t_it, threads = cpu_sample(sysd, iters=20)
         n_it = extra.get("fp64_iterations") or iters[-1]
         cpu = {"value": t_dic + t_it * n_it, "unit": "s", "cores": threads, "kind": "port",
                "sample": (f"oracle restatement of the reference PCG+DIC: DIC factorisation + "
-                          f"20 threaded iterations at {args.n}^3, extrapolated to {n_it} "
-                          f"iterations"),
-               "cpu": cpu_model(), "dic_build_s": t_dic, "s_per_iteration": t_it}
+                          f"20 threaded iterations at {args.n}^3, extrapolated to the {n_it} "
+                          f"iterations of this run's FP64 GPU solve"),
+               "extrapolated": True, "cpu": cpu_model(), "dic_build_s": t_dic,
+               "s_per_iteration": t_it}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.replace("256^3", f"{args.n}^3"), "n_cells": n,
-                       "n_faces": F, "rel_tol": args.rel_tol, "rhs_seed": 2,
-                       "solver": f"mixed FP32/FP64 reliable-update PCG+DIC, delta={args.delta}",
-                       "l2": "no flush: resident inputs (~1.9 GB) exceed the 129 MB L2",
-                       "parallelism": f"replicas x{world}"},
+            "config": headline_config(args, n, F, world),
+            "solver": f"mixed FP32/FP64 reliable-update PCG+DIC, delta={args.delta}",
             "roofline": {"bound": "hbm",
                          "kernel": ("mp_ap_stream_kernel<%s> (FP32 Amul + p.Ap, bulk-copy "
                                     "staged)" % ("true: owner-side half of the symmetric matrix"
                                                  if sym else "false: both sides")),
                          "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                         "traffic": traffic, "bytes_per_launch": b_amul(4, n, F),
-                         "bytes_formula": "B_amul(4) = 12n + 16F (diag, x, y; lower, upper; "
-                                          "int32 owner, neighbour)",
-                         "design_bytes_per_launch": design,
-                         "design_achieved": design / (avg_ms * 1e-3) / 1e9,
-                         "design_frac": design / (avg_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                         "bytes_per_launch": design,
+                         "bytes_formula": ("12n + 2*n_slots + 8.5*n_slots/32 (p, diag, Ap; "
+                                           "owner-side slots; offset and mirror entries)" if sym
+                                           else "12n + 4*n_slots + 8*n_slots/32 (p, diag, Ap; "
+                                                "both slot sides; one {offset, mask} entry per "
+                                                "32-slot column)"),
+                         "n_slots": topo.n_slots,
+                         "traffic": traffic["bytes"] if traffic else None,
+                         "traffic_source": traffic,
+                         "frac_survey_bytes": survey / peaks["hbm_gbs"],
+                         "survey_bytes_per_launch": b_amul(4, n, F),
+                         "survey_bytes_formula": "B_amul(4) = 12n + 16F (diag, x, y; lower, "
+                                                 "upper; int32 owner, neighbour -- not read by "
+                                                 "this kernel)",
                          "timed_launches": cnt.value, "avg_launch_us": avg_ms * 1e3},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "s", "statistic": "median of the timed steps",
                     "mean": e2e_mean, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "h2d_s_median": statistics.median(h2d_times) if h2d_times else None},
+                    "h2d_s_median": statistics.median(h2d_times) if h2d_times else None,
+                    "h2d_s_per_array_median": {k: statistics.median(v) for k, v in
+                                               per_copy.items()} if h2d_times else None,
+                    "h2d_GBs": h2d / statistics.median(h2d_times) / 1e9 if h2d_times else None,
+                    "link_probe_GBs": link,
+                    "setters_host_s_median": (statistics.median(host_setters)
+                                              if host_setters else None),
+                    "host": _host_placement(dev)},
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "extra": extra,

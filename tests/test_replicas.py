@@ -73,6 +73,17 @@ def test_reference_arm_runs_on_rank_zero_only():
     assert line["impl"] == "reference" and line["n_gpus"] == 2
     assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    # the iteration count the sample extrapolates to comes from a full solve
+    # run first, and the config carries the same keys as the GPU arm's
+    assert line["extrapolated"] is True and line["full_solve"]["converged"]
+    assert line["full_solve"]["iterations"] > 1
+    import argparse
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    a = argparse.Namespace(n=8, rel_tol=1e-10)
+    assert line["config"] == bench.headline_config(a, 512, 3 * 8 * 8 * 7, 2)
 
 
 if __name__ == "__main__":
