@@ -32,10 +32,14 @@ def test_batched_systems_converge_independently(tmp_path, monkeypatch):
         bb = b.cpu().numpy()
         xh = x.cpu().numpy()
         r = bb - O.amul(own, nei, d, lo, up, xh)
-        assert np.linalg.norm(r) / np.linalg.norm(bb) < 1e-8
+        tr = np.linalg.norm(r) / np.linalg.norm(bb)
+        assert tr < 1e-8
         pd = O.dic_build(own, nei, d, up)
         o = O.pcg(own, nei, d, lo, up, bb, np.zeros_like(bb), pd, 0.0, 1e-12, 20000)
-        assert np.linalg.norm(xh - o.x) / np.linalg.norm(o.x) < 1e-5
+        # |x - x*|/|x*| <= kappa * |r|/|b|: the error is bounded by the system's
+        # own true residual (measured on GB300: at most 23x it over these six
+        # systems, 1.8e-7 at the largest)
+        assert np.linalg.norm(xh - o.x) / np.linalg.norm(o.x) < 50 * tr
         its.append(it)
     assert len(set(its)) > 1  # uneven systems stop at different iterations
 

@@ -48,7 +48,8 @@ def test_mixed_reaches_fp64_accuracy(N, rel):
     o = O.pcg(d["owner"], d["neighbour"], d["diag"], d["lower"], d["upper"], d["b"],
               np.zeros(d["n"]), pd, 0.0, rel * 1e-2, 20000, threads=8)
     err = np.linalg.norm(xh - o.x) / np.linalg.norm(o.x)
-    assert err < 1e3 * rel, err  # Poisson conditioning: |dx|/|x| <= kappa * |dr|/|b|
+    # |dx|/|x| <= kappa |dr|/|b|; measured on GB300: 11.7 rel (32^3) and 9.8 rel (48^3)
+    assert err < 30 * rel, err
     # the kept Krylov space: inner iterations stay close to FP64 PCG's
     o2 = O.pcg(d["owner"], d["neighbour"], d["diag"], d["lower"], d["upper"], d["b"],
                np.zeros(d["n"]), pd, 0.0, rel, 20000, threads=8)

@@ -55,7 +55,8 @@ def test_mixed_bicgstab_reaches_fp64_accuracy(N, rel):
     o = oracle_solve(d, rel * 1e-2)
     assert o.converged
     err = np.linalg.norm(xh - o.x) / np.linalg.norm(o.x)
-    assert err < 1e2 * rel, err
+    # measured on GB300: 2.7 rel (32^3, 1e-10), 1.25 rel (48^3, 1e-8), 0.29 rel (40^3, 1e-12)
+    assert err < 10 * rel, err
     # the kept Krylov space: inner iterations stay close to FP64 BiCGStab's
     # (the oracle's count has two checks per iteration plus the first)
     o2 = oracle_solve(d, rel)

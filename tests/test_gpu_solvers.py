@@ -132,21 +132,22 @@ def test_pcg_matches_oracle_iteration_counts(pre):
 
 def test_pcg_config1_against_reference():
     """32^3 Poisson, PCG+DIC to 1e-6 relative: same iteration count
-    as the reference (198, counting the iteration-0 check); x within 1e-8 of
-    the reference's x (the reference's own thread-dependent dot products
-    move its x by ~1e-9 at this depth), and within 1e-11 after 50 iterations."""
+    as the reference (198, counting the iteration-0 check); x within 2e-11 of
+    the reference's x (measured on GB300: 2.4e-12; the dot products sum in a
+    different order than the reference's, so the two trajectories drift apart
+    by rounding), and within 1e-12 after 50 iterations (measured 1.4e-13)."""
     c1 = c1_poisson(32)
     m = mat(c1["n"], c1["owner"], c1["neighbour"], c1["diag"], c1["lower"], c1["upper"])
     b = torch.as_tensor(c1["b"])
     s = PCGSolver(tolerance=0.0, rel_tol=1e-6, max_iter=1000, preconditioner="DIC")
     x, it, res = s(m, b, torch.zeros(c1["n"], dtype=f64))
     assert it == int(G["c1_pcg_iterations"]) == 198
-    assert relerr(x.cpu().numpy(), G["c1_pcg_x"]) < 1e-8
+    assert relerr(x.cpu().numpy(), G["c1_pcg_x"]) < 2e-11
     assert res / s.last_info.initial_residual < 1e-6
     s50 = PCGSolver(tolerance=0.0, rel_tol=0.0, max_iter=50, preconditioner="DIC")
     x50, it50, _ = s50(m, b, torch.zeros(c1["n"], dtype=f64))
     assert it50 == 51
-    assert relerr(x50.cpu().numpy(), G["c1_pcg50_x"]) < 1e-11
+    assert relerr(x50.cpu().numpy(), G["c1_pcg50_x"]) < 1e-12
 
 
 # --------------------------------------------------------------------------
