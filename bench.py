@@ -876,6 +876,90 @@ def run_batch64(args, rank, world, local):
                "setup_s": t_setup, "first_solve_incl_autotune_s": t_tune})
 
 
+def cpu_unrolled_adjoint(h, gamma, x0, target, dt, steps, threads):
+    """The adjoint workload on the host cores: the oracle's restatement of
+    fvm.laplacian, then ``steps`` implicit steps by the oracle's threaded
+    FP64 PCG+DIC to 1e-14 (all states kept), then the adjoint sweep -- one
+    transposed solve per step (right-hand side scaled by a power of two, as
+    the GPU does, so the 1e-30 breakdown test does not stop a small adjoint
+    solve) and the face gradient s_f (x_N - x_P)(lam_P/V_P - lam_N/V_N),
+    -s_b lam_P x_P / V_P on boundary faces.  Returns (loss, gradient,
+    forward s, backward s)."""
+    import math
+
+    from oracle import oracle as O
+
+    own_all, nei = h.numpy("owner"), h.numpy("neighbour")
+    S, dl, V = h.numpy("face_areas"), h.numpy("delta_coefficients"), h.numpy("cell_volumes")
+    nint = nei.shape[0]
+    own = own_all[:nint]
+    t0 = time.perf_counter()
+    lo, up, dg = O.laplacian(h.n_cells, own_all, nei, S, dl, gamma, V)
+    d = dg + 1.0 / dt
+    pd = O.dic_build(own, nei, d, up)
+    xs = [x0]
+    x = x0
+    for _ in range(steps):
+        x = O.pcg(own, nei, d, lo, up, x / dt, x, pd, 0.0, 1e-14, 50000, threads=threads).x
+        xs.append(x)
+    t1 = time.perf_counter()
+    diff = x - target
+    loss = float(diff @ diff)
+    g = 2.0 * diff
+    sd = np.sqrt((S * S).sum(axis=1)) * dl
+    grad = np.zeros(own_all.shape[0])
+    pdT = O.dic_build(own, nei, d, lo)
+    for t in range(steps, 0, -1):
+        k = 30 - math.frexp(float(np.abs(g).max()))[1]
+        sc = math.ldexp(1.0, k)
+        lam = O.pcg(own, nei, d, up, lo, g * sc, np.zeros_like(g), pdT, 0.0, 1e-14, 50000,
+                    threads=threads).x * math.ldexp(1.0, -k)
+        xt = xs[t]
+        lv = lam / V
+        grad[:nint] += sd[:nint] * (xt[nei] - xt[own]) * (lv[own] - lv[nei])
+        ob = own_all[nint:]
+        grad[nint:] += sd[nint:] * (-lv[ob] * xt[ob])
+        g = lam / dt
+    t2 = time.perf_counter()
+    return loss, grad, t1 - t0, t2 - t1
+
+
+def reference_gradient_24cube(dev) -> dict:
+    """The 24^3 case of the adjoint workload against the gradient the
+    reference itself computed (tests/golden/reference_unroll24.npz: its
+    fvm.laplacian under autograd and DifferentiableLinearSolve per step, PCG
+    to 1e-13 without preconditioner).  Inputs come from the same seeded
+    draws; the target x_T(gamma') is computed here by the GPU solver."""
+    from pyopenfoam_gb300 import PCGSolver
+    from pyopenfoam_gb300.differentiable.unrolled import UnrolledImplicitDiffusion
+    from pyopenfoam_gb300.mesh import HexMesh
+
+    path = os.path.join(ROOT, "tests", "golden", "reference_unroll24.npz")
+    if not os.path.exists(path):
+        return {"unavailable": "fixture missing"}
+    R = np.load(path)
+    h = HexMesh(24)
+    rng = np.random.default_rng(4)
+    gamma = rng.lognormal(0.0, 1.0, h.n_faces)
+    gamma2 = rng.lognormal(0.0, 1.0, h.n_faces)
+    x0 = rng.uniform(0.0, 1.0, h.n_cells)
+    sol = PCGSolver(tolerance=0.0, rel_tol=1e-14, max_iter=5000, preconditioner="none")
+    model = UnrolledImplicitDiffusion(h.to(dev), dt=1e-3, steps=20, checkpoint_every=5,
+                                      solver=sol)
+    T = lambda a: torch.as_tensor(a).to(dev)  # noqa: E731
+    target = model.final_state(T(gamma2), T(x0))
+    loss, grad = model.loss_and_grad(T(gamma), T(x0), target)
+    g = grad.cpu().numpy()
+    ref = R["grad_at_faces"]
+    return {"n_cells": h.n_cells, "sampled_faces": int(R["faces"].shape[0]),
+            "max_rel_err_sampled_faces": float(np.abs(g[R["faces"]] - ref).max()
+                                               / np.abs(ref).max()),
+            "grad_norm_rel_err": float(abs(np.linalg.norm(g) - float(R["grad_norm"]))
+                                       / float(R["grad_norm"])),
+            "loss_rel_err": float(abs(loss - float(R["loss"])) / float(R["loss"])),
+            "reference_solver": "PCGSolver(tolerance=0, rel_tol=1e-13, preconditioner='none')"}
+
+
 def run_adjoint96(args, rank, world, local):
     """Adjoint gradient through 20 implicit diffusion steps at 96^3."""
     from pyopenfoam_gb300 import PCGSolver
@@ -884,11 +968,13 @@ def run_adjoint96(args, rank, world, local):
 
     dev = torch.device("cuda", local)
     N = 96 if args.n == 256 else args.n
-    mesh = HexMesh(N, device=dev)
+    hm = HexMesh(N)
+    mesh = hm.to(dev)
     rng = np.random.default_rng(4)
-    gamma = torch.as_tensor(rng.lognormal(0.0, 1.0, mesh.n_faces)).to(dev)
-    gamma2 = torch.as_tensor(rng.lognormal(0.0, 1.0, mesh.n_faces)).to(dev)
-    x0 = torch.as_tensor(rng.uniform(0.0, 1.0, mesh.n_cells)).to(dev)
+    gamma_h = rng.lognormal(0.0, 1.0, mesh.n_faces)
+    gamma2_h = rng.lognormal(0.0, 1.0, mesh.n_faces)
+    x0_h = rng.uniform(0.0, 1.0, mesh.n_cells)
+    gamma, gamma2, x0 = (torch.as_tensor(a).to(dev) for a in (gamma_h, gamma2_h, x0_h))
     solver = PCGSolver(tolerance=0.0, rel_tol=1e-14, max_iter=50000, preconditioner="DIC")
     model = UnrolledImplicitDiffusion(mesh, dt=1e-3, steps=20, checkpoint_every=5, solver=solver)
     target = model.final_state(gamma2, x0)
@@ -913,6 +999,19 @@ def run_adjoint96(args, rank, world, local):
         errs.append(abs(fd - g) / max(abs(g), 1e-300))
     t_fd = time.perf_counter() - t0
     f_s, b_s = statistics.median(fw), statistics.median(bw)
+    ref24 = reference_gradient_24cube(dev)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = len(os.sched_getaffinity(0))
+        c_loss, c_grad, c_f, c_b = cpu_unrolled_adjoint(
+            hm, gamma_h, x0_h, target.cpu().numpy(), 1e-3, 20, threads)
+        gh = grad.cpu().numpy()
+        cpu = {"value": c_f + c_b, "unit": "s", "cores": threads, "kind": "port",
+               "sample": "full forward + backward (20 steps, all states kept) by the oracle's "
+                         "threaded PCG+DIC and a numpy face gradient",
+               "forward_s": c_f, "backward_s": c_b,
+               "grad_rel_err_gpu_vs_cpu": float(np.abs(gh - c_grad).max() / np.abs(c_grad).max()),
+               "loss_rel_err_gpu_vs_cpu": abs(loss - c_loss) / c_loss}
     if rank == 0:
         _line(args, world, "adjoint gradient of 20 implicit steps (96^3), "
               "forward + backward time", f_s + b_s, "s", False,
@@ -924,7 +1023,9 @@ def run_adjoint96(args, rank, world, local):
                "peak_bytes_all_states": peak_all, "loss": loss,
                "solver_iterations_per_solve": statistics.mean(iters),
                "fd_faces": len(errs), "fd_h": 1e-6, "fd_max_rel_err": max(errs),
-               "fd_median_rel_err": statistics.median(errs), "fd_seconds": t_fd})
+               "fd_median_rel_err": statistics.median(errs), "fd_seconds": t_fd,
+               "reference_gradient_24cube": ref24},
+              cpu_baseline=cpu)
 
 
 def _event_time(fn, reps: int = 5, warmup: int = 2) -> float:

@@ -91,6 +91,31 @@ def test_unrolled_gradient_against_reference_autograd():
     assert rel(xT.detach().cpu().numpy(), G["unroll_xT"]) < 1e-12
 
 
+def test_unrolled_gradient_against_reference_autograd_24cube():
+    """24^3 (13,824 cells, 20 steps): the gradient on 1024 seeded faces, its
+    norm and sum, the loss and x_T against the reference's own autograd chain
+    (reference_unroll24.npz, made by make_golden.py --unroll24 with the
+    reference's PCG to 1e-13, no preconditioner).  Both sides solve every
+    step to 1e-13..1e-14; measured on GB300: 3.1e-13 on the sampled faces,
+    2.9e-14 on the norm, 2.2e-14 on the loss."""
+    import os
+
+    R = np.load(os.path.join(os.path.dirname(FIXTURE), "reference_unroll24.npz"))
+    uc = unroll_case(24)
+    model = _model(uc, 5)
+    gamma = torch.as_tensor(uc["gamma"]).cuda()
+    x0 = torch.as_tensor(uc["x0"]).cuda()
+    target = torch.as_tensor(uc["target"]).cuda()
+    loss, grad = model.loss_and_grad(gamma, x0, target)
+    g = grad.cpu().numpy()
+    assert abs(loss - float(R["loss"])) <= 1e-12 * float(R["loss"])
+    assert rel(g[R["faces"]], R["grad_at_faces"]) < 1e-11
+    assert abs(np.linalg.norm(g) - float(R["grad_norm"])) <= 1e-12 * float(R["grad_norm"])
+    assert abs(g.sum() - float(R["grad_sum"])) <= 1e-9 * np.abs(g).sum()
+    xT = model.final_state(gamma, x0).cpu().numpy()
+    assert rel(xT[R["cells"]], R["xT_at_cells"]) < 1e-10
+
+
 def test_checkpoint_interval_does_not_change_the_gradient():
     uc = unroll_case(10)
     gamma = torch.as_tensor(uc["gamma"]).cuda()
