@@ -159,13 +159,14 @@ inline int wave_grid(K kernel, int block, long long work) {
 
 // Kernel timing probes (gbf_timing_enable): timing_begin returns true when
 // an event was recorded; the caller then calls timing_end after the launch.
-constexpr int kNumProbes = 5;
+constexpr int kNumProbes = 6;
 enum {
   kProbePcgAp = 0,
   kProbeMixedAp = 1,
   kProbeBicgAmul = 2,
   kProbeMixedTrue = 3,
-  kProbeMixedBicgAmul = 4
+  kProbeMixedBicgAmul = 4,
+  kProbeBatchedAp = 5
 };
 bool timing_begin(int probe, cudaStream_t s);
 void timing_end(int probe, cudaStream_t s);

@@ -28,13 +28,14 @@ import torch
 
 from .. import _lib
 from ..core.ldu_matrix import LduMatrix
-from .preconditioners import DICPreconditioner, DILUPreconditioner
 from .residual import ConvergenceInfo
 
 __all__ = ["BatchedPCGSolver", "BatchLayout", "autotune_cache_path"]
 
 BLOCK_SIZES = (128, 256, 512)
 TILE_CELLS = (1024, 2048, 4096, 8192)
+FORMS = {"plain": 0, "graph": 1, "persistent": 2, "persistent_graph": 3}
+TUNED_FORMS = ("graph", "persistent")
 
 
 def autotune_cache_path() -> str:
@@ -124,21 +125,29 @@ class BatchedPCGSolver:
     ``solve(matrices, sources, x0s=None)`` returns a list of
     ``(x, iterations, final_residual)``, one per system, with the same
     conventions as the single-system solvers; ``last_infos`` holds the
-    per-system ConvergenceInfo."""
+    per-system ConvergenceInfo.  ``form`` is one of ``FORMS`` or None (the
+    autotuner chooses; ``use_graph=False`` means ``"plain"``)."""
 
     def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 1000,
                  min_iter: int = 0, preconditioner: str = "DIC", *, delta: float = 0.1,
                  block_size: int | None = None, tile_cells: int | None = None,
-                 use_graph: bool = True, autotune: bool = True, check_every: int = 16) -> None:
+                 use_graph: bool = True, autotune: bool = True, check_every: int = 16,
+                 form: str | None = None, wavefront: str | None = None) -> None:
         self.tolerance, self.rel_tol = float(tolerance), float(rel_tol)
         self.max_iter, self.min_iter = int(max_iter), int(min_iter)
         self.precond = preconditioner.upper()
         if self.precond not in ("DIC", "DILU", "NONE"):
             raise ValueError(f"Unknown preconditioner '{preconditioner}'. Use 'DIC', 'DILU', "
                              "or 'none'.")
+        if form is not None and form not in FORMS:
+            raise ValueError(f"form must be one of {sorted(FORMS)}, got {form!r}")
+        if wavefront not in (None, "cooperative", "per_level"):
+            raise ValueError("wavefront must be 'cooperative', 'per_level' or None")
         self.delta = float(delta)
         self.block_size, self.tile_cells = block_size, tile_cells
-        self.use_graph, self.autotune = bool(use_graph), bool(autotune)
+        self.form = form if form is not None else (None if use_graph else "plain")
+        self.wavefront = wavefront
+        self.autotune = bool(autotune)
         self.check_every = int(check_every)
         self._layouts: dict = {}
         self.last_infos: list[ConvergenceInfo] = []
@@ -155,15 +164,55 @@ class BatchedPCGSolver:
             self._layouts = {key: hit}
         return hit
 
-    def _run(self, bl: BatchLayout, b: torch.Tensor, x: torch.Tensor, block: int, tile: int,
-             max_iter: int, tol: float, rel: float):
+    def _factor(self, bl: BatchLayout, wavefront: str) -> torch.Tensor | None:
+        """The FP64 DIC/DILU diagonal of the batch matrix, cached on it; its
+        level-scheduled wavefront runs in one cooperative launch or as one
+        launch per level (same bits)."""
+        if self.precond == "NONE":
+            return None
+        m = bl.matrix
+        key = ("batched_factor", self.precond)
+        hit = m._csr_cache.get(key)
+        if hit is not None and hit[0] == (m.diag._version, m.lower._version, m.upper._version,
+                                          m.diag.data_ptr(), m.lower.data_ptr(),
+                                          m.upper.data_ptr()):
+            return hit[1]
+        d = self._build_factor(bl, wavefront)
+        m._csr_cache[key] = ((m.diag._version, m.lower._version, m.upper._version,
+                              m.diag.data_ptr(), m.lower.data_ptr(), m.upper.data_ptr()), d)
+        return d
+
+    def _build_factor(self, bl: BatchLayout, wavefront: str) -> torch.Tensor:
         m = bl.matrix
         topo = m.topology()
-        pre = None
+        coef = m.packed()
+        d = torch.empty(m.n_cells, device=bl.device, dtype=torch.float64)
+        bar = _lib.wavefront_barrier(bl.device) if wavefront == "cooperative" else None
+        bptr = None if bar is None else bar.data_ptr()
+        L = _lib.lib()
+        st = _lib.stream_ptr(bl.device)
         if self.precond == "DIC":
-            pre = DICPreconditioner(m).precond_diag
-        elif self.precond == "DILU":
-            pre = DILUPreconditioner(m).precond_diag
+            sched = topo.dic_schedule()
+            _lib.check(L.gbf_dic_build_f64(topo.layout_ref, coef.data_ptr(), m.diag.data_ptr(),
+                                           sched.ptr.data_ptr(), sched.items.data_ptr(),
+                                           sched.n_levels, sched.max_level_size, d.data_ptr(),
+                                           bptr, st), "gbf_dic_build_f64")
+        else:
+            sched = topo.dilu_schedule()
+            _lib.check(L.gbf_dilu_build_f64(topo.layout_ref, m.lower.data_ptr(),
+                                            m.upper.data_ptr(), m.diag.data_ptr(),
+                                            sched.ptr.data_ptr(), sched.items.data_ptr(),
+                                            sched.n_levels, sched.max_level_size, d.data_ptr(),
+                                            bptr, st), "gbf_dilu_build_f64")
+        if bar is not None:
+            _lib.check_wavefront(bar, "batched factorisation", bl.device)
+        return d
+
+    def _run(self, bl: BatchLayout, b: torch.Tensor, x: torch.Tensor, block: int, tile: int,
+             max_iter: int, tol: float, rel: float, form: str, wavefront: str):
+        m = bl.matrix
+        topo = m.topology()
+        pre = self._factor(bl, wavefront)
         coef64 = m.packed()
         coef32 = m.packed(dtype=torch.float32)
         T = bl.tiles(tile)
@@ -177,46 +226,79 @@ class BatchedPCGSolver:
         _lib.check(L.gbf_batched_mixed_pcg_solve(
             topo.layout_ref, ctypes.byref(T.struct), coef64.data_ptr(), m.diag.data_ptr(),
             coef32.data_ptr(), None if pre is None else pre.data_ptr(), b.data_ptr(),
-            x.data_ptr(), self.delta, ctypes.byref(P), int(block), int(self.use_graph), R,
+            x.data_ptr(), self.delta, ctypes.byref(P), int(block), FORMS[form], R,
             ws.data_ptr(), ws.numel(), _lib.stream_ptr(bl.device)), "gbf_batched_mixed_pcg_solve")
         return list(R)
 
-    def _tune(self, bl: BatchLayout, b: torch.Tensor) -> tuple[int, int]:
-        if self.block_size and self.tile_cells:
-            return self.block_size, self.tile_cells
+    def _timed(self, fn, reps: int = 2) -> float:
+        times = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        return min(times)
+
+    def _tune(self, bl: BatchLayout, b: torch.Tensor) -> dict:
+        fixed = {"block": self.block_size, "tile": self.tile_cells, "form": self.form,
+                 "wavefront": self.wavefront}
+        if all(v is not None for v in fixed.values()):
+            return fixed
         name = torch.cuda.get_device_name(bl.device)
-        key = f"{name}|{bl.n_cells}|{len(bl.sizes)}|{bl.matrix.n_internal_faces}"
+        key = (f"{name}|{bl.n_cells}|{len(bl.sizes)}|{bl.matrix.n_internal_faces}|"
+               f"{self.precond}")
         path = autotune_cache_path()
-        cache = {}
         try:
             with open(path) as f:
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
-        if key in cache and not (self.block_size or self.tile_cells):
-            c = cache[key]
-            return int(c["block"]), int(c["tile"])
+        hit = cache.get(key)
+        if hit is not None and all(k in hit for k in fixed):
+            return {k: (fixed[k] if fixed[k] is not None else hit[k]) for k in fixed}
         if not self.autotune:
-            return self.block_size or 256, self.tile_cells or 4096
+            return {"block": self.block_size or 256, "tile": self.tile_cells or 4096,
+                    "form": self.form or "graph", "wavefront": self.wavefront or "cooperative"}
+        timings: dict = {}
+        # wavefront of the factorisation: both ways once (same bits)
+        if self.precond == "NONE":
+            wf = self.wavefront or "cooperative"
+        elif self.wavefront is None:
+            for w in ("cooperative", "per_level"):
+                timings[f"factor_{w}"] = self._timed(lambda w=w: self._build_factor(bl, w))
+            wf = min(("cooperative", "per_level"), key=lambda w: timings[f"factor_{w}"])
+        else:
+            wf = self.wavefront
+        forms = [self.form] if self.form else list(TUNED_FORMS)
         blocks = [self.block_size] if self.block_size else list(BLOCK_SIZES)
         tiles = [self.tile_cells] if self.tile_cells else list(TILE_CELLS)
-        best, timings = None, {}
         x = torch.zeros_like(b)
-        for blk in blocks:
-            for tl in tiles:
-                times = []
-                for _ in range(2):
-                    x.zero_()
-                    torch.cuda.synchronize(bl.device)
-                    t0 = time.perf_counter()
-                    self._run(bl, b, x, blk, tl, 24, 0.0, 0.0)
-                    torch.cuda.synchronize(bl.device)
-                    times.append(time.perf_counter() - t0)
-                t = min(times)
-                timings[f"{blk}x{tl}"] = t
-                if best is None or t < best[0]:
-                    best = (t, blk, tl)
-        cache[key] = {"block": best[1], "tile": best[2], "timings": timings}
+        best_per_form = {}
+        for fm in forms:
+            best = None
+            for blk in blocks:
+                for tl in tiles:
+                    t = self._timed(lambda: (x.zero_(), self._run(bl, b, x, blk, tl, 24, 0.0,
+                                                                  0.0, fm, wf)))
+                    timings[f"{fm}:{blk}x{tl}"] = t
+                    if best is None or t < best[0]:
+                        best = (t, blk, tl)
+            best_per_form[fm] = best
+        # the forms differ most once systems finish unevenly: one full solve each
+        choice = None
+        for fm, (_, blk, tl) in best_per_form.items():
+            if len(best_per_form) > 1:
+                t = self._timed(lambda: (x.zero_(), self._run(bl, b, x, blk, tl, self.max_iter,
+                                                              self.tolerance, self.rel_tol, fm,
+                                                              wf)), reps=1)
+                timings[f"full_solve:{fm}"] = t
+            else:
+                t = 0.0
+            if choice is None or t < choice[0]:
+                choice = (t, fm, blk, tl)
+        cfg = {"block": choice[2], "tile": choice[3], "form": choice[1], "wavefront": wf}
+        cache[key] = dict(cfg, timings=timings)
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)
             with open(path, "w") as f:
@@ -224,7 +306,7 @@ class BatchedPCGSolver:
         except OSError:
             pass
         self.last_config["timings"] = timings
-        return best[1], best[2]
+        return cfg
 
     def solve(self, matrices: list[LduMatrix], sources: list[torch.Tensor],
               x0s: list[torch.Tensor] | None = None, tolerance: float | None = None,
@@ -238,11 +320,13 @@ class BatchedPCGSolver:
         bl.set_coefficients(matrices)
         b = bl.gather(sources)
         x = bl.gather(x0s) if x0s is not None else torch.zeros_like(b)
-        block, tile = self._tune(bl, b)
-        self.last_config.update({"block": block, "tile": tile, "tiles": bl.tiles(tile).struct.n_tiles})
+        cfg = self._tune(bl, b)
+        self.last_config.update(cfg)
+        self.last_config["tiles"] = bl.tiles(cfg["tile"]).struct.n_tiles
         tol = self.tolerance if tolerance is None else float(tolerance)
         mi = self.max_iter if max_iter is None else int(max_iter)
-        res = self._run(bl, b, x, block, tile, mi, tol, self.rel_tol)
+        res = self._run(bl, b, x, cfg["block"], cfg["tile"], mi, tol, self.rel_tol, cfg["form"],
+                        cfg["wavefront"])
         self.last_results = res
         self.last_infos = []
         out = []

@@ -44,17 +44,69 @@ def test_batched_systems_converge_independently(tmp_path, monkeypatch):
     assert len(set(its)) > 1  # uneven systems stop at different iterations
 
 
-def test_batched_graph_and_plain_launches_match():
-    mats, rhs, _ = poisson_batch(4, lo=8, hi=16, seed=5)
-    a = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=256,
-                         tile_cells=1024, use_graph=True)
-    b = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=256,
-                         tile_cells=1024, use_graph=False)
-    xa = [x.cpu().numpy() for x, _, _ in a.solve(mats, rhs)]
-    xb = [x.cpu().numpy() for x, _, _ in b.solve(mats, rhs)]
-    for u, v in zip(xa, xb):
+@pytest.mark.parametrize("block,tile", [(256, 1024), (128, 2048), (512, 4096)])
+def test_batched_forms_give_identical_bits(block, tile):
+    """Graph replay, plain launches, the persistent cooperative launch and the
+    persistent launch captured in a graph: the same per-element arithmetic
+    and the same per-tile reductions in tile order, so x, the iteration and
+    update counts and the residuals agree bit for bit -- also for systems
+    that stop at very different iterations (sides 6..24)."""
+    mats, rhs, _ = poisson_batch(7, lo=6, hi=24, seed=5)
+    ref = None
+    for form in ("graph", "plain", "persistent", "persistent_graph"):
+        s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=block,
+                             tile_cells=tile, form=form, wavefront="cooperative")
+        xs = [x.cpu().numpy() for x, _, _ in s.solve(mats, rhs)]
+        got = (xs, [(r.iterations, r.outer_updates, r.status, r.final_residual)
+                    for r in s.last_results])
+        assert all(i.converged for i in s.last_infos), form
+        if ref is None:
+            ref = got
+            assert len({r[0] for r in got[1]}) > 1  # uneven stops
+            continue
+        for u, v in zip(got[0], ref[0]):
+            np.testing.assert_array_equal(u, v)
+        assert got[1] == ref[1], form
+
+
+def test_batched_factor_wavefront_forms_match():
+    mats, rhs, _ = poisson_batch(3, lo=8, hi=12, seed=6)
+    out = []
+    for wf in ("cooperative", "per_level"):
+        s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=256,
+                             tile_cells=1024, form="graph", wavefront=wf)
+        out.append([x.cpu().numpy() for x, _, _ in s.solve(mats, rhs)])
+    for u, v in zip(*out):
         np.testing.assert_array_equal(u, v)
-    assert [r.iterations for r in a.last_results] == [r.iterations for r in b.last_results]
+
+
+def test_batched_persistent_form_against_oracle(tmp_path, monkeypatch):
+    monkeypatch.setenv("GBFOAM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    mats, rhs, _ = poisson_batch(5, lo=6, hi=18, seed=12)
+    s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=3000, form="persistent")
+    out = s.solve(mats, rhs)
+    assert s.last_config["form"] == "persistent"
+    for (x, it, res), m, b, info in zip(out, mats, rhs, s.last_infos):
+        assert info.converged
+        own, nei, d, lo, up = _np(m)
+        bb, xh = b.cpu().numpy(), x.cpu().numpy()
+        tr = np.linalg.norm(bb - O.amul(own, nei, d, lo, up, xh)) / np.linalg.norm(bb)
+        assert tr < 1e-8
+        o = O.pcg(own, nei, d, lo, up, bb, np.zeros_like(bb), O.dic_build(own, nei, d, up), 0.0,
+                  1e-12, 20000)
+        assert np.linalg.norm(xh - o.x) / np.linalg.norm(o.x) < 50 * tr
+
+
+def test_batched_autotuner_considers_both_forms(tmp_path, monkeypatch):
+    monkeypatch.setenv("GBFOAM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    mats, rhs, _ = poisson_batch(3, lo=6, hi=10, seed=7)
+    s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=256)
+    s.solve(mats, rhs)
+    t = s.last_config["timings"]
+    assert any(k.startswith("graph:") for k in t) and any(k.startswith("persistent:") for k in t)
+    assert "full_solve:graph" in t and "full_solve:persistent" in t
+    assert "factor_cooperative" in t and "factor_per_level" in t
+    assert s.last_config["form"] in ("graph", "persistent")
 
 
 def test_batched_matches_single_system_solver_closely():
