@@ -218,12 +218,14 @@ def test_staged_float32_amul_matches_generic_gather(N):
     assert fault.value == 0
 
 
-@pytest.mark.parametrize("N", [7, 20, 64])
+@pytest.mark.parametrize("N", [7, 20, 32, 64])
 def test_symmetric_half_storage_amul_matches_full_packing(N):
     """A symmetric matrix (lower == upper) stored as its owner-side half:
     gbf_amul_sym_f32 -- staged (aligned) and global-memory (unaligned x)
     paths -- gives the bits of gbf_amul_f32 on the full packing and of the
-    float oracle; a non-symmetric matrix is refused by the packing."""
+    float oracle; a non-symmetric matrix is refused by the packing.  N = 32
+    and 64 put the y and z mirror coefficients in whole earlier slices
+    (staged as 128-byte runs); N = 7 and 20 leave them to the gathers."""
     import ctypes
 
     from pyopenfoam_gb300 import _lib

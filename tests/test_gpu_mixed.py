@@ -97,7 +97,7 @@ def test_mixed_zero_rhs_and_float32_rejected():
         PCGSolver()(m32, torch.ones(2), torch.zeros(2))
 
 
-@pytest.mark.parametrize("N", [20, 48])
+@pytest.mark.parametrize("N", [20, 48, 64])
 def test_mixed_symmetric_half_storage_gives_identical_solve(N):
     """The inner Amul on the owner-side half of a symmetric matrix gives the
     bits of the full-packing Amul, so the whole mixed solve -- iterations,
