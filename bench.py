@@ -72,20 +72,25 @@ def parse():
                         "--n would abbreviate)")
     p.add_argument("--rel-tol", type=float, default=1e-10)
     p.add_argument("--delta", type=float, default=0.1)
+    p.add_argument("--storage", choices=["auto", "full", "symmetric"], default="auto",
+                   help="inner FP32 Amul of the mixed PCG: both coefficient sides, the "
+                        "owner-side half of a symmetric matrix, or the solver's default")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     p.add_argument("--ref-sample-only", action="store_true",
                    help="--impl reference: skip the full solve that sets the iteration count")
-    p.add_argument("--workload", choices=["poisson256", "poisson32", "convdiff128", "batch64",
-                                          "adjoint96", "next", "assembly"],
+    p.add_argument("--workload", choices=["poisson256", "poisson256_renumbered", "poisson32",
+                                          "convdiff128", "batch64", "adjoint96", "next",
+                                          "assembly"],
                    default="poisson256",
                    help="poisson256 (default, the headline): 256^3 mixed vs FP64 PCG; "
                         "poisson32: 32^3 PCG+DIC to 1e-6; convdiff128: 128^3 jittered "
                         "convection-diffusion with PBiCGStab+DILU; batch64: 64 uneven Poisson "
                         "systems, batched; adjoint96: adjoint gradient of 20 implicit steps at 96^3; "
                         "next: geometry, correctors, GAMG and smoothers")
-    p.add_argument("--convdiff-legs", default="standard,reference,mixed,standard_1e-10,mixed_1e-10",
+    p.add_argument("--convdiff-legs", default="standard,reference,mixed,mixed_kernels,mixed_gather,"
+                                              "standard_1e-10,mixed_1e-10",
                    help="convdiff128: comma-separated solver legs to run")
     p.add_argument("--fd-faces", type=int, default=32, help="adjoint96: faces checked by central "
                                                             "differences")
@@ -453,8 +458,9 @@ def run_ours(args, rank, world, local):
     L = _lib.lib()
     extra = {}
 
+    kw = {} if args.storage == "auto" else {"symmetric_storage": args.storage == "symmetric"}
     mixed = MixedPrecisionPCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
-                                    preconditioner="DIC", delta=args.delta)
+                                    preconditioner="DIC", delta=args.delta, **kw)
 
     def step():
         m.invalidate_cache()  # re-pack + re-factorise each solve, like the reference
@@ -626,6 +632,128 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def renumbered_system(N: int, seed: int = 2, perm_seed: int = 5) -> dict:
+    """The N^3 Poisson system of the headline under a seeded random cell
+    renumbering: cell c becomes perm[c]; every face is re-oriented so that
+    owner < neighbour (lower and upper swapped with it) and the faces are
+    re-sorted into upper-triangular (owner, neighbour) order.  The same
+    matrix up to a symmetric permutation, but neighbour offsets are no longer
+    uniform per slice, so the offset compression and the fixed 3 + 3 gather
+    do not apply: the Amul reads an explicit int32 column per slot."""
+    from pyopenfoam_gb300.mesh.poisson import hex_poisson
+
+    d = hex_poisson(N, seed=seed)
+    n = d["n"]
+    perm = np.random.default_rng(perm_seed).permutation(n)
+    own, nei = perm[d["owner"]], perm[d["neighbour"]]
+    lo, up = d["lower"].copy(), d["upper"].copy()
+    swap = own > nei
+    own[swap], nei[swap] = nei[swap], own[swap]
+    lo[swap], up[swap] = d["upper"][swap], d["lower"][swap]
+    order = np.lexsort((nei, own))
+    diag, b = np.empty(n), np.empty(n)
+    diag[perm], b[perm] = d["diag"], d["b"]
+    return {"n": n, "owner": np.ascontiguousarray(own[order]),
+            "neighbour": np.ascontiguousarray(nei[order]),
+            "lower": np.ascontiguousarray(lo[order]), "upper": np.ascontiguousarray(up[order]),
+            "diag": diag, "b": b, "perm": perm}
+
+
+def generic_layout_bytes(topo, s: int) -> int:
+    """Bytes one Amul moves on a generic (not offset-uniform) layout: x,
+    diagonal, y (s B per cell), one coefficient and one int32 column per
+    slot, the 8 B {offset, mask} entry per 32-slot column (read to learn that
+    the column is explicit) and the per-slice start and width."""
+    return 3 * s * topo.n_cells + (s + 4) * topo.n_slots + 8 * (topo.n_slots // 32) \
+        + 8 * topo.n_slices
+
+
+def run_poisson256_renumbered(args, rank, world, local):
+    """The headline system under a random cell renumbering: mixed-precision
+    PCG+DIC to 1e-10 on the general gather path, with the Amul's roofline on
+    the bytes that path moves."""
+    import ctypes
+
+    from pyopenfoam_gb300 import MixedPrecisionPCGSolver, PCGSolver, _lib
+
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    sysd = renumbered_system(args.n)
+    t_setup = time.perf_counter() - t0
+    n, F = sysd["n"], int(sysd["owner"].shape[0])
+    m = make_matrix(sysd, dev)
+    b = torch.as_tensor(sysd["b"]).to(dev)
+    x0 = torch.zeros(n, dtype=torch.float64, device=dev)
+    topo = m.topology()
+    L = _lib.lib()
+    mixed = MixedPrecisionPCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
+                                    preconditioner="DIC", delta=args.delta)
+
+    def step():
+        m.invalidate_cache()
+        return mixed(m, b, x0)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    L.gbf_timing_enable(1, 100000)
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            x, it, _ = step()
+        e1.record()
+        torch.cuda.synchronize()
+    sec = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
+    cnt, tot = ctypes.c_int32(), ctypes.c_double()
+    _lib.check(L.gbf_timing_read(1, ctypes.byref(cnt), ctypes.byref(tot)))
+    L.gbf_timing_enable(0, 0)
+    avg_s = tot.value / max(cnt.value, 1) / 1e3
+    moved = generic_layout_bytes(topo, 4)
+    peaks = load_peaks()
+    extra = {"iterations": it, "outer_updates": mixed.last_result.outer_updates,
+             "true_rel_residual": true_rel_residual(m, x, b), "setup_s": t_setup,
+             "layout": {"n_slots": topo.n_slots, "slots_per_face": topo.n_slots / (2 * F),
+                        "n_slices": topo.n_slices, "max_width": topo.max_width,
+                        "offset_uniform_entries": topo.n_uniform_entries,
+                        "slot_columns": topo.n_slots // 32,
+                        "dic_levels": topo.dic_schedule().n_levels},
+             "amul": time_amul(m, dev)}
+    if not args.no_fp64:
+        fp64 = PCGSolver(tolerance=0.0, rel_tol=args.rel_tol, max_iter=50000,
+                         preconditioner="DIC")
+        m.invalidate_cache()
+        fp64(m, b, x0)
+        m.invalidate_cache()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        x64, it64, _ = fp64(m, b, x0)
+        f1.record()
+        torch.cuda.synchronize()
+        extra.update(fp64_pcg_s=f0.elapsed_time(f1) / 1e3, fp64_iterations=it64,
+                     speedup_vs_fp64=f0.elapsed_time(f1) / 1e3 / sec,
+                     x_rel_err_vs_fp64=float(torch.linalg.vector_norm(x - x64) /
+                                             torch.linalg.vector_norm(x64)))
+    if rank == 0:
+        _line(args, world, f"{args.n}^3 Poisson, random cell renumbering: mixed PCG+DIC to "
+              f"{args.rel_tol:g} relative, time", sec, "s", False,
+              {"workload": f"{args.n}^3 Poisson (unit-cube hex, x0 fixed value) under a seeded "
+                           "random cell permutation (seed 5), faces in upper-triangular order",
+               "n_cells": n, "n_faces": F, "rel_tol": args.rel_tol,
+               "l2": "no flush: resident inputs exceed the 129 MB L2"},
+              extra,
+              roofline={"bound": "hbm", "kernel": "mp_ap_kernel<generic> (FP32 Amul + p.Ap, "
+                                                  "explicit columns)",
+                        "achieved": moved / avg_s / 1e9, "peak": peaks["hbm_gbs"],
+                        "unit": "GB/s", "frac": moved / avg_s / 1e9 / peaks["hbm_gbs"],
+                        "peak_source": peaks["source"], "bytes_per_launch": moved,
+                        "bytes_formula": "12n + 8*n_slots + 8*n_slots/32 + 8*n_slices",
+                        "traffic": None, "timed_launches": cnt.value,
+                        "avg_launch_us": avg_s * 1e6},
+              clocks=clk.summary())
+
+
 def _line(args, world, metric, value, unit, hib, workload, extra, **kw):
     d = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
          "warmup": args.warmup, "ms_per_step": value * 1e3 if unit == "s" else None,
@@ -744,6 +872,10 @@ def run_convdiff128(args, rank, world, local):
         "reference": PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000,
                                      omega="reference"),
         "mixed": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000),
+        "mixed_kernels": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8,
+                                                       max_iter=4000, form="kernels"),
+        "mixed_gather": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000,
+                                                      form="gather"),
         "standard_1e-10": PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=4000,
                                           omega="standard"),
         "mixed_1e-10": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10,
@@ -772,7 +904,8 @@ def run_convdiff128(args, rank, world, local):
                             k_v_us=(tot.value * 1e3 / cnt.value) if cnt.value else None)
         else:
             res[key].update(checks=it, iterations=(it - 1) / 2, iterations_per_s=(it - 1) / 2 / t)
-    for key, ref in (("mixed", "standard"), ("mixed_1e-10", "standard_1e-10")):
+    for key, ref in (("mixed", "standard"), ("mixed_kernels", "standard"),
+                     ("mixed_gather", "standard"), ("mixed_1e-10", "standard_1e-10")):
         if key not in res or ref not in res:
             continue
         res[key]["speedup_vs_fp64"] = res[ref]["s"] / res[key]["s"]
@@ -810,7 +943,8 @@ def run_convdiff128(args, rank, world, local):
         v.pop("x")
     if rank == 0:
         names = {"standard": "omega_standard", "reference": "omega_reference",
-                 "mixed": "mixed_fp32_fp64", "standard_1e-10": "fp64_to_1e-10",
+                 "mixed": "mixed_fp32_fp64", "mixed_kernels": "mixed_six_kernels_staged",
+                 "mixed_gather": "mixed_six_kernels_gather", "standard_1e-10": "fp64_to_1e-10",
                  "mixed_1e-10": "mixed_to_1e-10"}
         extra = {names[k]: v for k, v in res.items()}
         extra["setup_s"] = t_setup
@@ -824,34 +958,103 @@ def run_convdiff128(args, rank, world, local):
 
 def run_batch64(args, rank, world, local):
     """64 independent Poisson systems (sides U{16..96}, seed 3), mixed
-    FP32/FP64 refined PCG+DIC to 1e-8: one batched solve vs 64 sequential
-    single-system solves."""
-    from pyopenfoam_gb300 import MixedPrecisionPCGSolver
+    FP32/FP64 refined PCG+DIC to 1e-8: the batched solve in its two forms --
+    CUDA-graph replay of per-phase kernels and one persistent cooperative
+    launch -- each with the autotuner's block and tile, against 64 sequential
+    single-system solves; every system's x against an FP64 GPU PCG+DIC solve
+    of the same system."""
+    import ctypes
+
+    from pyopenfoam_gb300 import MixedPrecisionPCGSolver, PCGSolver, _lib
     from pyopenfoam_gb300.mesh.batch import poisson_batch
     from pyopenfoam_gb300.solvers.batched import BatchedPCGSolver
+
+    import tempfile
 
     dev = torch.device("cuda", local)
     t0 = time.perf_counter()
     mats, rhs, sides = poisson_batch(64, 16, 96, sigma=0.5, seed=3, device=dev)
     t_setup = time.perf_counter() - t0
     n_total = sum(m.n_cells for m in mats)
-    bs = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000)
+    # tune afresh in every run (a private cache file), so the timings are this box's
+    os.environ["GBFOAM_AUTOTUNE_CACHE"] = os.path.join(tempfile.mkdtemp(), "autotune.json")
+    auto = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000)
     t0 = time.perf_counter()
-    bs.solve(mats, rhs)  # autotune (cached) + warm-up
+    auto.solve(mats, rhs)  # autotune (cached) + warm-up
     torch.cuda.synchronize()
     t_tune = time.perf_counter() - t0
-    for _ in range(max(args.warmup - 1, 0)):
-        bs.solve(mats, rhs)
-    ts = []
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        out = bs.solve(mats, rhs)
-        torch.cuda.synchronize()
-        ts.append(time.perf_counter() - t0)
-    t_batch = max_over_ranks(statistics.median(ts), world)
-    conv = sum(i.converged for i in bs.last_infos)
-    worst = max(true_rel_residual(m, x, b) for (x, _, _), m, b in zip(out, mats, rhs))
+    tuned = dict(auto.last_config)
+    timings = tuned.pop("timings", None)
+
+    forms = {}
+    for form in ("graph", "persistent"):
+        # the autotuner's best block and tile for this form (short fixed-iteration runs)
+        cand = {k.split(":", 1)[1]: v for k, v in (timings or {}).items()
+                if k.startswith(form + ":")}
+        blk, tl = (int(v) for v in min(cand, key=cand.get).split("x")) if cand else (256, 4096)
+        bs = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000, form=form,
+                              block_size=blk, tile_cells=tl, wavefront=tuned["wavefront"])
+        bs.solve(mats, rhs)  # per-form tuning of block and tile (cached), warm-up
+        for _ in range(max(args.warmup - 1, 0)):
+            bs.solve(mats, rhs)
+        ts = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = bs.solve(mats, rhs)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        cfg = {k: v for k, v in bs.last_config.items() if k != "timings"}
+        forms[form] = {"s": max_over_ranks(statistics.median(ts), world), "config": cfg,
+                       "out": out, "results": bs.last_results,
+                       "converged": sum(i.converged for i in bs.last_infos)}
+    head = tuned["form"] if tuned.get("form") in forms else "graph"
+    t_batch = forms[head]["s"]
+    out = forms[head]["out"]
+    res = forms[head]["results"]
+    same_bits = all(bool(torch.equal(a[0], b[0])) for a, b in
+                    zip(forms["graph"]["out"], forms["persistent"]["out"])) \
+        if forms["graph"]["config"]["block"] == forms["persistent"]["config"]["block"] and \
+        forms["graph"]["config"]["tile"] == forms["persistent"]["config"]["tile"] else None
+
+    # every system against the FP64 GPU solver: same tolerance, and 1e-12
+    errs, errs_tight, worst_true = [], [], 0.0
+    f64 = PCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000, preconditioner="DIC")
+    f64t = PCGSolver(tolerance=0.0, rel_tol=1e-12, max_iter=20000, preconditioner="DIC")
+    for (x, _, _), m, b in zip(out, mats, rhs):
+        xr, _, _ = f64(m, b, torch.zeros_like(b))
+        xt, _, _ = f64t(m, b, torch.zeros_like(b))
+        nr, nt = torch.linalg.vector_norm(xr), torch.linalg.vector_norm(xt)
+        errs.append(float(torch.linalg.vector_norm(x - xr) / nr))
+        errs_tight.append(float(torch.linalg.vector_norm(x - xt) / nt))
+        worst_true = max(worst_true, true_rel_residual(m, x, b))
+
+    # batched Amul roofline: plain launches with the timing probe, a fixed 64
+    # iterations during which every system is still running
+    L = _lib.lib()
+    rb = BatchedPCGSolver(tolerance=0.0, rel_tol=0.0, max_iter=64, form="plain",
+                          block_size=forms["graph"]["config"]["block"],
+                          tile_cells=forms["graph"]["config"]["tile"],
+                          wavefront=tuned["wavefront"])
+    rb.solve(mats, rhs)
+    _lib.check(L.gbf_timing_enable(1, 100000))
+    rb.solve(mats, rhs)
+    cnt, tot = ctypes.c_int32(), ctypes.c_double()
+    _lib.check(L.gbf_timing_read(5, ctypes.byref(cnt), ctypes.byref(tot)))
+    _lib.check(L.gbf_timing_enable(0, 0))
+    topo = rb.layout(mats).matrix.topology()
+    moved = design_bytes_ap(topo.n_cells, topo.n_slots, False)
+    avg_s = tot.value / max(cnt.value, 1) / 1e3
+    peaks = load_peaks()
+    roof = {"bound": "hbm", "kernel": "bmp_ap_kernel (batched FP32 Amul + p.Ap, one tile per "
+                                      "CTA, unstaged gather)",
+            "achieved": moved / avg_s / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": moved / avg_s / 1e9 / peaks["hbm_gbs"], "peak_source": peaks["source"],
+            "bytes_per_launch": moved,
+            "bytes_formula": "12n + 4*n_slots + 8*n_slots/32 over the padded batch layout",
+            "n_cells_padded": topo.n_cells, "n_slots": topo.n_slots, "traffic": None,
+            "timed_launches": cnt.value, "avg_launch_us": avg_s * 1e6}
+
     single = MixedPrecisionPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000)
     for m, b in zip(mats[:4], rhs[:4]):
         single(m, b, torch.zeros_like(b))
@@ -862,18 +1065,46 @@ def run_batch64(args, rank, world, local):
         single(m, b, torch.zeros_like(b))
     torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+
+        threads = len(os.sched_getaffinity(0))
+        host = [(m.owner.cpu().numpy(), m.neighbour.cpu().numpy(), m.diag.cpu().numpy(),
+                 m.lower.cpu().numpy(), m.upper.cpu().numpy(), b.cpu().numpy())
+                for m, b in zip(mats, rhs)]
+        t0 = time.perf_counter()
+        its = 0
+        for own, nei, d, lo, up, bb in host:
+            o = O.pcg(own, nei, d, lo, up, bb, np.zeros_like(bb), O.dic_build(own, nei, d, up),
+                      0.0, 1e-8, 20000, threads=threads)
+            its += o.iterations
+        cpu = {"value": time.perf_counter() - t0, "unit": "s", "cores": threads, "kind": "port",
+               "sample": "all 64 systems, one after another: the oracle's threaded FP64 "
+                         "PCG+DIC (the reference's algorithm) to 1e-8, DIC factorisation "
+                         "included", "iterations_total": its}
     if rank == 0:
+        its = [r.iterations for r in res]
         _line(args, world, "64 uneven Poisson systems, batched mixed PCG+DIC to 1e-8, "
               "time", t_batch, "s", False,
               {"workload": "64 uniform hex Poisson systems, sides U{16..96} (seed 3), gamma "
                            "LogNormal(0,0.5), mixed FP32/FP64 refined to 1e-8",
-               "n_cells": n_total, "sides": sides},
-              {"sequential_s": t_seq, "speedup_vs_sequential": t_seq / t_batch,
-               "converged": conv, "worst_true_rel_residual": worst,
-               "iterations_min_max": [min(r.iterations for r in bs.last_results),
-                                      max(r.iterations for r in bs.last_results)],
-               "autotuned": {k: v for k, v in bs.last_config.items()},
-               "setup_s": t_setup, "first_solve_incl_autotune_s": t_tune})
+               "n_cells": n_total, "sides": sides,
+               "l2": "no flush: the batch (~1.2 GB of matrix and vectors) exceeds the 129 MB L2"},
+              {"form": head, "autotuned": tuned, "autotune_timings": timings,
+               "graph_replay_s": forms["graph"]["s"], "persistent_s": forms["persistent"]["s"],
+               "graph_config": forms["graph"]["config"],
+               "persistent_config": forms["persistent"]["config"],
+               "forms_same_bits": same_bits,
+               "sequential_s": t_seq, "speedup_vs_sequential": t_seq / t_batch,
+               "converged": forms[head]["converged"], "worst_true_rel_residual": worst_true,
+               "x_rel_err_vs_fp64_same_tol_max": max(errs),
+               "x_rel_err_vs_fp64_same_tol_median": statistics.median(errs),
+               "x_rel_err_vs_fp64_1e-12_max": max(errs_tight),
+               "iterations_min_max": [min(its), max(its)],
+               "setup_s": t_setup, "first_solve_incl_autotune_s": t_tune},
+              roofline=roof, cpu_baseline=cpu)
 
 
 def cpu_unrolled_adjoint(h, gamma, x0, target, dt, steps, threads):
@@ -1324,6 +1555,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "poisson32":
         run_poisson32(args, rank, world, local)
+    elif args.workload == "poisson256_renumbered":
+        run_poisson256_renumbered(args, rank, world, local)
     elif args.workload == "convdiff128":
         run_convdiff128(args, rank, world, local)
     elif args.workload == "batch64":

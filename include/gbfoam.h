@@ -592,10 +592,16 @@ int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double*
  * and diagonal preconditioner and the same FP64 reliable updates as
  * gbf_mixed_pcg_solve (residual replacement keeping p, r~ and rho).
  * Convergence on true residuals only (the FP64 solver's half-step check on
- * s is not taken).  P->variant: 0 omega = (t.z)/(t.t) as the reference,
- * 1 the standard (t.s)/(t.t).  coef32 = FP32 packing of the FP64 matrix;
- * precond_d = FP64 DILU/DIC diagonal or NULL.  history / R as for
- * gbf_mixed_pcg_solve.  Replaces PBiCGSTABSolver._solve
+ * s is not taken).  P->variant bit 0: 0 omega = (t.z)/(t.t) as the
+ * reference, 1 the standard (t.s)/(t.t); bits 1-2, the form: 0 automatic
+ * (the persistent form up to 2^21 cells, the kernels above), 1 six kernels
+ * per iteration (bulk-copy staged Amul on aligned hex layouts), 2 the same
+ * with the plain L2 gather Amul, 3 the whole inner loop in one cooperative
+ * launch (phases separated by a bounded grid barrier; its dot products sum
+ * over its own grid, so it agrees with the kernels to rounding; a barrier
+ * wait that runs out gives status GBF_DEVICE_TIMEOUT).  coef32 = FP32
+ * packing of the FP64 matrix; precond_d = FP64 DILU/DIC diagonal or NULL.
+ * history / R as for gbf_mixed_pcg_solve.  Replaces PBiCGSTABSolver._solve
  * (solvers/pbicgstab.py:103) for the momentum solve.                        */
 size_t gbf_mixed_pbicgstab_workspace_bytes(int32_t n_cells);
 int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef64, const double* diag64,

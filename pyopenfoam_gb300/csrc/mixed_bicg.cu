@@ -31,6 +31,7 @@
 #include <math.h>
 #include <string.h>
 
+#include "barrier.cuh"
 #include "bulk.cuh"
 
 namespace gbf {
@@ -486,6 +487,270 @@ __global__ void mb_fold_kernel(int n, double* __restrict__ x, MbVecs v) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// The whole inner loop in one cooperative launch (systems up to
+// kMbPersistentMaxCells).  The same iteration, breakdown tests and reliable
+// updates as the per-phase kernels above; the phases are separated by the
+// bounded grid barrier instead of kernel boundaries, and every block reduces
+// the per-block partials itself, in the same fixed order, so that all blocks
+// hold the same scalars and take the same decisions without a state round
+// trip.  Consecutive reductions alternate between two partial buffers: a
+// block may write the next reduction's partials while a slower block still
+// reads the previous one.  Each block owns a fixed set of cells in every
+// phase; data other blocks rewrite inside the launch (y, z, x, the partials)
+// is read from L2.  The dot products reduce over this launch's grid, so the
+// results agree with the per-phase form to rounding, not bit for bit.
+// ---------------------------------------------------------------------------
+constexpr int kMbPersistentMaxCells = 1 << 21;
+
+struct MbRegs {
+  double rho, alpha, omega, beta, res0, res, rmax, target;
+  int inner, status, n_hist, phase, fold_pending, updates, branch;
+};
+
+// Sum of this reduction's per-block partials (index `which` of two),
+// identical in every block and broadcast to every thread of it (the block
+// reduction leaves its result in thread 0 only); `slot` is a shared double.
+__device__ __forceinline__ double mb_grid_sum(const double* part, int which, double* sh,
+                                              double* slot) {
+  const double t = reduce_partials(part + which * gridDim.x, (int)gridDim.x, sh);
+  __syncthreads();  // every thread has read the slot's previous value
+  if (threadIdx.x == 0) *slot = t;
+  __syncthreads();
+  return *slot;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kBlock, 3)
+    mb_persistent_kernel(gbf_layout L, const double* __restrict__ coef64,
+                         const double* __restrict__ diag64, const float* __restrict__ coef32,
+                         const double* __restrict__ b, double* __restrict__ x, MbVecs v,
+                         double* hist, int hist_cap, double delta, gbf_solve_params P,
+                         int standard_omega, GridBarrier* bar) {
+  __shared__ double sh[kBlock / 32];
+  __shared__ double bc[2];  // the grid sums, broadcast to the block
+  const unsigned G = gridDim.x;
+  const int n = L.n_cells;
+  const int c0 = blockIdx.x * kBlock + threadIdx.x, cs = G * kBlock;
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+  // two partial buffers of 2G doubles each
+  double* partbuf[2] = {v.partials, v.partials + 2 * G};
+  int red = 0;
+  MbRegs q;
+  {
+    const MbState* st = v.st;  // written by mb_init_kernel, a separate launch
+    q.rho = st->rho;
+    q.alpha = st->alpha;
+    q.omega = st->omega;
+    q.beta = st->beta;
+    q.res0 = st->res0;
+    q.res = st->res;
+    q.rmax = st->rmax;
+    q.target = st->target;
+    q.inner = st->inner;
+    q.status = st->status;
+    q.n_hist = st->n_hist;
+    q.phase = MB_NORMAL;
+    q.fold_pending = 0;
+    q.updates = 0;
+    q.branch = 0;
+  }
+  const long long limit = (long long)P.max_iter + 2;
+  bool ok = true;
+  for (long long it = 0; q.status == GBF_RUNNING && it < limit; ++it) {
+    // v = A32 y, r~.v -> alpha
+    {
+      double* part = partbuf[red & 1];
+      DFAcc a;
+      for (int c = c0; c < n; c += cs) {
+        const float yc = __ldcg(v.y + c);
+        const float yv = cell_amul_k<KIND, float, float, false, true>(L, coef32, v.d32, v.y, c, yc);
+        v.v[c] = yv;
+        a.add_prod(__ldg(v.rt + c), yv);
+      }
+      const double s0 = block_sum_df(a, sh);
+      if (threadIdx.x == 0) part[blockIdx.x] = s0;
+      if (!(ok = grid_barrier(bar, G))) break;
+      const double t0 = mb_grid_sum(part, 0, sh, &bc[0]);
+      ++red;
+      if (fabs(t0) < 1e-30) {
+        q.status = GBF_BREAKDOWN;  // pbicgstab.py:168-171
+        break;
+      }
+      q.alpha = q.rho / t0;
+    }
+    // s = r - alpha v, z = s / d_M, x32 += alpha y
+    {
+      const float alpha = (float)q.alpha;
+      for (int c = c0; c < n; c += cs) {
+        const float s = fmaf(-alpha, __ldcg(v.v + c), __ldcg(v.r + c));
+        v.s[c] = s;
+        v.z[c] = __ldg(v.rD + c) * s;
+        v.xlo[c] = fmaf(alpha, __ldcg(v.y + c), __ldcg(v.xlo + c));
+      }
+      if (!(ok = grid_barrier(bar, G))) break;
+    }
+    // t = A32 z, t.t, t.s (or t.z) -> omega or the t.t branch
+    {
+      double* part = partbuf[red & 1];
+      DFAcc a0, a1;
+      for (int c = c0; c < n; c += cs) {
+        const float zc = __ldcg(v.z + c);
+        const float tv = cell_amul_k<KIND, float, float, false, true>(L, coef32, v.d32, v.z, c, zc);
+        v.t[c] = tv;
+        a0.add_prod(tv, tv);
+        a1.add_prod(tv, standard_omega ? __ldcg(v.s + c) : zc);
+      }
+      const double s0 = block_sum_df(a0, sh);
+      const double s1 = block_sum_df(a1, sh);
+      if (threadIdx.x == 0) {
+        part[blockIdx.x] = s0;
+        part[G + blockIdx.x] = s1;
+      }
+      if (!(ok = grid_barrier(bar, G))) break;
+      const double t0 = mb_grid_sum(part, 0, sh, &bc[0]);
+      const double t1 = mb_grid_sum(part, 1, sh, &bc[1]);
+      ++red;
+      if (fabs(t0) < 1e-30) {
+        q.branch = 1;  // pbicgstab.py:196-208
+      } else {
+        q.branch = 0;
+        q.omega = t1 / t0;
+      }
+    }
+    // x32 += omega z (folded into x64 when an update is pending),
+    // r = s - omega t, r.r, r~.r -> beta, update decision
+    {
+      double* part = partbuf[red & 1];
+      const int branch = q.branch;
+      const float omega = (float)q.omega;
+      const bool fold = q.fold_pending != 0;
+      DFAcc arr, artr;
+      for (int c = c0; c < n; c += cs) {
+        float xl = __ldcg(v.xlo + c);
+        const float s = __ldcg(v.s + c);
+        float r = s;
+        if (branch == 0) {
+          xl = fmaf(omega, __ldcg(v.z + c), xl);
+          r = fmaf(-omega, __ldcg(v.t + c), s);
+        }
+        if (fold) {
+          x[c] = __ldcg(x + c) + (double)xl;
+          xl = 0.0f;
+        }
+        v.r[c] = r;
+        v.xlo[c] = xl;
+        arr.add_prod(r, r);
+        artr.add_prod(__ldg(v.rt + c), r);
+      }
+      const double s0 = block_sum_df(arr, sh);
+      const double s1 = block_sum_df(artr, sh);
+      if (threadIdx.x == 0) {
+        part[blockIdx.x] = s0;
+        part[G + blockIdx.x] = s1;
+      }
+      if (!(ok = grid_barrier(bar, G))) break;
+      const double trr = mb_grid_sum(part, 0, sh, &bc[0]);
+      const double trtr = mb_grid_sum(part, 1, sh, &bc[1]);
+      ++red;
+      q.inner += 1;
+      q.res = sqrt(trr);
+      if (branch == 0 && fabs(q.omega) < 1e-30) {
+        q.status = GBF_BREAKDOWN;  // pbicgstab.py:227-229
+        break;
+      } else if (fold) {
+        q.fold_pending = 0;
+        q.phase = MB_TRUE_RESIDUAL;
+      } else {
+        q.beta = branch == 0 ? (trtr / q.rho) * (q.alpha / q.omega) : (trtr / q.rho) * q.alpha;
+        q.rho = trtr;
+        q.rmax = fmax(q.rmax, q.res);
+        if (q.res < delta * q.rmax || q.res < q.target || q.inner >= P.max_iter) {
+          q.fold_pending = 1;
+        } else if (fabs(trtr) < 1e-30) {
+          q.status = GBF_BREAKDOWN;  // the next iteration's rho test
+          break;
+        }
+      }
+    }
+    // r64 = b - A64 x64, r = (float) r64, |r64|, r~.r -> convergence, beta
+    if (q.phase == MB_TRUE_RESIDUAL) {
+      double* part = partbuf[red & 1];
+      double rr = 0.0;
+      DFAcc artr;
+      for (int c = c0; c < n; c += cs) {
+        const double xc = __ldcg(x + c);
+        const double y = cell_amul<double, double, false, true>(L, coef64, diag64, x, c, xc);
+        const double rh = __dsub_rn(__ldg(b + c), y);
+        const float r = (float)rh;
+        v.r[c] = r;
+        rr = fma(rh, rh, rr);
+        artr.add_prod(__ldg(v.rt + c), r);
+      }
+      rr = block_sum(rr, sh);
+      const double rtr = block_sum_df(artr, sh);
+      if (threadIdx.x == 0) {
+        part[blockIdx.x] = rr;
+        part[G + blockIdx.x] = rtr;
+      }
+      if (!(ok = grid_barrier(bar, G))) break;
+      const double trr = mb_grid_sum(part, 0, sh, &bc[0]);
+      const double trtr = mb_grid_sum(part, 1, sh, &bc[1]);
+      ++red;
+      q.res = sqrt(trr);
+      q.updates += 1;
+      if (lead && q.n_hist < hist_cap) hist[q.n_hist] = q.res;
+      q.n_hist += 1;
+      q.phase = MB_NORMAL;
+      if (mb_converged(q.res, q.res0, q.inner, P)) {
+        q.status = GBF_CONVERGED;
+        break;
+      } else if (q.inner >= P.max_iter) {
+        q.status = GBF_MAX_ITER;
+        break;
+      }
+      q.beta = q.branch == 0 ? (trtr / q.rho) * (q.alpha / q.omega) : (trtr / q.rho) * q.alpha;
+      q.rho = trtr;
+      q.rmax = q.res;
+      if (fabs(trtr) < 1e-30) {
+        q.status = GBF_BREAKDOWN;
+        break;
+      }
+    }
+    // p = r + beta (p - omega v), y = p / d_M
+    {
+      const float beta = (float)q.beta;
+      const float omega = q.branch == 0 ? (float)q.omega : 1.0f;
+      for (int c = c0; c < n; c += cs) {
+        const float p = fmaf(beta, fmaf(-omega, __ldcg(v.v + c), __ldcg(v.p + c)),
+                             __ldcg(v.r + c));
+        v.p[c] = p;
+        v.y[c] = __ldg(v.rD + c) * p;
+      }
+      if (!(ok = grid_barrier(bar, G))) break;
+    }
+  }
+  if (!ok) return;  // the host reads the barrier's fault word
+  // fold the remaining FP32 correction of this block's own cells
+  for (int c = c0; c < n; c += cs) {
+    const float xl = __ldcg(v.xlo + c);
+    if (xl != 0.0f) x[c] = __ldcg(x + c) + (double)xl;
+    v.xlo[c] = 0.0f;
+  }
+  if (lead) {
+    MbState* st = v.st;
+    st->rho = q.rho;
+    st->alpha = q.alpha;
+    st->omega = q.omega;
+    st->beta = q.beta;
+    st->res = q.res;
+    st->inner = q.inner;
+    st->status = q.status;
+    st->n_hist = q.n_hist;
+    st->updates = q.updates;
+  }
+}
+
 static size_t mb_a256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr int kMbVectors = 11;
 
@@ -496,8 +761,32 @@ using namespace gbf;
 extern "C" size_t gbf_mixed_pbicgstab_workspace_bytes(int32_t n) {
   if (n < 0) return 0;
   return kMbVectors * mb_a256(sizeof(float) * (size_t)n) +
-         mb_a256(sizeof(double) * 2 * kMaxGrid) + mb_a256(sizeof(MbState));
+         mb_a256(sizeof(double) * 2 * kMaxGrid) + mb_a256(sizeof(MbState)) +
+         mb_a256(sizeof(GridBarrier));
 }
+
+namespace gbf {
+// Resident blocks of the persistent form (occupancy x SMs, at most one per
+// 256 cells and kMaxGrid / 2 for the two partial buffers); 0 when the
+// device cannot launch it cooperatively.
+template <int KIND>
+static int mb_persistent_grid(int n) {
+  int dev = 0, sms = 0, coop = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mb_persistent_kernel<KIND>, kBlock,
+                                                    0) != cudaSuccess ||
+      per_sm <= 0)
+    return 0;
+  long long g = (long long)per_sm * sms;
+  const long long need = ((long long)n + kBlock - 1) / kBlock;
+  if (g > need) g = need;
+  if (g > kMaxGrid / 2) g = kMaxGrid / 2;
+  return g < 1 ? 1 : (int)g;
+}
+}  // namespace gbf
 
 extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef64,
                                          const double* diag64, const float* coef32,
@@ -535,12 +824,51 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
   v.partials = reinterpret_cast<double*>(w + kMbVectors * vb);
   v.st = reinterpret_cast<MbState*>(w + kMbVectors * vb +
                                     mb_a256(sizeof(double) * 2 * kMaxGrid));
-  const int standard_omega = P->variant == 1 ? 1 : 0;
+  GridBarrier* bar = reinterpret_cast<GridBarrier*>(
+      w + kMbVectors * vb + mb_a256(sizeof(double) * 2 * kMaxGrid) + mb_a256(sizeof(MbState)));
+  GBF_REQUIRE(P->variant >= 0 && P->variant <= 7, "mixed_pbicgstab: variant must be 0..7");
+  const int standard_omega = P->variant & 1;
+  const int form = P->variant >> 1;  // 0 auto, 1 kernels, 2 kernels + gather, 3 persistent
 
   const int Gi = wave_grid(mb_init_kernel, kBlock, n);
   const bool hex = layout_kind(*L) == kLayoutHex33;
+  // the whole inner loop in one cooperative launch (auto: up to 2^21 cells)
+  if (form == 3 || (form == 0 && n <= kMbPersistentMaxCells)) {
+    const int Gq = hex ? mb_persistent_grid<kLayoutHex33>(n) : mb_persistent_grid<kLayoutGeneric>(n);
+    GBF_REQUIRE(Gq > 0 || form != 3, "mixed_pbicgstab: the device cannot run the persistent form");
+    if (Gq > 0) {
+      GBF_CHECK_CUDA(cudaMemsetAsync(v.st, 0, sizeof(MbState), s));
+      GBF_CHECK_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), s));
+      mb_init_kernel<<<Gi, kBlock, 0, s>>>(*L, coef64, diag64, pd, b, x, v, hist, *P);
+      GBF_CHECK_LAUNCH();
+      gbf_layout Lc = *L;
+      gbf_solve_params Pc = *P;
+      int so = standard_omega, hc = hist_cap;
+      double dl = delta;
+      void* args[] = {&Lc, (void*)&coef64, (void*)&diag64, (void*)&coef32, (void*)&b, &x, &v,
+                      &hist, &hc, &dl, &Pc, &so, &bar};
+      GBF_CHECK_CUDA(cudaLaunchCooperativeKernel(
+          hex ? (const void*)mb_persistent_kernel<kLayoutHex33>
+              : (const void*)mb_persistent_kernel<kLayoutGeneric>,
+          dim3(Gq), dim3(kBlock), args, 0, s));
+      MbState hs;
+      GridBarrier hb;
+      GBF_CHECK_CUDA(cudaMemcpyAsync(&hs, v.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+      GBF_CHECK_CUDA(cudaMemcpyAsync(&hb, bar, sizeof(hb), cudaMemcpyDeviceToHost, s));
+      GBF_CHECK_CUDA(cudaStreamSynchronize(s));
+      R->iterations = hs.inner + 1;
+      R->status = hb.fault ? GBF_DEVICE_TIMEOUT
+                           : (hs.status == GBF_RUNNING ? GBF_MAX_ITER : hs.status);
+      R->final_residual = hs.res;
+      R->initial_residual = hs.res0;
+      R->inner_iterations = hs.inner;
+      R->outer_updates = hs.updates;
+      R->launches = 2;
+      return GBF_OK;
+    }
+  }
   // staged Amul: hex layout, 16-byte aligned coefficient / vector streams
-  const bool staged = hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
+  const bool staged = form != 2 && hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
   const int n_tiles = n / kTileCells;
   const long long tile_work = (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells;
   const int Ga = staged ? wave_grid(mb_amul_stream_kernel<0>, kTileCells, tile_work)

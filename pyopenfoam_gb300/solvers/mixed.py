@@ -126,11 +126,18 @@ class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
     Convergence is checked on the true residual only, once per update, so
     the half-step check on s is not taken.  ``omega`` (keyword only):
     ``"standard"`` (default here) takes (t.s)/(t.t); ``"reference"`` takes
-    the reference's (t.z)/(t.t)."""
+    the reference's (t.z)/(t.t).  ``form`` (keyword only): ``"persistent"``
+    runs the whole inner loop in one cooperative launch, ``"kernels"`` six
+    launches per iteration (bulk-copy staged Amul on hex layouts),
+    ``"gather"`` the same with the plain L2 gather Amul; ``"auto"`` takes
+    the persistent form up to 2^21 cells and the kernels above."""
+
+    FORMS = {"auto": 0, "kernels": 1, "gather": 2, "persistent": 3}
 
     def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 1000,
                  min_iter: int = 0, verbose: bool = False, preconditioner: str = "DILU", *,
-                 omega: str = "standard", delta: float = 0.1, check_every: int = 32) -> None:
+                 omega: str = "standard", delta: float = 0.1, check_every: int = 32,
+                 form: str = "auto") -> None:
         super().__init__(tolerance=tolerance, rel_tol=rel_tol, max_iter=max_iter,
                          min_iter=min_iter, verbose=verbose)
         self._precond_type = preconditioner.upper()
@@ -138,7 +145,10 @@ class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
             raise ValueError(f"omega must be 'reference' or 'standard', got {omega!r}")
         if not 0.0 < delta < 1.0:
             raise ValueError(f"delta must be in (0, 1), got {delta}")
+        if form not in self.FORMS:
+            raise ValueError(f"form must be one of {sorted(self.FORMS)}, got {form!r}")
         self._omega = omega
+        self._form = form
         self._delta = float(delta)
         self._check_every = int(check_every)
         self.last_result: _lib.SolveResult | None = None
@@ -178,7 +188,8 @@ class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
                          dtype=torch.uint8)
         P = _lib.SolveParams(float(monitor.tolerance), float(monitor.rel_tol), int(max_iter),
                              int(monitor.min_iter), self._check_every,
-                             1 if self._omega == "standard" else 0)
+                             (1 if self._omega == "standard" else 0)
+                             | (self.FORMS[self._form] << 1))
         R = _lib.SolveResult()
         _lib.check(
             L.gbf_mixed_pbicgstab_solve(topo.layout_ref, coef64.data_ptr(),
@@ -191,8 +202,9 @@ class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
         )
         self.last_result = R
         if R.status == _lib.GBF_DEVICE_TIMEOUT:
-            raise RuntimeError("gbf_mixed_pbicgstab_solve: a bounded wait on a staged copy ran "
-                               "out inside the Amul kernel; the result is invalid")
+            raise RuntimeError("gbf_mixed_pbicgstab_solve: a bounded wait (a staged copy in the "
+                               "Amul kernel, or a grid barrier of the persistent form) ran out; "
+                               "the result is invalid")
         nh = min(R.outer_updates + 1, cap) if n > 0 else 1
         monitor.record(hist[:nh].tolist() if n > 0 else [0.0])
         info = monitor.build_info(converged=(R.status == _lib.GBF_CONVERGED))

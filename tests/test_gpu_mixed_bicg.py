@@ -39,11 +39,15 @@ def oracle_solve(d, rel, omega="standard", max_iter=20000):
                        np.zeros(d["n"]), pd, 0.0, rel, max_iter, threads=8, omega=omega)
 
 
+FORMS = ("persistent", "kernels", "gather")
+
+
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("N,rel", [(32, 1e-10), (48, 1e-8), (40, 1e-12)])
-def test_mixed_bicgstab_reaches_fp64_accuracy(N, rel):
+def test_mixed_bicgstab_reaches_fp64_accuracy(N, rel, form):
     d = convection_diffusion(N, seed=1)
     m = mat(d)
-    s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=rel, max_iter=5000)
+    s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=rel, max_iter=5000, form=form)
     x, it, res = s(m, torch.as_tensor(d["b"]), torch.zeros(d["n"], dtype=f64))
     assert s.last_info.converged
     xh = x.cpu().numpy()
@@ -88,8 +92,9 @@ def test_mixed_bicgstab_matches_fp64_gpu_solver(pre):
     assert err < 1e-8, float(err)
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("permute", [False, True])
-def test_mixed_bicgstab_reference_omega_and_generic_layout(permute):
+def test_mixed_bicgstab_reference_omega_and_generic_layout(permute, form):
     """The reference's omega = (t.z)/(t.t) on a diagonally dominant system,
     on the hex layout and on shuffled, non-triangular addressing (generic
     gather)."""
@@ -97,7 +102,7 @@ def test_mixed_bicgstab_reference_omega_and_generic_layout(permute):
     d["b"] = d["r"]
     m = mat(d)
     s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=500,
-                                      omega="reference")
+                                      omega="reference", form=form)
     x, it, _ = s(m, torch.as_tensor(d["b"]), torch.zeros(d["n"], dtype=f64))
     assert s.last_info.converged
     xh = x.cpu().numpy()
@@ -106,25 +111,29 @@ def test_mixed_bicgstab_reference_omega_and_generic_layout(permute):
     assert np.linalg.norm(xh - o.x) / np.linalg.norm(o.x) < 1e-9
 
 
-def test_mixed_bicgstab_edge_cases():
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_bicgstab_edge_cases(form):
+    from functools import partial
+
+    MixedPrecisionPBiCGSTABSolver_ = partial(MixedPrecisionPBiCGSTABSolver, form=form)
     d = convection_diffusion(12, seed=5)
     m = mat(d)
     n = d["n"]
     b = torch.as_tensor(d["b"])
     # zero right-hand side: converged at the first check, x stays zero
-    s = MixedPrecisionPBiCGSTABSolver(tolerance=1e-12, rel_tol=0.0, max_iter=100)
+    s = MixedPrecisionPBiCGSTABSolver_(tolerance=1e-12, rel_tol=0.0, max_iter=100)
     x, it, res = s(m, torch.zeros(n, dtype=f64), torch.zeros(n, dtype=f64))
     assert s.last_info.converged and it == 1 and res == 0.0
     assert torch.count_nonzero(x) == 0
     # max_iter = 0: x0 unchanged, not converged
     x0 = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, n))
-    s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=0)
+    s = MixedPrecisionPBiCGSTABSolver_(tolerance=0.0, rel_tol=1e-10, max_iter=0)
     x, it, res = s(m, b, x0)
     assert not s.last_info.converged
     assert torch.equal(x.cpu(), x0)
     # iteration limit: the FP32 correction is folded into x and the last
     # reported residual is the true residual of that x
-    s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-14, max_iter=7)
+    s = MixedPrecisionPBiCGSTABSolver_(tolerance=0.0, rel_tol=1e-14, max_iter=7)
     x, it, res = s(m, b, torch.zeros(n, dtype=f64))
     assert not s.last_info.converged
     # the limit, plus the folding iteration unless a fold was already due
@@ -133,13 +142,13 @@ def test_mixed_bicgstab_edge_cases():
                                                          rel=1e-6)
     # an initial guess that already meets the absolute tolerance is returned
     o = oracle_solve(d, 1e-13)
-    s = MixedPrecisionPBiCGSTABSolver(tolerance=1e-8, rel_tol=0.0, max_iter=500)
+    s = MixedPrecisionPBiCGSTABSolver_(tolerance=1e-8, rel_tol=0.0, max_iter=500)
     x, it, _ = s(m, b, torch.as_tensor(o.x))
     assert it == 1 and torch.equal(x.cpu(), torch.as_tensor(o.x))
     # breakdown on a zero matrix (r~.v = 0), as the reference reports it
     z = dict(d, diag=np.zeros(n), lower=np.zeros_like(d["lower"]),
              upper=np.zeros_like(d["upper"]))
-    s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=50,
+    s = MixedPrecisionPBiCGSTABSolver_(tolerance=0.0, rel_tol=1e-8, max_iter=50,
                                       preconditioner="none")
     x, it, _ = s(mat(z), b, torch.zeros(n, dtype=f64))
     assert not s.last_info.converged
@@ -152,3 +161,24 @@ def test_mixed_bicgstab_by_name():
     d = convection_diffusion(16, seed=2)
     x, it, _ = s(mat(d), torch.as_tensor(d["b"]), torch.zeros(d["n"], dtype=f64))
     assert s.last_info.converged and true_rel(d, x.cpu().numpy()) < 1e-9
+
+
+def test_mixed_bicgstab_forms_agree():
+    """The persistent form and the per-iteration kernels run the same
+    iteration; their dot products sum over different grids, so x agrees to
+    rounding amplified by the Krylov recurrence -- and both reach the same
+    true residual bound.  An unknown form is refused."""
+    d = convection_diffusion(40, seed=4)
+    m = mat(d)
+    b = torch.as_tensor(d["b"])
+    xs = {}
+    for form in FORMS:
+        s = MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=3000, form=form)
+        x, it, _ = s(m, b, torch.zeros(d["n"], dtype=f64))
+        assert s.last_info.converged and true_rel(d, x.cpu().numpy()) < 1e-10
+        xs[form] = x
+    ref = xs["kernels"]
+    for form in ("persistent", "gather"):
+        assert float(torch.linalg.vector_norm(xs[form] - ref) / torch.linalg.vector_norm(ref)) < 1e-8
+    with pytest.raises(ValueError, match="form"):
+        MixedPrecisionPBiCGSTABSolver(form="fastest")
