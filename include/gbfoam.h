@@ -594,7 +594,8 @@ int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double*
  * Convergence on true residuals only (the FP64 solver's half-step check on
  * s is not taken).  P->variant bit 0: 0 omega = (t.z)/(t.t) as the
  * reference, 1 the standard (t.s)/(t.t); bits 1-2, the form: 0 automatic
- * (the persistent form up to 2^21 cells, the kernels above), 1 six kernels
+ * (the persistent form up to 2^16 cells, the kernels with the plain gather
+ * up to 2^22, the staged kernels above), 1 six kernels
  * per iteration (bulk-copy staged Amul on aligned hex layouts), 2 the same
  * with the plain L2 gather Amul, 3 the whole inner loop in one cooperative
  * launch (phases separated by a bounded grid barrier; its dot products sum

@@ -488,9 +488,8 @@ __global__ void mb_fold_kernel(int n, double* __restrict__ x, MbVecs v) {
 }
 
 // ---------------------------------------------------------------------------
-// The whole inner loop in one cooperative launch (systems up to
-// kMbPersistentMaxCells).  The same iteration, breakdown tests and reliable
-// updates as the per-phase kernels above; the phases are separated by the
+// The whole inner loop in one cooperative launch.  The same iteration,
+// breakdown tests and reliable updates as the per-phase kernels above; the phases are separated by the
 // bounded grid barrier instead of kernel boundaries, and every block reduces
 // the per-block partials itself, in the same fixed order, so that all blocks
 // hold the same scalars and take the same decisions without a state round
@@ -501,7 +500,14 @@ __global__ void mb_fold_kernel(int n, double* __restrict__ x, MbVecs v) {
 // is read from L2.  The dot products reduce over this launch's grid, so the
 // results agree with the per-phase form to rounding, not bit for bit.
 // ---------------------------------------------------------------------------
-constexpr int kMbPersistentMaxCells = 1 << 21;
+// Automatic form choice, from a sweep of the three forms on GB300
+// (convection-diffusion systems, 16^3 .. 128^3, us per inner iteration): the
+// single launch wins while the per-kernel launch gaps dominate (22.6 against
+// 29.5 at 32^3), the plain L2 gather from 48^3 on (30.7 against 36.0
+// persistent and 35.3 staged at 48^3; 81.1 against 84.5 staged at 128^3), and
+// the staged stream where blocks have many tiles each.
+constexpr int kMbAutoPersistentCells = 1 << 16;
+constexpr int kMbAutoGatherCells = 1 << 22;
 
 struct MbRegs {
   double rho, alpha, omega, beta, res0, res, rmax, target;
@@ -832,8 +838,8 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
 
   const int Gi = wave_grid(mb_init_kernel, kBlock, n);
   const bool hex = layout_kind(*L) == kLayoutHex33;
-  // the whole inner loop in one cooperative launch (auto: up to 2^21 cells)
-  if (form == 3 || (form == 0 && n <= kMbPersistentMaxCells)) {
+  // the whole inner loop in one cooperative launch (auto: up to 2^16 cells)
+  if (form == 3 || (form == 0 && n <= kMbAutoPersistentCells)) {
     const int Gq = hex ? mb_persistent_grid<kLayoutHex33>(n) : mb_persistent_grid<kLayoutGeneric>(n);
     GBF_REQUIRE(Gq > 0 || form != 3, "mixed_pbicgstab: the device cannot run the persistent form");
     if (Gq > 0) {
@@ -868,7 +874,8 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
     }
   }
   // staged Amul: hex layout, 16-byte aligned coefficient / vector streams
-  const bool staged = form != 2 && hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
+  const bool gather = form == 2 || (form == 0 && n <= kMbAutoGatherCells);
+  const bool staged = !gather && hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
   const int n_tiles = n / kTileCells;
   const long long tile_work = (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells;
   const int Ga = staged ? wave_grid(mb_amul_stream_kernel<0>, kTileCells, tile_work)
