@@ -615,11 +615,17 @@ int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef64, const d
  * No reference counterpart.  Many independent systems solved together: the
  * layout is their block-diagonal concatenation (each system's cells padded
  * to a multiple of 32), cut into tiles -- contiguous cell ranges of one
- * system, one CTA each.  Systems keep their own scalars, residual checks
- * and convergence; finished systems' tiles return at once.  Same iteration
- * as gbf_mixed_pcg_solve (FP32 inner, FP64 reliable updates); with
- * use_graph a chunk of iterations is captured once in a CUDA graph and
- * replayed.  R has n_systems entries.  block_size: 128, 256 or 512.        */
+ * system.  Systems keep their own scalars, residual checks and convergence;
+ * finished systems' tiles return at once.  Same iteration as
+ * gbf_mixed_pcg_solve (FP32 inner, FP64 reliable updates).  form: 0 one
+ * kernel per phase (one CTA per tile) launched directly, 1 the same with a
+ * chunk of iterations captured once in a CUDA graph and replayed, 2 every
+ * iteration of every system in one cooperative launch (phases separated by
+ * a bounded grid barrier; at most 4096 systems), 3 that launch and its
+ * set-up captured in a CUDA graph.  All forms give the same bits for the
+ * same block_size and tiles; a barrier wait of forms 2 and 3 that runs out
+ * gives status GBF_DEVICE_TIMEOUT in every system.  R has n_systems
+ * entries.  block_size: 128, 256 or 512.                                   */
 typedef struct gbf_batch {
   int32_t n_systems;
   int32_t n_tiles;
@@ -636,7 +642,7 @@ int gbf_batched_mixed_pcg_solve(const gbf_layout* L, const gbf_batch* B, const d
                                 const double* diag64, const float* coef32,
                                 const double* precond_d, const double* b, double* x,
                                 double delta, const gbf_solve_params* P, int32_t block_size,
-                                int32_t use_graph, gbf_solve_result* R, void* workspace,
+                                int32_t form, gbf_solve_result* R, void* workspace,
                                 size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
