@@ -1005,9 +1005,11 @@ def run_batch64(args, rank, world, local):
         # the autotuner's best block and tile for this form (short fixed-iteration runs)
         cand = {k.split(":", 1)[1]: v for k, v in (timings or {}).items()
                 if k.startswith(form + ":")}
-        blk, tl = (int(v) for v in min(cand, key=cand.get).split("x")) if cand else (256, 4096)
+        blk, tl, tpc = ((int(v) for v in min(cand, key=cand.get).split("x")) if cand
+                        else (256, 4096, 1))
         bs = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=20000, form=form,
-                              block_size=blk, tile_cells=tl, wavefront=tuned["wavefront"])
+                              block_size=blk, tile_cells=tl, wavefront=tuned["wavefront"],
+                              threads_per_cell=tpc)
         bs.solve(mats, rhs)  # per-form tuning of block and tile (cached), warm-up
         for _ in range(max(args.warmup - 1, 0)):
             bs.solve(mats, rhs)
@@ -1028,8 +1030,8 @@ def run_batch64(args, rank, world, local):
     res = forms[head]["results"]
     same_bits = all(bool(torch.equal(a[0], b[0])) for a, b in
                     zip(forms["graph"]["out"], forms["persistent"]["out"])) \
-        if forms["graph"]["config"]["block"] == forms["persistent"]["config"]["block"] and \
-        forms["graph"]["config"]["tile"] == forms["persistent"]["config"]["tile"] else None
+        if all(forms["graph"]["config"][k] == forms["persistent"]["config"][k]
+               for k in ("block", "tile", "tpc")) else None
 
     # every system against the FP64 GPU solver: same tolerance, and 1e-12
     errs, errs_tight, worst_true = [], [], 0.0
@@ -1049,7 +1051,8 @@ def run_batch64(args, rank, world, local):
     rb = BatchedPCGSolver(tolerance=0.0, rel_tol=0.0, max_iter=64, form="plain",
                           block_size=forms["graph"]["config"]["block"],
                           tile_cells=forms["graph"]["config"]["tile"],
-                          wavefront=tuned["wavefront"])
+                          wavefront=tuned["wavefront"],
+                          threads_per_cell=forms["graph"]["config"]["tpc"])
     rb.solve(mats, rhs)
     _lib.check(L.gbf_timing_enable(1, 100000))
     rb.solve(mats, rhs)

@@ -622,10 +622,13 @@ int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef64, const d
  * chunk of iterations captured once in a CUDA graph and replayed, 2 every
  * iteration of every system in one cooperative launch (phases separated by
  * a bounded grid barrier; at most 4096 systems), 3 that launch and its
- * set-up captured in a CUDA graph.  All forms give the same bits for the
- * same block_size and tiles; a barrier wait of forms 2 and 3 that runs out
- * gives status GBF_DEVICE_TIMEOUT in every system.  R has n_systems
- * entries.  block_size: 128, 256 or 512.                                   */
+ * set-up captured in a CUDA graph; + 4: the FP32 Amul runs two threads per
+ * cell (one sums the owner-side slots, the other the neighbour-side ones;
+ * same Amul bits, the p.Ap partial sums run over other threads).  All forms
+ * give the same bits for the same block_size, tiles and threads per cell; a
+ * barrier wait of forms 2 and 3 that runs out gives status
+ * GBF_DEVICE_TIMEOUT in every system.  R has n_systems entries.
+ * block_size: 128, 256 or 512.                                             */
 typedef struct gbf_batch {
   int32_t n_systems;
   int32_t n_tiles;

@@ -248,6 +248,52 @@ inline int layout_kind(const gbf_layout& L) {
     }                                               \
   } while (0)
 
+// One side of (A x)[c]: the owner-side sum (side 0) or the neighbour-side
+// sum (side 1), each from 0.0 in ascending face order with the products and
+// additions of cell_amul / cell_amul_fixed -- the two halves that a pair of
+// threads computes when a cell has two threads.  The caller forms
+// (diag * x + owner sum) + neighbour sum, the order of the one-thread forms.
+template <int KIND, typename T, typename A, bool COH = false>
+__device__ __forceinline__ A cell_side_sum(const gbf_layout& L, const T* __restrict__ coef,
+                                           const T* __restrict__ x, int c, int side) {
+  if constexpr (KIND == kLayoutHex33) {
+    const int s = c >> 5, lane = c & 31;
+    const int base = 32 * 6 * s + 32 * 3 * side + lane;
+    const int2* __restrict__ dm = reinterpret_cast<const int2*>(L.slot_dm) + 6 * s + 3 * side;
+    int d[3];
+    bool on[3];
+    T a[3], xv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int2 e = __ldg(dm + k);
+      d[k] = e.x;
+      on[k] = ((unsigned)e.y >> lane) & 1u;
+    }
+    if constexpr (sizeof(T) == 4) {
+      const unsigned long long ef = l2_evict_first();
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a[k] = ld_nc_hint(coef + base + 32 * k, ef);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a[k] = __ldg(coef + base + 32 * k);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) xv[k] = on[k] ? ldx<COH>(x + c + d[k]) : (T)0;
+    A sum = (A)0;
+    if (on[0]) sum = first_term((A)mul_rn(a[0], xv[0]));
+#pragma unroll
+    for (int k = 1; k < 3; ++k)
+      if (on[k]) sum = add_rn(sum, (A)mul_rn(a[k], xv[k]));
+    return sum;
+  } else {
+    if (L.n_faces == 0) return (A)0;
+    const CellSlots cs = cell_slots(L, c);
+    return side == 0 ? slot_sum<T, A, COH>(L, coef, x, c, cs.base, cs.e0, cs.wo)
+                     : slot_sum<T, A, COH>(L, coef, x, c, cs.base + 32 * cs.wo, cs.e0 + cs.wo,
+                                           cs.wn);
+  }
+}
+
 // True when a symmetric matrix on this layout may be stored as its
 // owner-side half (hex 3+3 kind with a mirror table).
 inline bool layout_sym_ok(const gbf_layout& L) {

@@ -181,19 +181,45 @@ __global__ void __launch_bounds__(BS)
 
 // ---- one tile of each phase of the iteration --------------------------------
 // Ap = A p (FP32), p.Ap; the system's last tile forms alpha (or breakdown).
-template <int BS, int KIND, bool COH>
+// TPC threads per cell: 1, or 2 -- the even thread of a pair sums the
+// owner-side slots, the odd one the neighbour-side slots, and the even one
+// forms (diag * p + owner sum) + neighbour sum, the one-thread order.  A tile
+// is a multiple of 32 cells long and a warp covers 16 consecutive cells per
+// step, so every lane of a warp runs the same number of steps (the pair
+// shuffle takes the full mask).
+template <int BS, int KIND, bool COH, int TPC>
 __device__ __forceinline__ void bmp_ap_tile(const gbf_layout& L, const BTiles& T, int tile,
                                             const float* __restrict__ coef32, const BVecs& v,
                                             double* sh) {
+  static_assert(TPC == 1 || TPC == 2, "one or two threads per cell");
   const int s = __ldg(T.tile_sys + tile);
   BState* st = v.st + s;
   if (tile_status<COH>(st) != GBF_RUNNING) return;
   BDFAcc a;
-  for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < __ldg(T.tile_end + tile); c += BS) {
-    const float pc = COH ? __ldcg(v.p + c) : __ldg(v.p + c);
-    const float y = cell_amul_k<KIND, float, float, false, COH>(L, coef32, v.d32, v.p, c, pc);
-    v.Ap[c] = y;
-    a.add_prod(pc, y);
+  const int c_end = __ldg(T.tile_end + tile);
+  if constexpr (TPC == 1) {
+    for (int c = __ldg(T.tile_begin + tile) + threadIdx.x; c < c_end; c += BS) {
+      const float pc = COH ? __ldcg(v.p + c) : __ldg(v.p + c);
+      const float y = cell_amul_k<KIND, float, float, false, COH>(L, coef32, v.d32, v.p, c, pc);
+      v.Ap[c] = y;
+      a.add_prod(pc, y);
+    }
+  } else {
+    const int side = threadIdx.x & 1;
+    for (int c = __ldg(T.tile_begin + tile) + (threadIdx.x >> 1); c < c_end; c += BS / 2) {
+      const float part = cell_side_sum<KIND, float, float, COH>(L, coef32, v.p, c, side);
+      const float sn = __shfl_down_sync(0xffffffffu, part, 1);
+      if (side == 0) {
+        const float pc = COH ? __ldcg(v.p + c) : __ldg(v.p + c);
+        float y = mul_rn(__ldg(v.d32 + c), pc);
+        if (L.n_faces > 0) {
+          y = add_rn(y, part);
+          y = add_rn(y, sn);
+        }
+        v.Ap[c] = y;
+        a.add_prod(pc, y);
+      }
+    }
   }
   const double acc = block_sum_df(a, sh);
   if (threadIdx.x == 0) v.partials[tile] = acc;
@@ -381,11 +407,11 @@ __device__ __forceinline__ void bmp_fold_tile(const BTiles& T, int tile, double*
 }
 
 // ---- the per-phase kernels: one tile per CTA --------------------------------
-template <int BS, int KIND>
+template <int BS, int KIND, int TPC>
 __global__ void __launch_bounds__(BS)
     bmp_ap_kernel(gbf_layout L, BTiles T, const float* __restrict__ coef32, BVecs v) {
   __shared__ double sh[BS / 32];
-  bmp_ap_tile<BS, KIND, false>(L, T, blockIdx.x, coef32, v, sh);
+  bmp_ap_tile<BS, KIND, false, TPC>(L, T, blockIdx.x, coef32, v, sh);
 }
 
 template <int BS>
@@ -493,7 +519,7 @@ __device__ __forceinline__ int active_tile(const BTiles& T, const int* pref, int
   return __ldg(T.sys_tile0 + lo) + (t - pref[lo]);
 }
 
-template <int BS, int KIND>
+template <int BS, int KIND, int TPC>
 __global__ void __launch_bounds__(BS)
     bmp_persistent_kernel(gbf_layout L, BTiles T, const double* __restrict__ coef64,
                           const double* __restrict__ diag64, const float* __restrict__ coef32,
@@ -510,7 +536,7 @@ __global__ void __launch_bounds__(BS)
   const long long cap = (long long)P.max_iter + 4;
   for (long long it = 0; nact > 0 && it < cap; ++it) {
     for (int t = blockIdx.x; t < nact; t += G)
-      bmp_ap_tile<BS, KIND, true>(L, T, active_tile(T, pref, t), coef32, v, sh);
+      bmp_ap_tile<BS, KIND, true, TPC>(L, T, active_tile(T, pref, t), coef32, v, sh);
     if (!grid_barrier(bar, G)) return;
     for (int t = blockIdx.x; t < nact; t += G)
       bmp_update_tile<BS, true>(T, active_tile(T, pref, t), x, v, delta, P, sh);
@@ -543,13 +569,13 @@ __global__ void bmp_ctl_init_kernel(BCtl* ctl, int n_systems) {
   ctl->bar.pad = 0;
 }
 
-template <int BS>
+template <int BS, int TPC>
 static int launch_iteration(cudaStream_t s, int nt, const gbf_layout& L, const BTiles& T,
                             const double* coef64, const double* diag64, const float* coef32,
                             const double* b, double* x, const BVecs& v, double delta,
                             const gbf_solve_params& P, bool probe) {
   const bool tb = probe && timing_begin(kProbeBatchedAp, s);
-  GBF_LAYOUT_DISPATCH(L, K, bmp_ap_kernel<BS, K><<<nt, BS, 0, s>>>(L, T, coef32, v));
+  GBF_LAYOUT_DISPATCH(L, K, bmp_ap_kernel<BS, K, TPC><<<nt, BS, 0, s>>>(L, T, coef32, v));
   if (tb) timing_end(kProbeBatchedAp, s);
   bmp_update_kernel<BS><<<nt, BS, 0, s>>>(T, x, v, delta, P);
   bmp_true_kernel<BS><<<nt, BS, 0, s>>>(L, T, coef64, diag64, b, x, v, P);
@@ -559,7 +585,7 @@ static int launch_iteration(cudaStream_t s, int nt, const gbf_layout& L, const B
 
 // Resident CTAs of the persistent kernel (occupancy x SMs, at most one per
 // tile); 0 when it cannot be launched cooperatively.
-template <int BS, int KIND>
+template <int BS, int KIND, int TPC>
 static int persistent_grid(int n_systems, int n_tiles) {
   int dev = 0, sms = 0, coop = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -567,8 +593,8 @@ static int persistent_grid(int n_systems, int n_tiles) {
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
     return 0;
   const size_t shm = sizeof(int) * (size_t)(n_systems + 1);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bmp_persistent_kernel<BS, KIND>, BS,
-                                                    shm) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bmp_persistent_kernel<BS, KIND, TPC>,
+                                                    BS, shm) != cudaSuccess ||
       per_sm <= 0)
     return 0;
   long long g = (long long)per_sm * sms;
@@ -576,7 +602,7 @@ static int persistent_grid(int n_systems, int n_tiles) {
   return g < 1 ? 1 : (int)g;
 }
 
-template <int BS, int KIND>
+template <int BS, int KIND, int TPC>
 static cudaError_t launch_persistent(int grid, cudaStream_t s, const gbf_layout& L,
                                      const BTiles& T, const double* coef64, const double* diag64,
                                      const float* coef32, const double* b, double* x,
@@ -591,8 +617,8 @@ static cudaError_t launch_persistent(int grid, cudaStream_t s, const gbf_layout&
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, bmp_persistent_kernel<BS, KIND>, L, T, coef64, diag64, coef32,
-                            b, x, v, delta, P);
+  return cudaLaunchKernelEx(&cfg, bmp_persistent_kernel<BS, KIND, TPC>, L, T, coef64, diag64,
+                            coef32, b, x, v, delta, P);
 }
 
 // Per-system results from the state blocks.
@@ -623,7 +649,7 @@ static int read_results(const BVecs& v, int S, int launches, gbf_solve_result* R
 // The persistent form: control words, the init kernel and one cooperative
 // launch for every iteration of every system (optionally captured together
 // in a CUDA graph and replayed once).
-template <int BS, int KIND>
+template <int BS, int KIND, int TPC>
 static int batched_solve_persistent(const gbf_layout* L, const BTiles& T, const double* coef64,
                                     const double* diag64, const float* coef32, const double* pd,
                                     const double* b, double* x, double delta,
@@ -633,7 +659,7 @@ static int batched_solve_persistent(const gbf_layout* L, const BTiles& T, const 
   GBF_REQUIRE(S <= kPersistentMaxSystems,
               "batched_pcg: the persistent form takes at most %d systems (got %d)",
               kPersistentMaxSystems, S);
-  const int G = persistent_grid<BS, KIND>(S, nt);
+  const int G = persistent_grid<BS, KIND, TPC>(S, nt);
   GBF_REQUIRE(G > 0, "batched_pcg: the device cannot run the persistent form");
   auto enqueue = [&](cudaStream_t q) -> cudaError_t {
     cudaError_t e = cudaMemsetAsync(v.st, 0, sizeof(BState) * (size_t)S, q);
@@ -642,7 +668,8 @@ static int batched_solve_persistent(const gbf_layout* L, const BTiles& T, const 
     bmp_init_kernel<BS><<<nt, BS, 0, q>>>(*L, T, coef64, diag64, pd, b, x, v, *P);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_persistent<BS, KIND>(G, q, *L, T, coef64, diag64, coef32, b, x, v, delta, *P);
+    return launch_persistent<BS, KIND, TPC>(G, q, *L, T, coef64, diag64, coef32, b, x, v, delta,
+                                            *P);
   };
   if (graph_capture) {
     cudaStream_t cap = nullptr;
@@ -680,7 +707,7 @@ static int batched_solve_persistent(const gbf_layout* L, const BTiles& T, const 
   return GBF_OK;
 }
 
-template <int BS>
+template <int BS, int TPC>
 static int batched_solve(const gbf_layout* L, const BTiles& T, const double* coef64,
                          const double* diag64, const float* coef32, const double* pd,
                          const double* b, double* x, double delta, const gbf_solve_params* P,
@@ -688,10 +715,10 @@ static int batched_solve(const gbf_layout* L, const BTiles& T, const double* coe
   const bool use_graph = (form & 1) != 0;
   if (form & 2) {
     if (layout_kind(*L) == kLayoutHex33)
-      return batched_solve_persistent<BS, kLayoutHex33>(L, T, coef64, diag64, coef32, pd, b, x,
-                                                        delta, P, use_graph, R, v, s);
-    return batched_solve_persistent<BS, kLayoutGeneric>(L, T, coef64, diag64, coef32, pd, b, x,
-                                                        delta, P, use_graph, R, v, s);
+      return batched_solve_persistent<BS, kLayoutHex33, TPC>(L, T, coef64, diag64, coef32, pd, b,
+                                                             x, delta, P, use_graph, R, v, s);
+    return batched_solve_persistent<BS, kLayoutGeneric, TPC>(L, T, coef64, diag64, coef32, pd, b,
+                                                             x, delta, P, use_graph, R, v, s);
   }
   const int nt = T.n_tiles;
   const int S = T.n_systems;
@@ -714,8 +741,8 @@ static int batched_solve(const gbf_layout* L, const BTiles& T, const double* coe
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     int rc = GBF_OK;
     for (int j = 0; j < chunk && e == cudaSuccess && rc == GBF_OK; ++j)
-      rc = launch_iteration<BS>(cap, nt, *L, T, coef64, diag64, coef32, b, x, v, delta, *P,
-                                false);
+      rc = launch_iteration<BS, TPC>(cap, nt, *L, T, coef64, diag64, coef32, b, x, v, delta, *P,
+                                     false);
     cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess && rc == GBF_OK) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -737,8 +764,8 @@ static int batched_solve(const gbf_layout* L, const BTiles& T, const double* coe
       }
     } else {
       for (int j = 0; j < chunk; ++j) {
-        rc = launch_iteration<BS>(s, nt, *L, T, coef64, diag64, coef32, b, x, v, delta, *P,
-                                  true);
+        rc = launch_iteration<BS, TPC>(s, nt, *L, T, coef64, diag64, coef32, b, x, v, delta, *P,
+                                       true);
         if (rc) break;
       }
       if (rc) {
@@ -795,7 +822,9 @@ extern "C" int gbf_batched_mixed_pcg_solve(const gbf_layout* L, const gbf_batch*
   GBF_REQUIRE(P->max_iter >= 0, "batched_pcg: negative max_iter");
   GBF_REQUIRE(block_size == 128 || block_size == 256 || block_size == 512,
               "batched_pcg: block_size must be 128, 256 or 512 (got %d)", block_size);
-  GBF_REQUIRE(form >= 0 && form <= 3, "batched_pcg: form must be 0..3 (got %d)", form);
+  GBF_REQUIRE(form >= 0 && form <= 7,
+              "batched_pcg: form must be 0..7 (bits 0-1 the launch form, bit 2 two threads "
+              "per cell; got %d)", form);
   const int n = L->n_cells;
   GBF_REQUIRE(diag64 && b && x && ws && (L->n_faces == 0 || (coef64 && coef32)),
               "batched_pcg: NULL pointer");
@@ -815,12 +844,20 @@ extern "C" int gbf_batched_mixed_pcg_solve(const gbf_layout* L, const gbf_batch*
   v.running = &v.ctl->running;
   BTiles T{B->n_systems, B->n_tiles, B->tile_sys, B->tile_begin, B->tile_end, B->sys_tile0};
   cudaStream_t s = as_stream(stream);
+  const int f = form & 3;
+  const bool pair = (form & 4) != 0;
+#define GBF_BATCHED_CASE(BSZ)                                                                  \
+  return pair ? batched_solve<BSZ, 2>(L, T, coef64, diag64, coef32, pd, b, x, delta, P, f, R, \
+                                      v, s)                                                    \
+              : batched_solve<BSZ, 1>(L, T, coef64, diag64, coef32, pd, b, x, delta, P, f, R, \
+                                      v, s)
   switch (block_size) {
     case 128:
-      return batched_solve<128>(L, T, coef64, diag64, coef32, pd, b, x, delta, P, form, R, v, s);
+      GBF_BATCHED_CASE(128);
     case 512:
-      return batched_solve<512>(L, T, coef64, diag64, coef32, pd, b, x, delta, P, form, R, v, s);
+      GBF_BATCHED_CASE(512);
     default:
-      return batched_solve<256>(L, T, coef64, diag64, coef32, pd, b, x, delta, P, form, R, v, s);
+      GBF_BATCHED_CASE(256);
   }
+#undef GBF_BATCHED_CASE
 }

@@ -36,6 +36,7 @@ BLOCK_SIZES = (128, 256, 512)
 TILE_CELLS = (1024, 2048, 4096, 8192)
 FORMS = {"plain": 0, "graph": 1, "persistent": 2, "persistent_graph": 3}
 TUNED_FORMS = ("graph", "persistent")
+THREADS_PER_CELL = (1, 2)
 
 
 def autotune_cache_path() -> str:
@@ -132,7 +133,8 @@ class BatchedPCGSolver:
                  min_iter: int = 0, preconditioner: str = "DIC", *, delta: float = 0.1,
                  block_size: int | None = None, tile_cells: int | None = None,
                  use_graph: bool = True, autotune: bool = True, check_every: int = 16,
-                 form: str | None = None, wavefront: str | None = None) -> None:
+                 form: str | None = None, wavefront: str | None = None,
+                 threads_per_cell: int | None = None) -> None:
         self.tolerance, self.rel_tol = float(tolerance), float(rel_tol)
         self.max_iter, self.min_iter = int(max_iter), int(min_iter)
         self.precond = preconditioner.upper()
@@ -143,6 +145,9 @@ class BatchedPCGSolver:
             raise ValueError(f"form must be one of {sorted(FORMS)}, got {form!r}")
         if wavefront not in (None, "cooperative", "per_level"):
             raise ValueError("wavefront must be 'cooperative', 'per_level' or None")
+        if threads_per_cell not in (None, 1, 2):
+            raise ValueError("threads_per_cell must be 1, 2 or None")
+        self.threads_per_cell = threads_per_cell
         self.delta = float(delta)
         self.block_size, self.tile_cells = block_size, tile_cells
         self.form = form if form is not None else (None if use_graph else "plain")
@@ -209,7 +214,7 @@ class BatchedPCGSolver:
         return d
 
     def _run(self, bl: BatchLayout, b: torch.Tensor, x: torch.Tensor, block: int, tile: int,
-             max_iter: int, tol: float, rel: float, form: str, wavefront: str):
+             max_iter: int, tol: float, rel: float, form: str, wavefront: str, tpc: int = 1):
         m = bl.matrix
         topo = m.topology()
         pre = self._factor(bl, wavefront)
@@ -226,7 +231,8 @@ class BatchedPCGSolver:
         _lib.check(L.gbf_batched_mixed_pcg_solve(
             topo.layout_ref, ctypes.byref(T.struct), coef64.data_ptr(), m.diag.data_ptr(),
             coef32.data_ptr(), None if pre is None else pre.data_ptr(), b.data_ptr(),
-            x.data_ptr(), self.delta, ctypes.byref(P), int(block), FORMS[form], R,
+            x.data_ptr(), self.delta, ctypes.byref(P), int(block),
+            FORMS[form] | (4 if tpc == 2 else 0), R,
             ws.data_ptr(), ws.numel(), _lib.stream_ptr(bl.device)), "gbf_batched_mixed_pcg_solve")
         return list(R)
 
@@ -242,7 +248,7 @@ class BatchedPCGSolver:
 
     def _tune(self, bl: BatchLayout, b: torch.Tensor) -> dict:
         fixed = {"block": self.block_size, "tile": self.tile_cells, "form": self.form,
-                 "wavefront": self.wavefront}
+                 "wavefront": self.wavefront, "tpc": self.threads_per_cell}
         if all(v is not None for v in fixed.values()):
             return fixed
         name = torch.cuda.get_device_name(bl.device)
@@ -259,7 +265,8 @@ class BatchedPCGSolver:
             return {k: (fixed[k] if fixed[k] is not None else hit[k]) for k in fixed}
         if not self.autotune:
             return {"block": self.block_size or 256, "tile": self.tile_cells or 4096,
-                    "form": self.form or "graph", "wavefront": self.wavefront or "cooperative"}
+                    "form": self.form or "graph", "wavefront": self.wavefront or "cooperative",
+                    "tpc": self.threads_per_cell or 1}
         timings: dict = {}
         # wavefront of the factorisation: both ways once (same bits)
         if self.precond == "NONE":
@@ -273,31 +280,34 @@ class BatchedPCGSolver:
         forms = [self.form] if self.form else list(TUNED_FORMS)
         blocks = [self.block_size] if self.block_size else list(BLOCK_SIZES)
         tiles = [self.tile_cells] if self.tile_cells else list(TILE_CELLS)
+        tpcs = [self.threads_per_cell] if self.threads_per_cell else list(THREADS_PER_CELL)
         x = torch.zeros_like(b)
         best_per_form = {}
         for fm in forms:
             best = None
-            for blk in blocks:
-                for tl in tiles:
-                    t = self._timed(lambda: (x.zero_(), self._run(bl, b, x, blk, tl, 24, 0.0,
-                                                                  0.0, fm, wf)))
-                    timings[f"{fm}:{blk}x{tl}"] = t
-                    if best is None or t < best[0]:
-                        best = (t, blk, tl)
+            for tpc in tpcs:
+                for blk in blocks:
+                    for tl in tiles:
+                        t = self._timed(lambda: (x.zero_(), self._run(bl, b, x, blk, tl, 24, 0.0,
+                                                                      0.0, fm, wf, tpc)))
+                        timings[f"{fm}:{blk}x{tl}x{tpc}"] = t
+                        if best is None or t < best[0]:
+                            best = (t, blk, tl, tpc)
             best_per_form[fm] = best
         # the forms differ most once systems finish unevenly: one full solve each
         choice = None
-        for fm, (_, blk, tl) in best_per_form.items():
+        for fm, (_, blk, tl, tpc) in best_per_form.items():
             if len(best_per_form) > 1:
                 t = self._timed(lambda: (x.zero_(), self._run(bl, b, x, blk, tl, self.max_iter,
                                                               self.tolerance, self.rel_tol, fm,
-                                                              wf)), reps=1)
+                                                              wf, tpc)), reps=1)
                 timings[f"full_solve:{fm}"] = t
             else:
                 t = 0.0
             if choice is None or t < choice[0]:
-                choice = (t, fm, blk, tl)
-        cfg = {"block": choice[2], "tile": choice[3], "form": choice[1], "wavefront": wf}
+                choice = (t, fm, blk, tl, tpc)
+        cfg = {"block": choice[2], "tile": choice[3], "form": choice[1], "wavefront": wf,
+               "tpc": choice[4]}
         cache[key] = dict(cfg, timings=timings)
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)
@@ -326,7 +336,7 @@ class BatchedPCGSolver:
         tol = self.tolerance if tolerance is None else float(tolerance)
         mi = self.max_iter if max_iter is None else int(max_iter)
         res = self._run(bl, b, x, cfg["block"], cfg["tile"], mi, tol, self.rel_tol, cfg["form"],
-                        cfg["wavefront"])
+                        cfg["wavefront"], cfg["tpc"])
         self.last_results = res
         self.last_infos = []
         out = []

@@ -44,8 +44,9 @@ def test_batched_systems_converge_independently(tmp_path, monkeypatch):
     assert len(set(its)) > 1  # uneven systems stop at different iterations
 
 
+@pytest.mark.parametrize("tpc", [1, 2])
 @pytest.mark.parametrize("block,tile", [(256, 1024), (128, 2048), (512, 4096)])
-def test_batched_forms_give_identical_bits(block, tile):
+def test_batched_forms_give_identical_bits(block, tile, tpc):
     """Graph replay, plain launches, the persistent cooperative launch and the
     persistent launch captured in a graph: the same per-element arithmetic
     and the same per-tile reductions in tile order, so x, the iteration and
@@ -55,7 +56,8 @@ def test_batched_forms_give_identical_bits(block, tile):
     ref = None
     for form in ("graph", "plain", "persistent", "persistent_graph"):
         s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=block,
-                             tile_cells=tile, form=form, wavefront="cooperative")
+                             tile_cells=tile, form=form, wavefront="cooperative",
+                             threads_per_cell=tpc)
         xs = [x.cpu().numpy() for x, _, _ in s.solve(mats, rhs)]
         got = (xs, [(r.iterations, r.outer_updates, r.status, r.final_residual)
                     for r in s.last_results])
@@ -67,6 +69,32 @@ def test_batched_forms_give_identical_bits(block, tile):
         for u, v in zip(got[0], ref[0]):
             np.testing.assert_array_equal(u, v)
         assert got[1] == ref[1], form
+
+
+def test_batched_two_threads_per_cell():
+    """Two threads per cell split a cell's Amul by side and give its bits;
+    the p.Ap partial sums run over other threads, so the solve agrees with
+    one thread per cell to rounding -- both reach the tolerance on their
+    true residuals, same iteration counts within one or two."""
+    mats, rhs, _ = poisson_batch(4, lo=8, hi=20, seed=8)
+    out = {}
+    for tpc in (1, 2):
+        s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=256,
+                             tile_cells=1024, form="graph", wavefront="cooperative",
+                             threads_per_cell=tpc)
+        xs = s.solve(mats, rhs)
+        assert all(i.converged for i in s.last_infos)
+        out[tpc] = (xs, [r.iterations for r in s.last_results])
+    for (x1, _, _), (x2, _, _), m, b in zip(out[1][0], out[2][0], mats, rhs):
+        own, nei, d, lo, up = _np(m)
+        bb = b.cpu().numpy()
+        for x in (x1, x2):
+            r = bb - O.amul(own, nei, d, lo, up, x.cpu().numpy())
+            assert np.linalg.norm(r) / np.linalg.norm(bb) < 1e-8
+        assert float(torch.linalg.vector_norm(x1 - x2) / torch.linalg.vector_norm(x1)) < 1e-6
+    assert all(abs(a - b) <= 2 for a, b in zip(out[1][1], out[2][1]))
+    with pytest.raises(ValueError, match="threads_per_cell"):
+        BatchedPCGSolver(threads_per_cell=3)
 
 
 def test_batched_factor_wavefront_forms_match():
@@ -104,6 +132,9 @@ def test_batched_autotuner_considers_both_forms(tmp_path, monkeypatch):
     s.solve(mats, rhs)
     t = s.last_config["timings"]
     assert any(k.startswith("graph:") for k in t) and any(k.startswith("persistent:") for k in t)
+    assert any(k.endswith("x1") for k in t if ":" in k and not k.startswith("full"))
+    assert any(k.endswith("x2") for k in t if ":" in k and not k.startswith("full"))
+    assert s.last_config["tpc"] in (1, 2)
     assert "full_solve:graph" in t and "full_solve:persistent" in t
     assert "factor_cooperative" in t and "factor_per_level" in t
     assert s.last_config["form"] in ("graph", "persistent")
