@@ -90,7 +90,7 @@ def parse():
                         "systems, batched; adjoint96: adjoint gradient of 20 implicit steps at 96^3; "
                         "next: geometry, correctors, GAMG and smoothers")
     p.add_argument("--convdiff-legs", default="standard,reference,mixed,mixed_kernels,mixed_gather,"
-                                              "standard_1e-10,mixed_1e-10",
+                                              "mixed_fused,standard_1e-10,mixed_1e-10",
                    help="convdiff128: comma-separated solver legs to run")
     p.add_argument("--fd-faces", type=int, default=32, help="adjoint96: faces checked by central "
                                                             "differences")
@@ -890,6 +890,8 @@ def run_convdiff128(args, rank, world, local):
                                                        max_iter=4000, form="kernels"),
         "mixed_gather": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000,
                                                       form="gather"),
+        "mixed_fused": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-8, max_iter=4000,
+                                                     form="fused"),
         "standard_1e-10": PBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10, max_iter=4000,
                                           omega="standard"),
         "mixed_1e-10": MixedPrecisionPBiCGSTABSolver(tolerance=0.0, rel_tol=1e-10,
@@ -919,7 +921,8 @@ def run_convdiff128(args, rank, world, local):
         else:
             res[key].update(checks=it, iterations=(it - 1) / 2, iterations_per_s=(it - 1) / 2 / t)
     for key, ref in (("mixed", "standard"), ("mixed_kernels", "standard"),
-                     ("mixed_gather", "standard"), ("mixed_1e-10", "standard_1e-10")):
+                     ("mixed_gather", "standard"), ("mixed_fused", "standard"),
+                     ("mixed_1e-10", "standard_1e-10")):
         if key not in res or ref not in res:
             continue
         res[key]["speedup_vs_fp64"] = res[ref]["s"] / res[key]["s"]
@@ -958,7 +961,8 @@ def run_convdiff128(args, rank, world, local):
     if rank == 0:
         names = {"standard": "omega_standard", "reference": "omega_reference",
                  "mixed": "mixed_fp32_fp64", "mixed_kernels": "mixed_six_kernels_staged",
-                 "mixed_gather": "mixed_six_kernels_gather", "standard_1e-10": "fp64_to_1e-10",
+                 "mixed_gather": "mixed_six_kernels_gather",
+                 "mixed_fused": "mixed_three_kernels_fused", "standard_1e-10": "fp64_to_1e-10",
                  "mixed_1e-10": "mixed_to_1e-10"}
         extra = {names[k]: v for k, v in res.items()}
         extra["setup_s"] = t_setup

@@ -593,14 +593,18 @@ int gbf_mixed_pcg_solve(const gbf_layout* L, const double* coef64, const double*
  * gbf_mixed_pcg_solve (residual replacement keeping p, r~ and rho).
  * Convergence on true residuals only (the FP64 solver's half-step check on
  * s is not taken).  P->variant bit 0: 0 omega = (t.z)/(t.t) as the
- * reference, 1 the standard (t.s)/(t.t); bits 1-2, the form: 0 automatic
- * (the persistent form up to 2^16 cells, the kernels with the plain gather
- * up to 2^22, the staged kernels above), 1 six kernels
+ * reference, 1 the standard (t.s)/(t.t); bits 1-3, the form: 0 automatic
+ * (the persistent form up to 2^16 cells, the fused form up to 2^19, the
+ * kernels with the plain gather up to 2^22, the staged kernels above), 1 six
+ * kernels
  * per iteration (bulk-copy staged Amul on aligned hex layouts), 2 the same
  * with the plain L2 gather Amul, 3 the whole inner loop in one cooperative
  * launch (phases separated by a bounded grid barrier; its dot products sum
  * over its own grid, so it agrees with the kernels to rounding; a barrier
- * wait that runs out gives status GBF_DEVICE_TIMEOUT).  coef32 = FP32
+ * wait that runs out gives status GBF_DEVICE_TIMEOUT), 4 three kernels per
+ * iteration, one per reduction (the p update folded into the next v = A y,
+ * the s / z update into t = A z, the multiplied vector formed at neighbour
+ * cells; hex 3+3 layouts, others run form 2).  coef32 = FP32
  * packing of the FP64 matrix; precond_d = FP64 DILU/DIC diagonal or NULL.
  * history / R as for gbf_mixed_pcg_solve.  Replaces PBiCGSTABSolver._solve
  * (solvers/pbicgstab.py:103) for the momentum solve.                        */

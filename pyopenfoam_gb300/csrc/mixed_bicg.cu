@@ -46,6 +46,7 @@ struct MbState {
 
 struct MbVecs {
   float *r, *rt, *p, *v, *y, *s, *z, *t, *xlo, *rD, *d32;
+  float *p2, *v2;  // the fused form's second p and v buffers (iteration parity)
   double* partials;
   MbState* st;
 };
@@ -478,6 +479,127 @@ __global__ void __launch_bounds__(kBlock) mb_p_kernel(int n, MbVecs v) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// The fused form (hex 3+3 layouts): three kernels per iteration, one per
+// reduction, instead of five vector and Amul passes.  The p update of an
+// iteration moves into the next iteration's v = A y kernel, and the s / z
+// update into the t = A z kernel; the multiplied vector's values at
+// neighbour cells (y, z) are formed there from the stored vectors instead of
+// read -- with the same fmaf sequences as the per-phase kernels, so every
+// element has the bits it has there.  p and v are double-buffered by
+// iteration parity: the v = A y kernel reads the old p and v at neighbour
+// cells while it writes the new ones.
+// ---------------------------------------------------------------------------
+
+// (A w)[c] on a hex 3+3 layout for a vector w that is not stored: wq(q)
+// forms w at cell q.  The products and summation order of
+// cell_amul_fixed<float, float, false, 3, 3>.
+template <typename WQ>
+__device__ __forceinline__ float hex33_amul_formed(const gbf_layout& L,
+                                                   const float* __restrict__ coef,
+                                                   const float* __restrict__ diag, int c,
+                                                   float wc, WQ&& wq) {
+  constexpr int W = 6;
+  const int sl = c >> 5, lane = c & 31;
+  const int base = 32 * W * sl + lane;
+  const int4* __restrict__ dm4 = reinterpret_cast<const int4*>(L.slot_dm) + (W / 2) * sl;
+  int d[W];
+  unsigned m[W];
+#pragma unroll
+  for (int q = 0; q < W / 2; ++q) {
+    const int4 e = __ldg(dm4 + q);
+    d[2 * q] = e.x;
+    m[2 * q] = (unsigned)e.y;
+    d[2 * q + 1] = e.z;
+    m[2 * q + 1] = (unsigned)e.w;
+  }
+  float a[W], xv[W];
+  bool on[W];
+  const unsigned long long ef = l2_evict_first();
+#pragma unroll
+  for (int k = 0; k < W; ++k) a[k] = ld_nc_hint(coef + base + 32 * k, ef);
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    on[k] = (m[k] >> lane) & 1u;
+    xv[k] = on[k] ? wq(c + d[k]) : 0.0f;
+  }
+  float so = 0.0f, sn = 0.0f;
+  if (on[0]) so = first_term(mul_rn(a[0], xv[0]));
+#pragma unroll
+  for (int k = 1; k < 3; ++k)
+    if (on[k]) so = add_rn(so, mul_rn(a[k], xv[k]));
+  if (on[3]) sn = first_term(mul_rn(a[3], xv[3]));
+#pragma unroll
+  for (int k = 4; k < W; ++k)
+    if (on[k]) sn = add_rn(sn, mul_rn(a[k], xv[k]));
+  float y = mul_rn(__ldg(diag + c), wc);
+  y = add_rn(y, so);
+  return add_rn(y, sn);
+}
+
+// p = r + beta (p_old - omega v_old) (t.t branch: omega = 1), y = p / d_M,
+// v = A32 y, r~.v -> alpha.  In the first iteration beta = 0, so p = r.
+__global__ void __launch_bounds__(kBlock)
+    mb_pv_kernel(gbf_layout L, const float* __restrict__ coef32, MbVecs v, int parity) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ double sh[kBlock / 32];
+  const float beta = (float)v.st->beta;
+  const float omega = v.st->branch == 0 ? (float)v.st->omega : 1.0f;
+  const float* __restrict__ po = parity ? v.p2 : v.p;
+  const float* __restrict__ vo = parity ? v.v2 : v.v;
+  float* __restrict__ pn = parity ? v.p : v.p2;
+  float* __restrict__ vn = parity ? v.v : v.v2;
+  const float* __restrict__ r = v.r;
+  const float* __restrict__ rD = v.rD;
+  auto yq = [&](int q) {
+    return __ldg(rD + q) * fmaf(beta, fmaf(-omega, __ldg(vo + q), __ldg(po + q)), __ldg(r + q));
+  };
+  DFAcc a0, a1;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells;
+       c += gridDim.x * blockDim.x) {
+    const float pc = fmaf(beta, fmaf(-omega, __ldg(vo + c), __ldg(po + c)), __ldg(r + c));
+    const float yc = __ldg(rD + c) * pc;
+    pn[c] = pc;
+    v.y[c] = yc;
+    const float yv = hex33_amul_formed(L, coef32, v.d32, c, yc, yq);
+    vn[c] = yv;
+    a0.add_prod(__ldg(v.rt + c), yv);
+  }
+  mb_amul_finish<0>(v, a0, a1, sh);
+}
+
+// s = r - alpha v, z = s / d_M, x32 += alpha y, t = A32 z, t.t and t.s (or
+// t.z) -> omega or the t.t branch.
+__global__ void __launch_bounds__(kBlock)
+    mb_st_kernel(gbf_layout L, const float* __restrict__ coef32, MbVecs v, int parity,
+                 int standard_omega) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (v.st->status != GBF_RUNNING) return;
+  __shared__ double sh[kBlock / 32];
+  const float alpha = (float)v.st->alpha;
+  const float* __restrict__ vn = parity ? v.v : v.v2;  // this iteration's v
+  const float* __restrict__ r = v.r;
+  const float* __restrict__ rD = v.rD;
+  auto zq = [&](int q) { return __ldg(rD + q) * fmaf(-alpha, __ldg(vn + q), __ldg(r + q)); };
+  DFAcc a0, a1;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L.n_cells;
+       c += gridDim.x * blockDim.x) {
+    const float sc = fmaf(-alpha, __ldg(vn + c), __ldg(r + c));
+    const float zc = __ldg(rD + c) * sc;
+    v.s[c] = sc;
+    v.z[c] = zc;
+    v.xlo[c] = fmaf(alpha, v.y[c], v.xlo[c]);
+    const float tv = hex33_amul_formed(L, coef32, v.d32, c, zc, zq);
+    v.t[c] = tv;
+    a0.add_prod(tv, tv);
+    a1.add_prod(tv, standard_omega ? sc : zc);
+  }
+  mb_amul_finish<1>(v, a0, a1, sh);
+}
+
 // Folds the remaining FP32 correction into x at the end of the solve.
 __global__ void mb_fold_kernel(int n, double* __restrict__ x, MbVecs v) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
@@ -500,13 +622,16 @@ __global__ void mb_fold_kernel(int n, double* __restrict__ x, MbVecs v) {
 // is read from L2.  The dot products reduce over this launch's grid, so the
 // results agree with the per-phase form to rounding, not bit for bit.
 // ---------------------------------------------------------------------------
-// Automatic form choice, from a sweep of the three forms on GB300
-// (convection-diffusion systems, 16^3 .. 128^3, us per inner iteration): the
-// single launch wins while the per-kernel launch gaps dominate (22.6 against
-// 29.5 at 32^3), the plain L2 gather from 48^3 on (30.7 against 36.0
-// persistent and 35.3 staged at 48^3; 81.1 against 84.5 staged at 128^3), and
-// the staged stream where blocks have many tiles each.
+// Automatic form choice, from a sweep of the forms on GB300 (convection-
+// diffusion systems, 16^3 .. 128^3, us per inner iteration): the single
+// launch wins while the per-kernel launch gaps dominate (22.7 against 27.8
+// fused and 29.5 gather at 32^3), the fused three-kernel form in the middle
+// (34.8 against 38.7 gather at 64^3, level at 96^3), the plain L2 gather
+// above (81.0 against 92.1 fused and 84.4 staged at 128^3: there the fused
+// form's neighbour values, formed from four vectors, cost more than the
+// passes it saves), and the staged stream where blocks have many tiles.
 constexpr int kMbAutoPersistentCells = 1 << 16;
+constexpr int kMbAutoFusedCells = 1 << 19;
 constexpr int kMbAutoGatherCells = 1 << 22;
 
 struct MbRegs {
@@ -758,7 +883,7 @@ __global__ void __launch_bounds__(kBlock, 3)
 }
 
 static size_t mb_a256(size_t b) { return (b + 255) & ~(size_t)255; }
-constexpr int kMbVectors = 11;
+constexpr int kMbVectors = 13;
 
 }  // namespace gbf
 
@@ -824,17 +949,18 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
   char* w = static_cast<char*>(ws);
   const size_t vb = mb_a256(sizeof(float) * (size_t)n);
   MbVecs v;
-  float** vecs[kMbVectors] = {&v.r, &v.rt, &v.p, &v.v,   &v.y,  &v.s,
-                              &v.z, &v.t,  &v.xlo, &v.rD, &v.d32};
+  float** vecs[kMbVectors] = {&v.r, &v.rt, &v.p,  &v.v,   &v.y, &v.s, &v.z,
+                              &v.t, &v.xlo, &v.rD, &v.d32, &v.p2, &v.v2};
   for (int i = 0; i < kMbVectors; ++i) *vecs[i] = reinterpret_cast<float*>(w + i * vb);
   v.partials = reinterpret_cast<double*>(w + kMbVectors * vb);
   v.st = reinterpret_cast<MbState*>(w + kMbVectors * vb +
                                     mb_a256(sizeof(double) * 2 * kMaxGrid));
   GridBarrier* bar = reinterpret_cast<GridBarrier*>(
       w + kMbVectors * vb + mb_a256(sizeof(double) * 2 * kMaxGrid) + mb_a256(sizeof(MbState)));
-  GBF_REQUIRE(P->variant >= 0 && P->variant <= 7, "mixed_pbicgstab: variant must be 0..7");
+  GBF_REQUIRE(P->variant >= 0 && P->variant <= 9, "mixed_pbicgstab: variant must be 0..9");
   const int standard_omega = P->variant & 1;
-  const int form = P->variant >> 1;  // 0 auto, 1 kernels, 2 kernels + gather, 3 persistent
+  // 0 auto, 1 kernels (staged Amul), 2 kernels + gather, 3 persistent, 4 fused
+  const int form = P->variant >> 1;
 
   const int Gi = wave_grid(mb_init_kernel, kBlock, n);
   const bool hex = layout_kind(*L) == kLayoutHex33;
@@ -874,7 +1000,10 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
     }
   }
   // staged Amul: hex layout, 16-byte aligned coefficient / vector streams
-  const bool gather = form == 2 || (form == 0 && n <= kMbAutoGatherCells);
+  // the fused form needs the hex 3+3 gather; on other layouts it runs as the
+  // gather kernels
+  const bool fused = hex && (form == 4 || (form == 0 && n <= kMbAutoFusedCells));
+  const bool gather = form == 2 || form == 4 || (form == 0 && n <= kMbAutoGatherCells);
   const bool staged = !gather && hex && hex_stream_aligned(coef32, ws, ws, L->slot_dm);
   const int n_tiles = n / kTileCells;
   const long long tile_work = (long long)(n_tiles > 0 ? n_tiles : 1) * kTileCells;
@@ -901,11 +1030,26 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
   // a fold + true residual ends the solve (at most max_iter + 2 iterations)
   int launched = 0;
   const int limit = P->max_iter + 2;
+  const int Gpv = fused ? wave_grid(mb_pv_kernel, kBlock, n) : 0;
+  const int Gst = fused ? wave_grid(mb_st_kernel, kBlock, n) : 0;
   while (hs.status == GBF_RUNNING && launched < limit) {
     for (int j = 0; j < chunk && launched < limit; ++j, ++launched) {
       const gbf_layout Lv = *L;
       const bool tb = (launched % 8 == 0) && timing_begin(kProbeMixedBicgAmul, s);
       cudaError_t e;
+      if (fused) {
+        const int parity = launched & 1;
+        e = launch_pdl(mb_pv_kernel, Gpv, kBlock, s, Lv, coef32, v, parity);
+        if (tb) timing_end(kProbeMixedBicgAmul, s);
+        if (e == cudaSuccess)
+          e = launch_pdl(mb_st_kernel, Gst, kBlock, s, Lv, coef32, v, parity, standard_omega);
+        if (e == cudaSuccess) e = launch_pdl(mb_r_kernel, Gr, kBlock, s, n, x, v, delta, *P);
+        if (e == cudaSuccess)
+          e = launch_pdl(mb_true_kernel, Gt, kBlock, s, Lv, coef64, diag64, b,
+                         static_cast<const double*>(x), v, hist, hist_cap, *P);
+        GBF_CHECK_CUDA(e);
+        continue;
+      }
       if (staged)
         e = launch_pdl(mb_amul_stream_kernel<0>, Ga, Ba, s, Lv, coef32, v, n_tiles,
                        standard_omega);
@@ -946,6 +1090,6 @@ extern "C" int gbf_mixed_pbicgstab_solve(const gbf_layout* L, const double* coef
   R->initial_residual = hs.res0;
   R->inner_iterations = hs.inner;
   R->outer_updates = hs.updates;
-  R->launches = 2 + 6 * launched;
+  R->launches = 2 + (fused ? 4 : 6) * launched;
   return GBF_OK;
 }

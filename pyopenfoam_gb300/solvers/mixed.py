@@ -129,11 +129,15 @@ class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
     the reference's (t.z)/(t.t).  ``form`` (keyword only): ``"persistent"``
     runs the whole inner loop in one cooperative launch, ``"kernels"`` six
     launches per iteration (bulk-copy staged Amul on hex layouts),
-    ``"gather"`` the same with the plain L2 gather Amul; ``"auto"`` takes
-    the persistent form up to 2^16 cells, the gather kernels up to 2^22 and
-    the staged kernels above (the fastest of the three in a sweep on GB300)."""
+    ``"gather"`` the same with the plain L2 gather Amul, ``"fused"`` three
+    kernels per iteration (one per reduction: the p update folded into the
+    next v = A y, the s / z update into t = A z; hex 3+3 layouts, others run
+    the gather kernels); ``"auto"`` takes
+    the persistent form up to 2^16 cells, the fused form up to 2^19, the
+    gather kernels up to 2^22 and the staged kernels above (the fastest in a
+    sweep of the forms on GB300)."""
 
-    FORMS = {"auto": 0, "kernels": 1, "gather": 2, "persistent": 3}
+    FORMS = {"auto": 0, "kernels": 1, "gather": 2, "persistent": 3, "fused": 4}
 
     def __init__(self, tolerance: float = 1e-6, rel_tol: float = 0.01, max_iter: int = 1000,
                  min_iter: int = 0, verbose: bool = False, preconditioner: str = "DILU", *,

@@ -39,7 +39,7 @@ def oracle_solve(d, rel, omega="standard", max_iter=20000):
                        np.zeros(d["n"]), pd, 0.0, rel, max_iter, threads=8, omega=omega)
 
 
-FORMS = ("persistent", "kernels", "gather")
+FORMS = ("persistent", "kernels", "gather", "fused")
 
 
 @pytest.mark.parametrize("form", FORMS)
@@ -178,7 +178,7 @@ def test_mixed_bicgstab_forms_agree():
         assert s.last_info.converged and true_rel(d, x.cpu().numpy()) < 1e-10
         xs[form] = x
     ref = xs["kernels"]
-    for form in ("persistent", "gather"):
+    for form in ("persistent", "gather", "fused"):
         assert float(torch.linalg.vector_norm(xs[form] - ref) / torch.linalg.vector_norm(ref)) < 1e-8
     with pytest.raises(ValueError, match="form"):
         MixedPrecisionPBiCGSTABSolver(form="fastest")
