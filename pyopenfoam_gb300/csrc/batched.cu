@@ -519,8 +519,10 @@ __device__ __forceinline__ int active_tile(const BTiles& T, const int* pref, int
   return __ldg(T.sys_tile0 + lo) + (t - pref[lo]);
 }
 
+// Compiled for 1536 resident threads per SM (40 registers): with every
+// phase's registers in one kernel it would otherwise hold 62 and run 1024.
 template <int BS, int KIND, int TPC>
-__global__ void __launch_bounds__(BS)
+__global__ void __launch_bounds__(BS, 1536 / BS)
     bmp_persistent_kernel(gbf_layout L, BTiles T, const double* __restrict__ coef64,
                           const double* __restrict__ diag64, const float* __restrict__ coef32,
                           const double* __restrict__ b, double* __restrict__ x, BVecs v,
