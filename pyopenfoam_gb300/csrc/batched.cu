@@ -30,11 +30,13 @@ struct BState {
 
 // Batch-wide control words, in the last 256 bytes of the workspace: the
 // number of systems still iterating, the "some system folds this
-// iteration" flag of the persistent form, and its grid barrier.
+// iteration" flag of the persistent form, its tile queue and its grid
+// barrier.
 struct BCtl {
   int running;
   int fold;
-  int pad[2];
+  unsigned int queue;  // tiles taken so far (wraps; only differences are used)
+  int pad;
   GridBarrier bar;
 };
 
@@ -445,9 +447,10 @@ __global__ void __launch_bounds__(BS) bmp_fold_kernel(BTiles T, double* __restri
 //
 // All CTAs are resident (cooperative launch).  Each phase walks the tiles of
 // the systems still running: every CTA holds, in shared memory, the prefix
-// sums of the running systems' tile counts, and takes active tiles
-// blockIdx.x, blockIdx.x + G, ...  The phases are separated by the bounded
-// grid barrier.  The map of running systems is rebuilt in the p phase, the
+// sums of the running systems' tile counts, takes active tile blockIdx.x
+// first and then further active tiles from the batch's tile queue, so that a
+// CTA whose tiles ran short takes more (see for_active_tiles).  The phases
+// are separated by the bounded grid barrier.  The map of running systems is rebuilt in the p phase, the
 // one phase in which no status changes (statuses change only at the end of
 // the Amul phase -- breakdown -- and of the true-residual phase), so every
 // CTA builds the same map; a system that stops later in the iteration keeps
@@ -519,6 +522,36 @@ __device__ __forceinline__ int active_tile(const BTiles& T, const int* pref, int
   return __ldg(T.sys_tile0 + lo) + (t - pref[lo]);
 }
 
+// Runs body(t) for the active tiles t < nact of one phase on this CTA: tile
+// blockIdx.x, then the tiles G + k that the queue hands out, k counted from
+// the queue's value when the phase began (base).  Thread 0 takes the next
+// ticket before the current tile starts, so the atomic's round trip hides
+// behind the tile.  Every CTA that ran a tile takes exactly one ticket that
+// comes back >= nact, and one that did not run any takes none, so a phase
+// takes exactly nact tickets whatever the timing: every CTA advances base by
+// nact and the next phase starts from the same value without a reset.  The
+// grid barrier between phases orders one phase's tickets before the next's.
+// Which CTA runs a tile never changes its result: the tile's partial sums
+// and the per-system scalars that the last tile of a system forms are
+// summed in a fixed order.
+template <typename Body>
+__device__ __forceinline__ void for_active_tiles(unsigned int* queue, unsigned int& base, int nact,
+                                                 Body&& body) {
+  __shared__ int s_next[2];  // double-buffered: one barrier per tile
+  const int G = (int)gridDim.x;
+  int t = (int)blockIdx.x, k = 0;
+  while (t < nact) {
+    unsigned int ticket = 0u;
+    if (threadIdx.x == 0) ticket = atomicAdd(queue, 1u);
+    body(t);
+    if (threadIdx.x == 0) s_next[k] = G + (int)(ticket - base);
+    __syncthreads();
+    t = s_next[k];
+    k ^= 1;
+  }
+  base += (unsigned int)nact;
+}
+
 // Compiled for 1536 resident threads per SM (40 registers): with every
 // phase's registers in one kernel it would otherwise hold 62 and run 1024.
 template <int BS, int KIND, int TPC>
@@ -535,23 +568,29 @@ __global__ void __launch_bounds__(BS, 1536 / BS)
   // keeps them unchanged until every CTA has built the same first map
   int nact = build_active_map<BS>(T, v, pref);
   if (!grid_barrier(bar, G)) return;
+  unsigned int* queue = &v.ctl->queue;
+  unsigned int base = 0u;  // the init kernel zeroed the queue
   const long long cap = (long long)P.max_iter + 4;
   for (long long it = 0; nact > 0 && it < cap; ++it) {
-    for (int t = blockIdx.x; t < nact; t += G)
+    for_active_tiles(queue, base, nact, [&](int t) {
       bmp_ap_tile<BS, KIND, true, TPC>(L, T, active_tile(T, pref, t), coef32, v, sh);
+    });
     if (!grid_barrier(bar, G)) return;
-    for (int t = blockIdx.x; t < nact; t += G)
+    for_active_tiles(queue, base, nact, [&](int t) {
       bmp_update_tile<BS, true>(T, active_tile(T, pref, t), x, v, delta, P, sh);
+    });
     if (!grid_barrier(bar, G)) return;
     if (__ldcg(&v.ctl->fold) != 0) {
-      for (int t = blockIdx.x; t < nact; t += G)
+      for_active_tiles(queue, base, nact, [&](int t) {
         bmp_true_tile<BS, true>(L, T, active_tile(T, pref, t), coef64, diag64, b, x, v, P, sh);
+      });
       if (!grid_barrier(bar, G)) return;
     }
     // p phase: no status changes here, so every CTA rebuilds the same map
     nact = build_active_map<BS>(T, v, pref);
     if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->fold = 0;  // read by all before this phase
-    for (int t = blockIdx.x; t < nact; t += G) bmp_p_tile<BS, true>(T, active_tile(T, pref, t), v);
+    for_active_tiles(queue, base, nact,
+                     [&](int t) { bmp_p_tile<BS, true>(T, active_tile(T, pref, t), v); });
     if (!grid_barrier(bar, G)) return;
   }
   // fold the FP32 corrections left in x32 into x (every tile once)
@@ -565,7 +604,8 @@ static size_t b256(size_t b) { return (b + 255) & ~(size_t)255; }
 __global__ void bmp_ctl_init_kernel(BCtl* ctl, int n_systems) {
   ctl->running = n_systems;
   ctl->fold = 0;
-  ctl->pad[0] = ctl->pad[1] = 0;
+  ctl->queue = 0u;
+  ctl->pad = 0;
   ctl->bar.count = 0ull;
   ctl->bar.fault = 0;
   ctl->bar.pad = 0;
