@@ -1531,13 +1531,20 @@ def run_assembly(args, rank, world, local):
             del mat._csr_cache[k]
         return (cls(mat).precond_diag,)
 
+    # the default dataflow walk, and the barrier-per-level walk it replaced
+    DICLevels = type("DICLevels", (DICPreconditioner,), {"factor_form": "levels"})
+    DILULevels = type("DILULevels", (DILUPreconditioner,), {"factor_form": "levels"})
     leg("dic_factorisation", lambda: fresh(A, DICPreconditioner),
+        lambda: (O.dic_build(own_i, nei, dg_h, up_h),), 16 * n + 16 * ni)
+    leg("dic_factorisation_levels", lambda: fresh(A, DICLevels),
         lambda: (O.dic_build(own_i, nei, dg_h, up_h),), 16 * n + 16 * ni)
     D = fvm.div(fl, torch.zeros(1), "Gauss upwind", mesh=m)
     M = LduMatrix(n, A.owner, A.neighbour, device=dev)
     M.diag, M.lower, M.upper = A.diag - D.diag, A.lower - D.lower, A.upper - D.upper
     md, ml, mu = (t.cpu().numpy() for t in (M.diag, M.lower, M.upper))
     leg("dilu_factorisation", lambda: fresh(M, DILUPreconditioner),
+        lambda: (O.dilu_build(own_i, nei, md, ml, mu),), 16 * n + 48 * ni)
+    leg("dilu_factorisation_levels", lambda: fresh(M, DILULevels),
         lambda: (O.dilu_build(own_i, nei, md, ml, mu),), 16 * n + 48 * ni)
 
     def dlap():

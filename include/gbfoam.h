@@ -100,6 +100,11 @@ int gbf_selftest_bounded_waits(int32_t* timed_out_h);
  * result_h[0] = the barrier's fault word (1 expected), result_h[1] = 1 if
  * the output was overwritten with NaN.  No GPU fault is involved.          */
 int gbf_selftest_wavefront_fault(int32_t* result_h);
+/* Self-test of the dataflow factorisations' failure path: two faces whose
+ * slot links point at each other (a cycle, 1000-pass limit).  result_h[0] =
+ * the fault word (1 expected), result_h[1] = 1 if the output is all NaN.
+ * No GPU fault is involved.                                                */
+int gbf_selftest_flow_fault(int32_t* result_h);
 /* Kernel timing probes (no reference counterpart; used by the benchmark to
  * time the dominant kernel inside a solve).  While enabled, the solvers
  * bracket the launches of their Amul kernels with CUDA events on the
@@ -157,6 +162,19 @@ int gbf_dic_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
 int gbf_dilu_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
                       const int32_t* neighbour_h, int32_t* level_ptr_h,
                       int32_t* level_faces_h, int32_t* n_levels, int32_t* max_level_size);
+
+/* Links of the dataflow DILU factorisation (gbf_dilu_build_flow_f64) for the
+ * schedule level_faces_h of gbf_dilu_schedule: item i (face level_faces[i])
+ * writes slots 2i (owner after the face) and 2i+1 (neighbour after it);
+ * prev_h[2i], prev_h[2i+1] (2 * n_faces entries) name the slots holding the
+ * two cells' values before the face in the sequential face order of
+ * preconditioners.py:254-268, -1 for the diagonal; cell_last_h (n_cells)
+ * the slot of each cell's last face, -1 if none.  GBF_ERR_ARG if
+ * level_faces_h is not a permutation or puts a face before one it reads;
+ * n_faces < 2^30.                                                          */
+int gbf_dilu_flow_links(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                        const int32_t* neighbour_h, const int32_t* level_faces_h,
+                        int32_t* prev_h, int32_t* cell_last_h);
 
 /* Per-cell boundary-face lists (ascending face order) for the assembly:
  * owner_b = owner of boundary faces n_internal..n_internal+n_bnd-1; bnd_ptr
@@ -251,6 +269,25 @@ int gbf_dilu_build_f64(const gbf_layout* L, const double* lower, const double* u
                        const double* diag, const int32_t* level_ptr,
                        const int32_t* level_faces, int32_t n_levels, int32_t max_level_size,
                        double* d_out, void* barrier, void* stream);
+/* The same two factorisations as dataflow walks, the same bits: no barrier
+ * between levels; every value a step reads sits in a slot that its producer
+ * fills, and a step waits only on the slots it reads (bounded waits; on
+ * timeout the barrier's fault word is set and d_out is NaN, as for the
+ * cooperative level walk).  One cooperative launch plus one output kernel;
+ * `barrier` (gbf_wavefront_barrier_bytes) is required.
+ * DIC (preconditioners.py:102-133): the cells of gbf_dic_schedule in level
+ * order; d_out doubles as the slots.                                       */
+int gbf_dic_build_flow_f64(const gbf_layout* L, const double* coef, const double* diag,
+                           const int32_t* level_cells, double* d_out, void* barrier,
+                           void* stream);
+/* DILU (preconditioners.py:228-272): the faces of gbf_dilu_schedule in level
+ * order with the links of gbf_dilu_flow_links; slots = device scratch of
+ * gbf_dilu_flow_slots_bytes(n_faces) bytes.                                */
+size_t gbf_dilu_flow_slots_bytes(int32_t n_faces);
+int gbf_dilu_build_flow_f64(const gbf_layout* L, const double* lower, const double* upper,
+                            const double* diag, const int32_t* level_faces, const int32_t* prev,
+                            const int32_t* cell_last, double* slots, double* d_out,
+                            void* barrier, void* stream);
 /* DIC/DILU apply(): z = r / d (preconditioners.py:151, :288).               */
 /* One triangular sweep of apply_full: for the faces of each level,
  * res[W] -= (coef[f] * res[R]) / d[R] if |d[R]| > 1e-30 (coef in face order:

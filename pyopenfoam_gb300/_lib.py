@@ -160,6 +160,7 @@ EXPORTED: dict[str, tuple] = {
                                            _c_vp, _c_vp, _c_vp]),
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
+    "gbf_dilu_flow_links": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_sweep_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
                                           _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_sweep_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_i32,
@@ -194,11 +195,16 @@ EXPORTED: dict[str, tuple] = {
     "gbf_amul_f32": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp]),
     "gbf_wavefront_barrier_bytes": (_c_size, []),
     "gbf_selftest_wavefront_fault": (ctypes.c_int, [_P(_c_i32)]),
+    "gbf_selftest_flow_fault": (ctypes.c_int, [_P(_c_i32)]),
     "gbf_wavefront_fault": (ctypes.c_int, [_c_vp, _P(_c_i32), _c_vp]),
     "gbf_dic_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
                                          _c_vp, _c_vp]),
     "gbf_dilu_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32,
                                           _c_vp, _c_vp, _c_vp]),
+    "gbf_dic_build_flow_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_dilu_flow_slots_bytes": (_c_size, [_c_i32]),
+    "gbf_dilu_build_flow_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                               _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_diag_apply_f64": (ctypes.c_int, [_c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_pcg_workspace_bytes": (_c_size, [_c_i32]),
     "gbf_pcg_solve_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,

@@ -20,7 +20,7 @@ import torch
 
 from .._lib import Layout, check, lib
 
-__all__ = ["Topology", "get_topology", "Schedule"]
+__all__ = ["Topology", "get_topology", "Schedule", "FlowLinks"]
 
 
 @dataclass
@@ -31,6 +31,16 @@ class Schedule:
     items: torch.Tensor
     n_levels: int
     max_level_size: int
+
+
+@dataclass
+class FlowLinks:
+    """Dataflow DILU links: prev[2i], prev[2i+1] = slots holding face item
+    i's owner / neighbour value before it (-1: the diagonal); cell_last[c] =
+    slot of cell c's last face (-1: none)."""
+
+    prev: torch.Tensor
+    cell_last: torch.Tensor
 
 
 def _i32_host(t: torch.Tensor, n_cells: int, name: str) -> np.ndarray:
@@ -121,6 +131,7 @@ class Topology:
         )
         self._dic: Schedule | None = None
         self._dilu: Schedule | None = None
+        self._dilu_flow: FlowLinks | None = None
         self._sweeps: dict = {}
 
     @property
@@ -185,7 +196,26 @@ class Topology:
             )
             self._dilu = Schedule(torch.from_numpy(ptr[: nl.value + 1].copy()).to(self.device),
                                   torch.from_numpy(faces).to(self.device), nl.value, mx.value)
+            self._dilu_faces_h = faces
         return self._dilu
+
+    def dilu_flow_links(self) -> FlowLinks:
+        """Slot links of the dataflow DILU factorisation over
+        ``dilu_schedule()`` (see ``gbf_dilu_flow_links``)."""
+        if self._dilu_flow is None:
+            self.dilu_schedule()
+            nf, n = self.n_faces, self.n_cells
+            prev = np.empty(max(2 * nf, 1), np.int32)
+            last = np.empty(max(n, 1), np.int32)
+            check(
+                lib().gbf_dilu_flow_links(n, nf, self._own_h.ctypes.data, self._nei_h.ctypes.data,
+                                          self._dilu_faces_h.ctypes.data, prev.ctypes.data,
+                                          last.ctypes.data),
+                "gbf_dilu_flow_links",
+            )
+            self._dilu_flow = FlowLinks(torch.from_numpy(prev).to(self.device),
+                                        torch.from_numpy(last).to(self.device))
+        return self._dilu_flow
 
     def sweep_schedule(self, reverse: bool, lower_only: bool) -> Schedule:
         """Level schedule of one triangular sweep of the full DIC/DILU solve

@@ -305,6 +305,58 @@ extern "C" int gbf_dilu_schedule(int32_t n, int32_t nf, const int32_t* own, cons
   return GBF_OK;
 }
 
+// Links of the dataflow DILU factorisation.  Item i of the level schedule
+// (face level_faces[i]) writes slots 2i (its owner's value after the face)
+// and 2i+1 (its neighbour's); prev[2i] and prev[2i+1] name the slots that
+// hold the two cells' values before the face -- the slot written by the
+// previous face touching the cell in face order, the sequential order of
+// preconditioners.py:254-268 -- or -1 where that is the diagonal.
+// cell_last[c] is the slot of the last face touching c, or -1.  Refuses a
+// level_faces that is not a permutation of the faces or that places a face
+// before one it reads (the walk would wait on a later step).
+extern "C" int gbf_dilu_flow_links(int32_t n, int32_t nf, const int32_t* own, const int32_t* nei,
+                                   const int32_t* level_faces, int32_t* prev,
+                                   int32_t* cell_last) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  if (nf >= (1 << 30)) {
+    gbf::set_error("dilu_flow_links: %d faces (at most 2^30 - 1)", nf);
+    return GBF_ERR_ARG;
+  }
+  if (n > 0 && !cell_last) {
+    gbf::set_error("dilu_flow_links: NULL pointer");
+    return GBF_ERR_ARG;
+  }
+  if (nf > 0 && (!level_faces || !prev)) {
+    gbf::set_error("dilu_flow_links: NULL pointer");
+    return GBF_ERR_ARG;
+  }
+  std::vector<int32_t> pos((size_t)nf, -1);
+  for (int32_t i = 0; i < nf; ++i) {
+    const int32_t f = level_faces[i];
+    if (f < 0 || f >= nf || pos[f] >= 0) {
+      gbf::set_error("dilu_flow_links: level_faces is not a permutation of the faces (item %d)",
+                     i);
+      return GBF_ERR_ARG;
+    }
+    pos[f] = i;
+  }
+  for (int32_t c = 0; c < n; ++c) cell_last[c] = -1;
+  for (int32_t f = 0; f < nf; ++f) {
+    const int32_t i = pos[f], p = own[f], q = nei[f];
+    const int32_t a = cell_last[p], b = cell_last[q];
+    if ((a >= 0 && a / 2 >= i) || (b >= 0 && b / 2 >= i)) {
+      gbf::set_error("dilu_flow_links: face %d is scheduled before a face it reads", f);
+      return GBF_ERR_ARG;
+    }
+    prev[2 * (int64_t)i] = a;
+    prev[2 * (int64_t)i + 1] = b;
+    cell_last[p] = 2 * i;
+    cell_last[q] = 2 * i + 1;
+  }
+  return GBF_OK;
+}
+
 // Per-cell lists of boundary faces in ascending face order (the order in
 // which fvm.laplacian's boundary scatter_add, operators.py:508-515, adds
 // them).  owner_b holds owner[n_internal .. n_internal + n_bnd); the listed

@@ -28,6 +28,7 @@ import torch
 
 from .. import _lib
 from ..core.ldu_matrix import LduMatrix
+from .preconditioners import factor_dic, factor_dilu
 from .residual import ConvergenceInfo
 
 __all__ = ["BatchedPCGSolver", "BatchLayout", "autotune_cache_path"]
@@ -37,6 +38,10 @@ TILE_CELLS = (1024, 2048, 4096, 8192)
 FORMS = {"plain": 0, "graph": 1, "persistent": 2, "persistent_graph": 3}
 TUNED_FORMS = ("graph", "persistent")
 THREADS_PER_CELL = (1, 2)
+#: wavefront grouping of the factorisation -> preconditioners.FACTOR_FORMS:
+#: a dataflow walk, one cooperative launch with a grid barrier per level, or
+#: one launch per level (the same bits)
+WAVEFRONTS = {"flow": "flow", "cooperative": "levels", "per_level": "per_level"}
 
 
 def autotune_cache_path() -> str:
@@ -143,8 +148,8 @@ class BatchedPCGSolver:
                              "or 'none'.")
         if form is not None and form not in FORMS:
             raise ValueError(f"form must be one of {sorted(FORMS)}, got {form!r}")
-        if wavefront not in (None, "cooperative", "per_level"):
-            raise ValueError("wavefront must be 'cooperative', 'per_level' or None")
+        if wavefront is not None and wavefront not in WAVEFRONTS:
+            raise ValueError(f"wavefront must be one of {tuple(WAVEFRONTS)} or None")
         if threads_per_cell not in (None, 1, 2):
             raise ValueError("threads_per_cell must be 1, 2 or None")
         self.threads_per_cell = threads_per_cell
@@ -171,8 +176,8 @@ class BatchedPCGSolver:
 
     def _factor(self, bl: BatchLayout, wavefront: str) -> torch.Tensor | None:
         """The FP64 DIC/DILU diagonal of the batch matrix, cached on it; its
-        level-scheduled wavefront runs in one cooperative launch or as one
-        launch per level (same bits)."""
+        wavefront runs as a dataflow walk, as one cooperative launch with a
+        grid barrier per level, or as one launch per level (same bits)."""
         if self.precond == "NONE":
             return None
         m = bl.matrix
@@ -190,27 +195,11 @@ class BatchedPCGSolver:
     def _build_factor(self, bl: BatchLayout, wavefront: str) -> torch.Tensor:
         m = bl.matrix
         topo = m.topology()
-        coef = m.packed()
         d = torch.empty(m.n_cells, device=bl.device, dtype=torch.float64)
-        bar = _lib.wavefront_barrier(bl.device) if wavefront == "cooperative" else None
-        bptr = None if bar is None else bar.data_ptr()
-        L = _lib.lib()
-        st = _lib.stream_ptr(bl.device)
         if self.precond == "DIC":
-            sched = topo.dic_schedule()
-            _lib.check(L.gbf_dic_build_f64(topo.layout_ref, coef.data_ptr(), m.diag.data_ptr(),
-                                           sched.ptr.data_ptr(), sched.items.data_ptr(),
-                                           sched.n_levels, sched.max_level_size, d.data_ptr(),
-                                           bptr, st), "gbf_dic_build_f64")
+            factor_dic(topo, m.packed(), m.diag, d, bl.device, WAVEFRONTS[wavefront])
         else:
-            sched = topo.dilu_schedule()
-            _lib.check(L.gbf_dilu_build_f64(topo.layout_ref, m.lower.data_ptr(),
-                                            m.upper.data_ptr(), m.diag.data_ptr(),
-                                            sched.ptr.data_ptr(), sched.items.data_ptr(),
-                                            sched.n_levels, sched.max_level_size, d.data_ptr(),
-                                            bptr, st), "gbf_dilu_build_f64")
-        if bar is not None:
-            _lib.check_wavefront(bar, "batched factorisation", bl.device)
+            factor_dilu(topo, m.lower, m.upper, m.diag, d, bl.device, WAVEFRONTS[wavefront])
         return d
 
     def _run(self, bl: BatchLayout, b: torch.Tensor, x: torch.Tensor, block: int, tile: int,
@@ -265,16 +254,16 @@ class BatchedPCGSolver:
             return {k: (fixed[k] if fixed[k] is not None else hit[k]) for k in fixed}
         if not self.autotune:
             return {"block": self.block_size or 256, "tile": self.tile_cells or 4096,
-                    "form": self.form or "graph", "wavefront": self.wavefront or "cooperative",
+                    "form": self.form or "graph", "wavefront": self.wavefront or "flow",
                     "tpc": self.threads_per_cell or 1}
         timings: dict = {}
         # wavefront of the factorisation: both ways once (same bits)
         if self.precond == "NONE":
-            wf = self.wavefront or "cooperative"
+            wf = self.wavefront or "flow"
         elif self.wavefront is None:
-            for w in ("cooperative", "per_level"):
+            for w in WAVEFRONTS:
                 timings[f"factor_{w}"] = self._timed(lambda w=w: self._build_factor(bl, w))
-            wf = min(("cooperative", "per_level"), key=lambda w: timings[f"factor_{w}"])
+            wf = min(WAVEFRONTS, key=lambda w: timings[f"factor_{w}"])
         else:
             wf = self.wavefront
         forms = [self.form] if self.form else list(TUNED_FORMS)

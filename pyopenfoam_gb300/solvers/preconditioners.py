@@ -1,14 +1,18 @@
 """DIC and DILU preconditioners on the GPU, drop-in for
 ``pyfoam.solvers.preconditioners`` (``src/pyfoam/solvers/preconditioners.py``).
 
-The factorised diagonal is built by libgbfoam's level-scheduled wavefront
-kernels, which apply the reference's sequential updates in the reference's
-order, so the diagonal is bitwise identical:
+The factorised diagonal is built by libgbfoam's wavefront kernels, which
+apply the reference's sequential updates in the reference's order, so the
+diagonal is bitwise identical:
 
 * DIC (``preconditioners.py:88-133``): cells ascending, for each face into
   the cell (face order) ``d[i] -= a*a / d[j]`` with ``a = upper[f]``;
 * DILU (``preconditioners.py:228-272``): faces ascending, both ends updated
   from the values before the face.
+
+By default the wavefront runs as a dataflow walk (``FACTOR_FORMS``): one
+cooperative launch in which every step waits only on the values it reads,
+with no barrier between levels.
 
 ``apply`` is the reference's diagonal-only ``r / d``; ``apply_full`` is the
 forward / diagonal / backward sweep pair (``:153-201``, ``:290-337``).
@@ -27,7 +31,69 @@ from .. import _lib
 from ..core.dtype import assert_floating
 from ..core.ldu_matrix import LduMatrix
 
-__all__ = ["Preconditioner", "DICPreconditioner", "DILUPreconditioner"]
+__all__ = ["Preconditioner", "DICPreconditioner", "DILUPreconditioner", "FACTOR_FORMS",
+           "factor_dic", "factor_dilu"]
+
+#: How a factorisation walks its level schedule, all giving the same bits:
+#: "flow" -- one cooperative launch, every step waiting only on the values it
+#: reads (gbf_dic_build_flow_f64 / gbf_dilu_build_flow_f64); "levels" -- one
+#: cooperative launch with a grid barrier between levels; "per_level" -- one
+#: launch per level.
+FACTOR_FORMS = ("flow", "levels", "per_level")
+
+
+def _check_form(form: str) -> None:
+    if form not in FACTOR_FORMS:
+        raise ValueError(f"factorisation form must be one of {FACTOR_FORMS}, got {form!r}")
+
+
+def factor_dic(topo, coef: torch.Tensor, diag: torch.Tensor, d: torch.Tensor, device,
+               form: str = "flow") -> None:
+    """DIC factorised diagonal of the FP64 matrix (coef = packed slots) into d;
+    raises if a bounded wait of a cooperative form ran out."""
+    _check_form(form)
+    sched = topo.dic_schedule()
+    L, st = _lib.lib(), _lib.stream_ptr(device)
+    bar = None if form == "per_level" else _lib.wavefront_barrier(device)
+    if form == "flow":
+        _lib.check(L.gbf_dic_build_flow_f64(topo.layout_ref, coef.data_ptr(), diag.data_ptr(),
+                                            sched.items.data_ptr(), d.data_ptr(),
+                                            bar.data_ptr(), st), "gbf_dic_build_flow_f64")
+    else:
+        _lib.check(L.gbf_dic_build_f64(topo.layout_ref, coef.data_ptr(), diag.data_ptr(),
+                                       sched.ptr.data_ptr(), sched.items.data_ptr(),
+                                       sched.n_levels, sched.max_level_size, d.data_ptr(),
+                                       None if bar is None else bar.data_ptr(), st),
+                   "gbf_dic_build_f64")
+    if bar is not None:
+        _lib.check_wavefront(bar, "DIC factorisation", device)
+
+
+def factor_dilu(topo, lower: torch.Tensor, upper: torch.Tensor, diag: torch.Tensor,
+                d: torch.Tensor, device, form: str = "flow") -> None:
+    """DILU factorised diagonal of the FP64 matrix into d; raises if a
+    bounded wait of a cooperative form ran out."""
+    _check_form(form)
+    sched = topo.dilu_schedule()
+    L, st = _lib.lib(), _lib.stream_ptr(device)
+    bar = None if form == "per_level" else _lib.wavefront_barrier(device)
+    if form == "flow":
+        links = topo.dilu_flow_links()
+        slots = torch.empty(max(2 * topo.n_faces, 1), dtype=torch.float64, device=device)
+        _lib.check(L.gbf_dilu_build_flow_f64(topo.layout_ref, lower.data_ptr(), upper.data_ptr(),
+                                             diag.data_ptr(), sched.items.data_ptr(),
+                                             links.prev.data_ptr(), links.cell_last.data_ptr(),
+                                             slots.data_ptr(), d.data_ptr(), bar.data_ptr(), st),
+                   "gbf_dilu_build_flow_f64")
+    else:
+        _lib.check(L.gbf_dilu_build_f64(topo.layout_ref, lower.data_ptr(), upper.data_ptr(),
+                                        diag.data_ptr(), sched.ptr.data_ptr(),
+                                        sched.items.data_ptr(), sched.n_levels,
+                                        sched.max_level_size, d.data_ptr(),
+                                        None if bar is None else bar.data_ptr(), st),
+                   "gbf_dilu_build_f64")
+    if bar is not None:
+        _lib.check_wavefront(bar, "DILU factorisation", device)
 
 
 class Preconditioner(Protocol):
@@ -48,6 +114,8 @@ def _as_f64_matrix(matrix: LduMatrix):
 
 class _DiagonalFactor:
     kind = ""
+    #: walk of the factorisation (one of FACTOR_FORMS; the same bits)
+    factor_form = "flow"
 
     def __init__(self, matrix: LduMatrix) -> None:
         self._matrix = matrix
@@ -95,17 +163,7 @@ class DICPreconditioner(_DiagonalFactor):
         d = torch.empty(self._matrix.n_cells, device=self._device, dtype=torch.float64)
         if self._matrix.n_cells == 0:
             return d.to(self._dtype)
-        sched = topo.dic_schedule()
-        coef = m64.packed()
-        bar = _lib.wavefront_barrier(self._device)
-        _lib.check(
-            _lib.lib().gbf_dic_build_f64(topo.layout_ref, coef.data_ptr(), diag.data_ptr(),
-                                         sched.ptr.data_ptr(), sched.items.data_ptr(),
-                                         sched.n_levels, sched.max_level_size, d.data_ptr(),
-                                         bar.data_ptr(), _lib.stream_ptr(self._device)),
-            "gbf_dic_build_f64",
-        )
-        _lib.check_wavefront(bar, "gbf_dic_build_f64", self._device)
+        factor_dic(topo, m64.packed(), diag, d, self._device, self.factor_form)
         return d.to(self._dtype)
 
     def apply_full(self, r: torch.Tensor) -> torch.Tensor:
@@ -127,17 +185,7 @@ class DILUPreconditioner(_DiagonalFactor):
         d = torch.empty(self._matrix.n_cells, device=self._device, dtype=torch.float64)
         if self._matrix.n_cells == 0:
             return d.to(self._dtype)
-        sched = topo.dilu_schedule()
-        bar = _lib.wavefront_barrier(self._device)
-        _lib.check(
-            _lib.lib().gbf_dilu_build_f64(topo.layout_ref, lower.data_ptr(), upper.data_ptr(),
-                                          diag.data_ptr(), sched.ptr.data_ptr(),
-                                          sched.items.data_ptr(), sched.n_levels,
-                                          sched.max_level_size, d.data_ptr(), bar.data_ptr(),
-                                          _lib.stream_ptr(self._device)),
-            "gbf_dilu_build_f64",
-        )
-        _lib.check_wavefront(bar, "gbf_dilu_build_f64", self._device)
+        factor_dilu(topo, lower, upper, diag, d, self._device, self.factor_form)
         return d.to(self._dtype)
 
     def apply_full(self, r: torch.Tensor) -> torch.Tensor:

@@ -100,12 +100,13 @@ def test_batched_two_threads_per_cell():
 def test_batched_factor_wavefront_forms_match():
     mats, rhs, _ = poisson_batch(3, lo=8, hi=12, seed=6)
     out = []
-    for wf in ("cooperative", "per_level"):
+    for wf in ("flow", "cooperative", "per_level"):
         s = BatchedPCGSolver(tolerance=0.0, rel_tol=1e-8, max_iter=2000, block_size=256,
                              tile_cells=1024, form="graph", wavefront=wf)
         out.append([x.cpu().numpy() for x, _, _ in s.solve(mats, rhs)])
-    for u, v in zip(*out):
+    for u, v, w in zip(*out):
         np.testing.assert_array_equal(u, v)
+        np.testing.assert_array_equal(u, w)
 
 
 def test_batched_persistent_form_against_oracle(tmp_path, monkeypatch):
@@ -136,7 +137,7 @@ def test_batched_autotuner_considers_both_forms(tmp_path, monkeypatch):
     assert any(k.endswith("x2") for k in t if ":" in k and not k.startswith("full"))
     assert s.last_config["tpc"] in (1, 2)
     assert "full_solve:graph" in t and "full_solve:persistent" in t
-    assert "factor_cooperative" in t and "factor_per_level" in t
+    assert "factor_flow" in t and "factor_cooperative" in t and "factor_per_level" in t
     assert s.last_config["form"] in ("graph", "persistent")
 
 

@@ -160,6 +160,54 @@ def test_dilu_schedule_respects_face_order(perm):
             last[cell] = f
 
 
+def _flow_links(n, own, nei, items):
+    o = np.ascontiguousarray(own, np.int32)
+    q = np.ascontiguousarray(nei, np.int32)
+    it = np.ascontiguousarray(items, np.int32)
+    prev = np.empty(max(2 * o.shape[0], 1), np.int32)
+    last = np.empty(max(n, 1), np.int32)
+    rc = _lib.lib().gbf_dilu_flow_links(n, o.shape[0], o.ctypes.data, q.ctypes.data,
+                                        it.ctypes.data, prev.ctypes.data, last.ctypes.data)
+    return rc, prev, last
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_dilu_flow_links_name_the_previous_face_of_each_end(perm):
+    """Slot links of the dataflow DILU walk against a plain restatement of
+    the sequential face loop (preconditioners.py:254-268): item i's owner
+    and neighbour read the slot written by the previous face touching that
+    cell in face order, and cell_last names each cell's last face."""
+    c = random_ldu(5, seed=8, permute_faces=perm)
+    n, own, nei = c["n"], c["owner"], c["neighbour"]
+    nf = own.shape[0]
+    o = np.ascontiguousarray(own, np.int32)
+    q = np.ascontiguousarray(nei, np.int32)
+    ptr = np.empty(nf + 1, np.int32)
+    items = np.empty(nf, np.int32)
+    nl, mx = ctypes.c_int32(), ctypes.c_int32()
+    _lib.check(_lib.lib().gbf_dilu_schedule(n, nf, o.ctypes.data, q.ctypes.data,
+                                            ptr.ctypes.data, items.ctypes.data,
+                                            ctypes.byref(nl), ctypes.byref(mx)))
+    rc, prev, last = _flow_links(n, own, nei, items)
+    assert rc == 0
+    pos = np.empty(nf, int)
+    pos[items] = np.arange(nf)
+    expect_last = {}
+    for f in range(nf):
+        i = pos[f]
+        for side, cell in ((0, own[f]), (1, nei[f])):
+            want = expect_last.get(cell, -1)
+            assert prev[2 * i + side] == want
+            assert want < 0 or want // 2 < i  # an earlier item of the walk
+            expect_last[cell] = 2 * i + side
+    assert all(last[cl] == expect_last.get(cl, -1) for cl in range(n))
+    # refusals: not a permutation; a face placed before one it reads
+    bad = items.copy()
+    bad[1] = bad[0]
+    assert _flow_links(n, own, nei, bad)[0] != 0
+    assert _flow_links(n, own, nei, np.arange(nf)[::-1].copy())[0] != 0
+
+
 def test_topology_rejects_bad_addressing():
     L = _lib.lib()
     o = np.array([0, 5], np.int32)
