@@ -14,8 +14,10 @@ the 129 MB L2, so no flush is needed between steps).  The FP64 PCG solve of
 the same system is timed once beside it for the speed-up.
 
 ``e2e`` repeats the step through the public API with HOST buffers: the
-matrix coefficients and RHS are copied from pinned host memory and x is read
-back inside the timed region.
+page-locked host coefficients and RHS go to the LduMatrix setters and
+``to_device`` (which move them with the SMs over NVLink-C2C) and x is read
+back with ``to_host``, all inside the timed region; the same loop with
+copy-engine copies is timed beside it (``e2e.copy_engine_loop``).
 
 ``roofline``: the dominant kernel is the FP32 Amul + p.Ap reduction of the
 inner iteration.  ``achieved`` is the bytes that kernel moves per launch in
@@ -459,6 +461,7 @@ def run_ours(args, rank, world, local):
     import ctypes
 
     from pyopenfoam_gb300 import MixedPrecisionPCGSolver, PCGSolver, _lib
+    from pyopenfoam_gb300.core.device import to_device, to_host
     from pyopenfoam_gb300.mesh.poisson import hex_poisson
 
     dev = torch.device("cuda", local)
@@ -513,36 +516,64 @@ def run_ours(args, rank, world, local):
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = n * 8
     xs_host = torch.empty(n, dtype=torch.float64).pin_memory()
-    # device buffers the caller keeps across steps (as a time loop would):
-    # each step copies all four host arrays into them, then hands them to the
-    # setters, solves and reads x back
-    dbuf = {k: torch.empty_like(t, device=dev) for k, t in host.items()}
     link = None if args.no_e2e else _pinned_link_probe(dev)
-    e2e_times, h2d_times, per_copy, host_setters = [], [], {k: [] for k in names}, []
+    # each step hands the page-locked host arrays to the public API: the
+    # LduMatrix setters and to_device upload them (by the SMs, over
+    # NVLink-C2C; each returns when its copy is done), the solver runs, and
+    # to_host reads x back into page-locked memory
+    e2e_times, h2d_times, d2h_times = [], [], []
+    per_copy, host_setters = {k: [] for k in names}, []
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 3)]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ev[0].record()
-        for j, k in enumerate(names):
-            dbuf[k].copy_(host[k], non_blocking=True)
-            ev[j + 1].record()  # stream-ordered after copy j: its device time alone
+        m.diag = host["diag"]
+        ev[1].record()  # stream-ordered after upload j: its device time alone
+        m.lower = host["lower"]
+        ev[2].record()
+        m.upper = host["upper"]
+        ev[3].record()
+        bd = to_device(host["b"], dev, torch.float64)
+        ev[4].record()
         t1 = time.perf_counter()
-        m.diag, m.lower, m.upper = dbuf["diag"], dbuf["lower"], dbuf["upper"]
-        t2 = time.perf_counter()
-        xe, _, _ = mixed(m, dbuf["b"], x0)
-        xs_host.copy_(xe, non_blocking=True)
+        xe, _, _ = mixed(m, bd, x0)
+        ev[5].record()
+        to_host(xe, xs_host)
+        ev[6].record()
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
-            h2d_times.append(ev[0].elapsed_time(ev[-1]) / 1e3)
+            h2d_times.append(ev[0].elapsed_time(ev[4]) / 1e3)
+            d2h_times.append(ev[5].elapsed_time(ev[6]) / 1e3)
             for j, k in enumerate(names):
                 per_copy[k].append(ev[j].elapsed_time(ev[j + 1]) / 1e3)
-            host_setters.append(t2 - t1)
+            host_setters.append(t1 - t0)
     # median over the steps (one slow step -- a host-side stall -- moved the
     # mean by up to 10 %); the mean is reported beside it
     e2e = max_over_ranks(statistics.median(e2e_times), world) if e2e_times else None
     e2e_mean = max_over_ranks(statistics.mean(e2e_times), world) if e2e_times else None
+    # the same loop with the copy engines (device buffers kept across steps,
+    # torch copy_ from the same page-locked arrays), for comparison
+    ce_times, ce_h2d = [], []
+    if not args.no_e2e:
+        dbuf = {k: torch.empty_like(t, device=dev) for k, t in host.items()}
+        for i in range(1 + min(args.steps, 3)):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ev0.record()
+            for k in names:
+                dbuf[k].copy_(host[k], non_blocking=True)
+            ev1.record()
+            m.diag, m.lower, m.upper = dbuf["diag"], dbuf["lower"], dbuf["upper"]
+            xe, _, _ = mixed(m, dbuf["b"], x0)
+            xs_host.copy_(xe, non_blocking=True)
+            torch.cuda.synchronize()
+            if i > 0:
+                ce_times.append(time.perf_counter() - t0)
+                ce_h2d.append(ev0.elapsed_time(ev1) / 1e3)
+        del dbuf
 
     # --- FP64 comparison: the same system, the same API, the same K steps ---
     x64 = None
@@ -635,9 +666,21 @@ def run_ours(args, rank, world, local):
                     "h2d_s_per_array_median": {k: statistics.median(v) for k, v in
                                                per_copy.items()} if h2d_times else None,
                     "h2d_GBs": h2d / statistics.median(h2d_times) / 1e9 if h2d_times else None,
-                    "link_probe_GBs": link,
-                    "setters_host_s_median": (statistics.median(host_setters)
+                    "d2h_s_median": statistics.median(d2h_times) if d2h_times else None,
+                    "copies": "by the SMs over NVLink-C2C (gbf_copy_from_host / "
+                              "gbf_copy_to_host) through the LduMatrix setters, to_device and "
+                              "to_host, from and into page-locked host arrays",
+                    "uploads_host_s_median": (statistics.median(host_setters)
                                               if host_setters else None),
+                    "copy_engine_loop": {
+                        "s_median": statistics.median(ce_times) if ce_times else None,
+                        "h2d_s_median": statistics.median(ce_h2d) if ce_h2d else None,
+                        "steps": len(ce_times),
+                        "what": "the same loop with torch copy_ (copy engines) into kept "
+                                "device buffers"},
+                    "link_probe_GBs": link,
+                    "link_probe": "one 256 MB copy-engine copy from page-locked memory, best "
+                                  "of 4",
                     "host": _host_placement(dev)},
             "clocks": clk.summary(),
             "gpu_launches": launches,

@@ -88,6 +88,15 @@ int gbf_stream_fault(int32_t* fault);
 int gbf_version(void);
 /* Number of SMs of the current device (grid sizing of the reductions).     */
 int gbf_device_sm_count(int32_t* n_sm);
+/* Host <-> device copies driven by the SMs (loads / stores of page-locked
+ * host memory over NVLink-C2C) instead of the copy engines; no reference
+ * counterpart (the reference moves tensors with torch's .to(), i.e. the copy
+ * engines).  src_host / dst_host must be page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister; torch pin_memory), the other side
+ * device memory; anything else is refused with GBF_ERR_ARG.  Asynchronous
+ * on `stream`; any alignment and size.                                      */
+int gbf_copy_from_host(void* dst, const void* src_host, size_t bytes, void* stream);
+int gbf_copy_to_host(void* dst_host, const void* src, size_t bytes, void* stream);
 /* Self-test of the bounded device-side waits (no reference counterpart):
  * makes a grid-barrier wait (one participant never arrives) and an mbarrier
  * wait (nothing ever completes it) run out after short poll limits, on the

@@ -196,6 +196,8 @@ EXPORTED: dict[str, tuple] = {
     "gbf_wavefront_barrier_bytes": (_c_size, []),
     "gbf_selftest_wavefront_fault": (ctypes.c_int, [_P(_c_i32)]),
     "gbf_selftest_flow_fault": (ctypes.c_int, [_P(_c_i32)]),
+    "gbf_copy_from_host": (ctypes.c_int, [_c_vp, _c_vp, _c_size, _c_vp]),
+    "gbf_copy_to_host": (ctypes.c_int, [_c_vp, _c_vp, _c_size, _c_vp]),
     "gbf_wavefront_fault": (ctypes.c_int, [_c_vp, _P(_c_i32), _c_vp]),
     "gbf_dic_build_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
                                          _c_vp, _c_vp]),

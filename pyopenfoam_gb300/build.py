@@ -36,6 +36,7 @@ SOURCES = [
     "smooth.cu",
     "gamg.cu",
     "selftest.cu",
+    "hostcopy.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

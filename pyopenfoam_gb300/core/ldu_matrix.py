@@ -17,7 +17,7 @@ from __future__ import annotations
 import torch
 
 from .. import _lib
-from .device import resolve_device
+from .device import resolve_device, to_device
 from .dtype import CFD_DTYPE, INDEX_DTYPE, assert_floating
 from .topology import Topology, get_topology
 
@@ -94,7 +94,7 @@ class LduMatrix:
     def _coerce(self, value: torch.Tensor, size: int, name: str) -> torch.Tensor:
         if not isinstance(value, torch.Tensor):
             value = torch.as_tensor(value)
-        v = value.to(device=self._device, dtype=self._dtype).contiguous()
+        v = to_device(value, self._device, self._dtype)
         if v.dim() != 1 or v.shape[0] != size:
             raise ValueError(f"{name} must have shape ({size},), got {tuple(v.shape)}")
         return v

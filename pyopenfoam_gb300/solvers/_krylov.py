@@ -8,6 +8,7 @@ import ctypes
 import torch
 
 from .. import _lib
+from ..core.device import to_device
 from ..core.ldu_matrix import LduMatrix
 from .residual import ConvergenceInfo, ResidualMonitor
 
@@ -31,7 +32,7 @@ def run_solver(fn_name: str, ws_name: str, matrix: LduMatrix, source: torch.Tens
         raise ValueError(
             f"source/x0 have {source.shape[0]}/{x0.shape[0]} elements, expected {n}"
         )
-    b = source.to(device=dev, dtype=torch.float64).contiguous()
+    b = to_device(source, dev, torch.float64)
     x = x0.to(device=dev, dtype=torch.float64).clone().contiguous()
     topo = matrix.topology()
     coef = matrix.packed()

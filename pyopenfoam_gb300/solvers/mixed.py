@@ -20,6 +20,7 @@ import ctypes
 import torch
 
 from .. import _lib
+from ..core.device import to_device
 from ..core.ldu_matrix import LduMatrix
 from .linear_solver import LinearSolverBase
 from .preconditioners import DICPreconditioner, DILUPreconditioner, Preconditioner
@@ -74,7 +75,7 @@ class MixedPrecisionPCGSolver(LinearSolverBase):
         if source.shape[0] != n or x0.shape[0] != n:
             raise ValueError(f"source/x0 have {source.shape[0]}/{x0.shape[0]} elements, "
                              f"expected {n}")
-        b = source.to(device=dev, dtype=torch.float64).contiguous()
+        b = to_device(source, dev, torch.float64)
         x = x0.to(device=dev, dtype=torch.float64).clone().contiguous()
         precond = self._make_preconditioner(matrix)
         pd = None if precond is None else precond.precond_diag
@@ -179,7 +180,7 @@ class MixedPrecisionPBiCGSTABSolver(LinearSolverBase):
         if source.shape[0] != n or x0.shape[0] != n:
             raise ValueError(f"source/x0 have {source.shape[0]}/{x0.shape[0]} elements, "
                              f"expected {n}")
-        b = source.to(device=dev, dtype=torch.float64).contiguous()
+        b = to_device(source, dev, torch.float64)
         x = x0.to(device=dev, dtype=torch.float64).clone().contiguous()
         precond = self._make_preconditioner(matrix)
         pd = None if precond is None else precond.precond_diag
