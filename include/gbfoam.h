@@ -478,6 +478,16 @@ int gbf_gauss_seidel_f64(const gbf_layout* L, const double* slot_coef, const dou
                          const double* b, const int32_t* level_ptr, const int32_t* level_cells,
                          const int32_t* level_ptr_h, int32_t n_levels, double omega,
                          int32_t relax, double* x, void* barrier, void* stream);
+/* The same sweep as a dataflow walk (no barrier between levels; the same
+ * bits): the cells of gbf_gs_schedule(reverse) in level order, old values
+ * read from x, new ones written to `scratch` (n_cells doubles of device
+ * memory, not x) and copied back into x at the end.  `barrier` (64 bytes,
+ * gbf_wavefront_barrier_bytes) is required; a wait that runs out sets its
+ * fault word and x becomes NaN.                                            */
+int gbf_gauss_seidel_flow_f64(const gbf_layout* L, const double* coef, const double* diag,
+                              const double* b, const int32_t* level_cells, int32_t reverse,
+                              double omega, int32_t relax, double* x, double* scratch,
+                              void* barrier, void* stream);
 /* r = b - A x, A x bitwise LduMatrix.Ax (core/ldu_matrix.py:172-217); the
  * residual of every smoother and of the smoothing solvers.                 */
 int gbf_residual_f64(const gbf_layout* L, const double* slot_coef, const double* diag,

@@ -151,48 +151,7 @@ __global__ void __launch_bounds__(kBlock)
 // and the order of the subtractions are those of the level-scheduled
 // kernels, so the results are the same bits.
 //
-// The empty marker is the all-ones bit pattern (a NaN); a NaN result is
-// stored as the canonical NaN so that it cannot read as empty.  Every wait
-// is bounded: after max_polls passes a warp sets the barrier's fault word
-// and returns, and the warps that see the fault word return too; the
-// output kernel then writes NaN everywhere.
-constexpr long long kFlowEmpty = -1LL;
-constexpr long long kFlowPolls = 1LL << 22;  // a few seconds of passes
-
-__device__ __forceinline__ double ld_flow(const double* p) {
-  double v;
-  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_flow(double* p, double v) {
-  if (v != v) v = __longlong_as_double(0x7ff8000000000000LL);
-  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
-}
-
-__device__ __forceinline__ bool flow_empty(double v) {
-  return __double_as_longlong(v) == kFlowEmpty;
-}
-
-// End of one pass over a chunk: true when every lane is done; false with
-// *quit set when a wait ran out here or elsewhere.
-__device__ __forceinline__ bool flow_pass_end(bool done, long long& polls, long long max_polls,
-                                              GridBarrier* bar, bool* quit) {
-  if (__all_sync(0xffffffffu, done)) return true;
-  ++polls;
-  if (polls > max_polls) {
-    if ((threadIdx.x & 31) == 0) atomicExch(&bar->fault, 1);
-    *quit = true;
-    return false;
-  }
-  // one decision for the whole warp (polls is the same in every lane)
-  if ((polls & 63) == 0 && __any_sync(0xffffffffu, *(volatile int*)&bar->fault != 0)) {
-    *quit = true;
-    return false;
-  }
-  __nanosleep(64);
-  return false;
-}
+// The slots, the empty marker and the bounded pass loop: wavefront.cuh.
 
 // DIC: step = one cell of the level schedule; its slot is d[c] itself
 // (every cell's factored value is written once, by its own step, and read

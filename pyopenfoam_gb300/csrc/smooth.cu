@@ -24,13 +24,13 @@
 
 namespace gbf {
 
-template <bool RELAX>
-__device__ __forceinline__ void gs_cell(const gbf_layout& L, const double* __restrict__ coef,
-                                        const double* __restrict__ diag,
-                                        const double* __restrict__ b, int c, double omega,
-                                        double* x) {
-  const double dc = __ldg(diag + c);
-  const double xc = __ldcg(x + c);
+// The row sum of cell c's update: dc * xc, then coef * x[col] over the
+// cell's slots in ascending face order (owner-side and neighbour-side slots
+// merged by face index), one rounding per operation.  fetch(col) gives the
+// x value the update reads at col.
+template <typename FETCH>
+__device__ __forceinline__ double gs_row(const gbf_layout& L, const double* __restrict__ coef,
+                                         double dc, double xc, int c, FETCH&& fetch) {
   double row = __dmul_rn(dc, xc);
   bool merged = false;
   if (L.n_faces > 0) {
@@ -50,7 +50,7 @@ __device__ __forceinline__ void gs_cell(const gbf_layout& L, const double* __res
         fk[k] = use ? __ldg(L.slot_face + slot) : -1;
         const int col = use ? slot_column(L, cs.e0 + slot_k, slot, c) : -1;
         a[k] = use ? __ldg(coef + slot) : 0.0;
-        xv[k] = (use && col >= 0) ? __ldcg(x + col) : 0.0;
+        xv[k] = (use && col >= 0) ? fetch(col) : 0.0;
       }
       int max_nei = -1, min_own = INT_MAX;
 #pragma unroll
@@ -82,18 +82,36 @@ __device__ __forceinline__ void gs_cell(const gbf_layout& L, const double* __res
       const int k = fi < fj ? i : cs.wo + j;
       const int slot = cs.base + 32 * k;
       const int col = slot_column(L, cs.e0 + k, slot, c);
-      row = __dadd_rn(row, __dmul_rn(__ldg(coef + slot), __ldcg(x + col)));
+      row = __dadd_rn(row, __dmul_rn(__ldg(coef + slot), fetch(col)));
       if (fi < fj)
         ++i;
       else
         ++j;
     }
   }
+  return row;
+}
+
+// The updated value of cell c from its row sum (the value itself when the
+// diagonal is too small to divide by, as in the reference).
+template <bool RELAX>
+__device__ __forceinline__ double gs_update(double row, double dc, double xc, double bc,
+                                            double omega) {
   const double off = __dsub_rn(row, __dmul_rn(dc, xc));
-  if (fabs(dc) > 1e-30) {
-    const double nv = __ddiv_rn(__dsub_rn(__ldg(b + c), off), dc);
-    x[c] = RELAX ? __dadd_rn(xc, __dmul_rn(omega, __dsub_rn(nv, xc))) : nv;
-  }
+  if (!(fabs(dc) > 1e-30)) return xc;
+  const double nv = __ddiv_rn(__dsub_rn(bc, off), dc);
+  return RELAX ? __dadd_rn(xc, __dmul_rn(omega, __dsub_rn(nv, xc))) : nv;
+}
+
+template <bool RELAX>
+__device__ __forceinline__ void gs_cell(const gbf_layout& L, const double* __restrict__ coef,
+                                        const double* __restrict__ diag,
+                                        const double* __restrict__ b, int c, double omega,
+                                        double* x) {
+  const double dc = __ldg(diag + c);
+  const double xc = __ldcg(x + c);
+  const double row = gs_row(L, coef, dc, xc, c, [&](int col) { return __ldcg(x + col); });
+  if (fabs(dc) > 1e-30) x[c] = gs_update<RELAX>(row, dc, xc, __ldg(b + c), omega);
 }
 
 template <bool RELAX>
@@ -119,6 +137,68 @@ __global__ void __launch_bounds__(kBlock)
         gs_cell<RELAX>(L, coef, diag, b, __ldg(level_cells + i), omega, x);
       }))
     poison(x, L.n_cells);
+}
+
+// A whole Gauss-Seidel sweep as a dataflow walk (wavefront.cuh): the cells
+// of the level schedule in level order, dealt 32 at a time round-robin to
+// the warps of one block per SM.  The sweep reads the old values from x_old
+// (never written during the walk) and writes the new ones into the slots
+// x_new (initialised to the empty marker); a cell polls only the new values
+// it reads -- its neighbours swept before it (lower-numbered forward,
+// higher-numbered backward), which are at earlier levels -- so the warp
+// holding the earliest unfinished cell always finds its inputs.  The row sum
+// and the update are gs_cell's (gs_row, gs_update): the same bits.
+template <bool RELAX>
+__global__ void __launch_bounds__(kBlock)
+    gs_flow_kernel(gbf_layout L, const double* __restrict__ coef, const double* __restrict__ diag,
+                   const double* __restrict__ b, const int32_t* __restrict__ cells, int reverse,
+                   double omega, const double* __restrict__ x_old, double* x_new,
+                   GridBarrier* bar, long long max_polls) {
+  const int n = L.n_cells;
+  const int lane = threadIdx.x & 31;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long chunks = ((long long)n + 31) >> 5;
+  long long polls = 0;
+  for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < chunks;
+       ch += warps) {
+    const long long i = ch * 32 + lane;
+    bool done = i >= n;
+    int c = 0;
+    double dc = 0.0, xc = 0.0, bc = 0.0;
+    if (!done) {
+      c = __ldg(cells + i);
+      dc = __ldg(diag + c);
+      xc = __ldg(x_old + c);
+      bc = __ldg(b + c);
+    }
+    bool quit = false;
+    for (;;) {
+      if (!done) {
+        bool missing = false;
+        const double row = gs_row(L, coef, dc, xc, c, [&](int col) {
+          if (reverse ? col > c : col < c) {
+            const double v = ld_flow(x_new + col);
+            missing |= flow_empty(v);
+            return v;
+          }
+          return __ldg(x_old + col);
+        });
+        if (!missing) {
+          st_flow(x_new + c, gs_update<RELAX>(row, dc, xc, bc, omega));
+          done = true;
+        }
+      }
+      if (flow_pass_end(done, polls, max_polls, bar, &quit)) break;
+      if (quit) return;
+    }
+  }
+}
+
+// x = the new values, or NaN everywhere if a wait of the walk ran out.
+__global__ void gs_flow_out_kernel(int n, const GridBarrier* bar, const double* __restrict__ x_new,
+                                   double* __restrict__ x) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) x[c] = bar->fault != 0 ? __longlong_as_double(0x7ff8000000000000LL) : x_new[c];
 }
 
 // r = b - A x with A x in the reference's order (cell_amul).
@@ -265,6 +345,38 @@ extern "C" int gbf_gauss_seidel_f64(const gbf_layout* L, const double* coef, con
       gs_level_kernel<false><<<grid, kBlock, 0, s>>>(*L, coef, diag, b, level_ptr, level_cells,
                                                      l, omega, x);
   }
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
+extern "C" int gbf_gauss_seidel_flow_f64(const gbf_layout* L, const double* coef,
+                                         const double* diag, const double* b,
+                                         const int32_t* level_cells, int32_t reverse,
+                                         double omega, int32_t relax, double* x, double* scratch,
+                                         void* barrier, void* stream) {
+  ::gbf::NvtxScope nvtx_("gbf_gauss_seidel_flow_f64");
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int n = L->n_cells;
+  if (n == 0) return GBF_OK;
+  GBF_REQUIRE(diag && b && x && level_cells && scratch && barrier && (L->n_faces == 0 || coef),
+              "gauss_seidel_flow: NULL pointer");
+  GBF_REQUIRE(scratch != x, "gauss_seidel_flow: scratch must not be x");
+  cudaStream_t s = as_stream(stream);
+  const void* k = relax ? (const void*)gs_flow_kernel<true> : (const void*)gs_flow_kernel<false>;
+  // one block per SM (the polling of warps ahead of the front slows it)
+  const int grid = wavefront_grid(k, kBlock, n, 1);
+  GBF_REQUIRE(grid > 0, "gauss_seidel_flow: the device cannot launch cooperative kernels");
+  GBF_CHECK_CUDA(cudaMemsetAsync(scratch, 0xff, sizeof(double) * (size_t)n, s));
+  gbf_layout Lc = *L;
+  int rev = reverse != 0;
+  long long polls = kFlowPolls;
+  GridBarrier* bar = static_cast<GridBarrier*>(barrier);
+  const double* xo = x;
+  void* args[] = {&Lc, (void*)&coef, (void*)&diag, (void*)&b, (void*)&level_cells, &rev,
+                  &omega, (void*)&xo, &scratch, &bar, &polls};
+  GBF_CHECK_CUDA(launch_wavefront(k, grid, args, barrier, s));
+  gs_flow_out_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(n, bar, scratch, x);
   GBF_CHECK_LAUNCH();
   return GBF_OK;
 }

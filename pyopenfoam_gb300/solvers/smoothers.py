@@ -68,19 +68,38 @@ def _gs_schedule(matrix: LduMatrix, reverse: bool) -> _GsSchedule:
     return cache[reverse]
 
 
+#: How a Gauss-Seidel sweep walks its level schedule (the same bits):
+#: "flow" -- one cooperative launch in which a cell waits only on the new
+#: values it reads (gbf_gauss_seidel_flow_f64); "levels" -- one cooperative
+#: launch with a grid barrier per level; "per_level" -- a launch per level.
+GS_FORMS = ("flow", "levels", "per_level")
+
+
 def gs_sweep(matrix: LduMatrix, x: torch.Tensor, b: torch.Tensor, reverse: bool = False,
-             omega: float = 1.0, relax: bool = False) -> None:
+             omega: float = 1.0, relax: bool = False, form: str = "flow") -> None:
     """One Gauss-Seidel sweep over x in place: cells ascending (or
     descending with ``reverse``); ``relax`` uses x_c += omega (new - x_c)
-    (GaussSeidelSmoother), otherwise x_c = new (SmoothSolver)."""
+    (GaussSeidelSmoother), otherwise x_c = new (SmoothSolver).  If a bounded
+    wait of a cooperative form runs out, x becomes NaN."""
+    if form not in GS_FORMS:
+        raise ValueError(f"form must be one of {GS_FORMS}, got {form!r}")
     sch = _gs_schedule(matrix, reverse)
     topo = matrix.topology()
     coef = matrix.packed()
+    st = _lib.stream_ptr(matrix.device)
+    if form == "flow":
+        scratch = torch.empty(max(matrix.n_cells, 1), dtype=torch.float64, device=matrix.device)
+        _lib.check(_lib.lib().gbf_gauss_seidel_flow_f64(
+            topo.layout_ref, coef.data_ptr(), matrix.diag.data_ptr(), b.data_ptr(),
+            sch.cells.data_ptr(), int(reverse), float(omega), int(relax), x.data_ptr(),
+            scratch.data_ptr(), _lib.wavefront_barrier(matrix.device).data_ptr(), st),
+            "gbf_gauss_seidel_flow_f64")
+        return
+    bar = _lib.wavefront_barrier(matrix.device) if form == "levels" else None
     _lib.check(_lib.lib().gbf_gauss_seidel_f64(
         topo.layout_ref, coef.data_ptr(), matrix.diag.data_ptr(), b.data_ptr(), sch.ptr.data_ptr(),
         sch.cells.data_ptr(), sch.ptr_h.ctypes.data, sch.n_levels, float(omega), int(relax),
-        x.data_ptr(), _lib.wavefront_barrier(matrix.device).data_ptr(),
-        _lib.stream_ptr(matrix.device)), "gbf_gauss_seidel_f64")
+        x.data_ptr(), None if bar is None else bar.data_ptr(), st), "gbf_gauss_seidel_f64")
 
 
 def residual(matrix: LduMatrix, b: torch.Tensor, x: torch.Tensor,

@@ -13,6 +13,8 @@ import numpy as np
 import pytest
 import torch
 
+from oracle import oracle as O
+
 from pyopenfoam_gb300 import LduMatrix, create_solver, solver_from_dict
 from pyopenfoam_gb300.solvers import (DICGSmoother, GaussSeidelSmoother, JacobiSmoother,
                                       SmoothSolver)
@@ -143,3 +145,39 @@ def test_wavefront_single_launch_matches_per_level_launches(N, perm):
                 return x.cpu().numpy()
             a, b = both(gs)
             assert _eq(a, b), ("gs", reverse, relax)
+
+
+@pytest.mark.parametrize("N,perm", [(12, True), (24, False), (48, True)])
+def test_gauss_seidel_flow_matches_level_walks(N, perm):
+    """The Gauss-Seidel sweep as a dataflow walk (gbf_gauss_seidel_flow_f64,
+    the default of gs_sweep) gives the bits of the level walks (grid barrier
+    per level, and a launch per level), forward and backward, plain and
+    relaxed, on sorted and shuffled face orders; and the oracle's serial
+    sweep.  A zero diagonal entry keeps its cell's value, and a NaN
+    propagates as in the reference."""
+    from pyopenfoam_gb300.solvers.smoothers import GS_FORMS, gs_sweep
+
+    c = random_ldu(N, seed=21, permute_faces=perm)
+    c["diag"] = c["diag"].copy()
+    c["diag"][7] = 0.0
+    c["x"] = c["x"].copy()
+    c["x"][11] = np.nan
+    m = LduMatrix(c["n"], torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(k) for k in (c["diag"], c["lower"], c["upper"]))
+    rhs = torch.as_tensor(c["r"]).cuda()
+    for reverse in (False, True):
+        for relax, omega in ((False, 1.0), (True, 0.8)):
+            out = {}
+            for form in GS_FORMS:
+                x = torch.as_tensor(c["x"]).cuda().clone()
+                gs_sweep(m, x, rhs, reverse=reverse, omega=omega, relax=relax, form=form)
+                gs_sweep(m, x, rhs, reverse=reverse, omega=omega, relax=relax, form=form)
+                out[form] = x.cpu().numpy()
+            for form in GS_FORMS[1:]:
+                np.testing.assert_array_equal(out["flow"], out[form],
+                                              err_msg=f"{form} {reverse} {relax}")
+            if not reverse and not relax:
+                ref = O.gauss_seidel(c["owner"], c["neighbour"], c["diag"], c["lower"],
+                                     c["upper"], c["r"], c["x"], 2)
+                np.testing.assert_array_equal(out["flow"], ref)
