@@ -172,6 +172,19 @@ int gbf_dilu_schedule(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
                       const int32_t* neighbour_h, int32_t* level_ptr_h,
                       int32_t* level_faces_h, int32_t* n_levels, int32_t* max_level_size);
 
+/* Links of the dataflow triangular sweep (gbf_sweep_flow_f64) over the
+ * schedule of gbf_sweep_schedule(reverse, lower_only): items_h = its
+ * level_faces (n_items = level_ptr[n_levels]).  Item i writes slot i (the
+ * written cell's value after the face); prev_h[2i] (2 * n_items entries)
+ * names the slot of that cell's value before it, prev_h[2i+1] the slot of
+ * the read cell's value at it (-1: the value on entry), in the sequential
+ * face order of preconditioners.py:170-201 / :306-337; cell_last_h
+ * (n_cells) each cell's last slot, -1 if none.  GBF_ERR_ARG if the items are
+ * not distinct faces or one comes before a face it reads.                 */
+int gbf_sweep_flow_links(int32_t n_cells, int32_t n_faces, const int32_t* owner_h,
+                         const int32_t* neighbour_h, int32_t reverse, int32_t n_items,
+                         const int32_t* items_h, int32_t* prev_h, int32_t* cell_last_h);
+
 /* Links of the dataflow DILU factorisation (gbf_dilu_build_flow_f64) for the
  * schedule level_faces_h of gbf_dilu_schedule: item i (face level_faces[i])
  * writes slots 2i (owner after the face) and 2i+1 (neighbour after it);
@@ -305,6 +318,15 @@ int gbf_sweep_f64(const gbf_layout* L, const double* coef, const double* d,
                   const int32_t* level_ptr, const int32_t* level_faces, int32_t n_levels,
                   int32_t max_level_size, int32_t reverse, double* res, void* barrier,
                   void* stream);
+/* The same sweep as a dataflow walk (no barrier between levels; the same
+ * bits): items = the schedule's level_faces (n_items of them), prev /
+ * cell_last from gbf_sweep_flow_links, slots = n_items doubles of device
+ * scratch; `barrier` (64 bytes) is required, and a wait that runs out sets
+ * its fault word and makes res NaN.                                        */
+int gbf_sweep_flow_f64(const gbf_layout* L, const double* coef, const double* d,
+                       const int32_t* items, int32_t n_items, const int32_t* prev,
+                       const int32_t* cell_last, int32_t reverse, double* res, double* slots,
+                       void* barrier, void* stream);
 int gbf_diag_apply_f64(int32_t n, const double* r, const double* d, double* z, void* stream);
 
 /* ---- Krylov solvers --------------------------------------------------------

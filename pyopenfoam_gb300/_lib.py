@@ -161,6 +161,8 @@ EXPORTED: dict[str, tuple] = {
     "gbf_dic_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_dilu_flow_links": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_sweep_flow_links": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
+                                            _c_vp, _c_vp]),
     "gbf_sweep_schedule": (ctypes.c_int, [_c_i32, _c_i32, _c_vp, _c_vp, _c_i32, _c_i32, _c_vp,
                                           _c_vp, _P(_c_i32), _P(_c_i32)]),
     "gbf_sweep_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_i32, _c_i32,
@@ -205,6 +207,8 @@ EXPORTED: dict[str, tuple] = {
                                           _c_vp, _c_vp, _c_vp]),
     "gbf_gauss_seidel_flow_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_i32, _c_dbl,
                                                  _c_i32, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "gbf_sweep_flow_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_i32, _c_vp, _c_vp, _c_i32,
+                                          _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_dic_build_flow_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "gbf_dilu_flow_slots_bytes": (_c_size, [_c_i32]),
     "gbf_dilu_build_flow_f64": (ctypes.c_int, [_L, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,

@@ -133,6 +133,8 @@ class Topology:
         self._dilu: Schedule | None = None
         self._dilu_flow: FlowLinks | None = None
         self._sweeps: dict = {}
+        self._sweeps_h: dict = {}
+        self._sweep_links: dict = {}
 
     @property
     def layout_ref(self):
@@ -235,6 +237,26 @@ class Topology:
             hit = Schedule(torch.from_numpy(ptr[: nl.value + 1].copy()).to(self.device),
                            torch.from_numpy(faces).to(self.device), nl.value, mx.value)
             self._sweeps[key] = hit
+            self._sweeps_h[key] = (int(ptr[nl.value]) if nl.value > 0 else 0, faces)
+        return hit
+
+    def sweep_flow_links(self, reverse: bool, lower_only: bool) -> tuple[int, FlowLinks]:
+        """(item count, slot links) of the dataflow form of
+        ``sweep_schedule(reverse, lower_only)`` (see ``gbf_sweep_flow_links``)."""
+        key = (bool(reverse), bool(lower_only))
+        hit = self._sweep_links.get(key)
+        if hit is None:
+            self.sweep_schedule(reverse, lower_only)
+            n_items, faces = self._sweeps_h[key]
+            prev = np.empty(max(2 * n_items, 1), np.int32)
+            last = np.empty(max(self.n_cells, 1), np.int32)
+            check(lib().gbf_sweep_flow_links(self.n_cells, self.n_faces, self._own_h.ctypes.data,
+                                             self._nei_h.ctypes.data, int(reverse), n_items,
+                                             faces.ctypes.data, prev.ctypes.data,
+                                             last.ctypes.data), "gbf_sweep_flow_links")
+            hit = (n_items, FlowLinks(torch.from_numpy(prev).to(self.device),
+                                      torch.from_numpy(last).to(self.device)))
+            self._sweep_links[key] = hit
         return hit
 
 

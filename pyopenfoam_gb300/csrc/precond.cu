@@ -635,6 +635,110 @@ __global__ void __launch_bounds__(kBlock)
 }
 }  // namespace gbf
 
+namespace gbf {
+// The sweep as a dataflow walk: item i (face f of the schedule, in level
+// order) writes slot i = W's value after the face; prev[2i] / prev[2i+1]
+// name the slots holding W's value before the face and R's value at it (-1:
+// the entry value in res, which the walk never writes).  sweep_face's
+// arithmetic, so the same bits.
+__global__ void __launch_bounds__(kBlock)
+    sweep_flow_kernel(const int32_t* __restrict__ own, const int32_t* __restrict__ nei,
+                      const double* __restrict__ coef, const double* __restrict__ d,
+                      const int32_t* __restrict__ items, const int32_t* __restrict__ prev,
+                      int n_items, int reverse, const double* __restrict__ res, double* slots,
+                      GridBarrier* bar, long long max_polls) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long chunks = ((long long)n_items + 31) >> 5;
+  long long polls = 0;
+  for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < chunks;
+       ch += warps) {
+    const long long i = ch * 32 + lane;
+    bool done = i >= n_items;
+    int sw = -1, sr = -1;
+    double w = 0.0, r = 0.0, dr = 0.0, cf = 0.0;
+    if (!done) {
+      const int f = __ldg(items + i);
+      const int R = reverse ? __ldg(nei + f) : __ldg(own + f);
+      const int W = reverse ? __ldg(own + f) : __ldg(nei + f);
+      cf = __ldg(coef + f);
+      dr = __ldg(d + R);
+      sw = __ldg(prev + 2 * i);
+      sr = __ldg(prev + 2 * i + 1);
+      if (sw < 0) w = __ldg(res + W);
+      if (sr < 0) r = __ldg(res + R);
+    }
+    bool quit = false;
+    for (;;) {
+      if (!done) {
+        const double vw = sw >= 0 ? ld_flow(slots + sw) : 0.0;
+        const double vr = sr >= 0 ? ld_flow(slots + sr) : 0.0;
+        if (sw >= 0 && !flow_empty(vw)) {
+          w = vw;
+          sw = -1;
+        }
+        if (sr >= 0 && !flow_empty(vr)) {
+          r = vr;
+          sr = -1;
+        }
+        if (sw < 0 && sr < 0) {
+          st_flow(slots + i,
+                  fabs(dr) > 1e-30 ? __dsub_rn(w, __ddiv_rn(__dmul_rn(cf, r), dr)) : w);
+          done = true;
+        }
+      }
+      if (flow_pass_end(done, polls, max_polls, bar, &quit)) break;
+      if (quit) return;
+    }
+  }
+}
+
+// res[c] = c's last written value (unchanged if none), or NaN everywhere if
+// a wait of the walk ran out.
+__global__ void sweep_flow_out_kernel(int n, const int32_t* __restrict__ cell_last,
+                                      const double* __restrict__ slots, const GridBarrier* bar,
+                                      double* res) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  if (bar->fault != 0) {
+    res[c] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  const int s = __ldg(cell_last + c);
+  if (s >= 0) res[c] = slots[s];
+}
+}  // namespace gbf
+
+extern "C" int gbf_sweep_flow_f64(const gbf_layout* L, const double* coef, const double* d,
+                                  const int32_t* items, int32_t n_items, const int32_t* prev,
+                                  const int32_t* cell_last, int32_t reverse, double* res,
+                                  double* slots, void* barrier, void* stream) {
+  int rc = check_layout(L);
+  if (rc) return rc;
+  const int n = L->n_cells;
+  if (n == 0 || n_items == 0) return GBF_OK;
+  GBF_REQUIRE(coef && d && items && prev && cell_last && res && slots && barrier && L->owner &&
+                  L->neighbour && n_items > 0 && n_items <= L->n_faces,
+              "sweep_flow: NULL pointer or bad item count");
+  cudaStream_t s = as_stream(stream);
+  const int grid = wavefront_grid((const void*)sweep_flow_kernel, kBlock, n_items, 1);
+  GBF_REQUIRE(grid > 0, "sweep_flow: the device cannot launch cooperative kernels");
+  GBF_CHECK_CUDA(cudaMemsetAsync(slots, 0xff, sizeof(double) * (size_t)n_items, s));
+  const int32_t* own = L->owner;
+  const int32_t* nei = L->neighbour;
+  int ni = n_items, rev = reverse ? 1 : 0;
+  long long polls = kFlowPolls;
+  GridBarrier* bar = static_cast<GridBarrier*>(barrier);
+  const double* r0 = res;
+  void* args[] = {(void*)&own, (void*)&nei, (void*)&coef, (void*)&d, (void*)&items,
+                  (void*)&prev, &ni, &rev, (void*)&r0, &slots, &bar, &polls};
+  GBF_CHECK_CUDA(launch_wavefront((const void*)sweep_flow_kernel, grid, args, barrier, s));
+  sweep_flow_out_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(n, cell_last, slots, bar,
+                                                                     res);
+  GBF_CHECK_LAUNCH();
+  return GBF_OK;
+}
+
 extern "C" int gbf_sweep_f64(const gbf_layout* L, const double* coef, const double* d,
                              const int32_t* level_ptr, const int32_t* level_faces,
                              int32_t n_levels, int32_t max_level_size, int32_t reverse,

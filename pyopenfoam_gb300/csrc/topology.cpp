@@ -357,6 +357,53 @@ extern "C" int gbf_dilu_flow_links(int32_t n, int32_t nf, const int32_t* own, co
   return GBF_OK;
 }
 
+// Links of the dataflow triangular sweep over the schedule of
+// gbf_sweep_schedule(reverse, lower_only) (items = its level_faces, n_items
+// of them).  Item i (face f, read cell R, written cell W) writes slot i, the
+// value of W after the face; prev[2i] names the slot of W's value before the
+// face and prev[2i+1] the slot of R's value at the face -- the slot of the
+// last earlier face in sweep order that wrote the cell, or -1 for the
+// cell's value on entry.  cell_last[c] is the slot of c's last write, or -1.
+// Refuses items that are not distinct faces or that come before a face they
+// read.
+extern "C" int gbf_sweep_flow_links(int32_t n, int32_t nf, const int32_t* own,
+                                    const int32_t* nei, int32_t reverse, int32_t n_items,
+                                    const int32_t* items, int32_t* prev, int32_t* cell_last) {
+  int rc = check_faces(n, nf, own, nei);
+  if (rc) return rc;
+  if (n_items < 0 || n_items > nf || (n_items > 0 && (!items || !prev)) ||
+      (n > 0 && !cell_last)) {
+    gbf::set_error("sweep_flow_links: bad arguments");
+    return GBF_ERR_ARG;
+  }
+  std::vector<int32_t> pos((size_t)nf, -1);
+  for (int32_t i = 0; i < n_items; ++i) {
+    const int32_t f = items[i];
+    if (f < 0 || f >= nf || pos[f] >= 0) {
+      gbf::set_error("sweep_flow_links: items are not distinct faces (item %d)", i);
+      return GBF_ERR_ARG;
+    }
+    pos[f] = i;
+  }
+  for (int32_t c = 0; c < n; ++c) cell_last[c] = -1;
+  for (int32_t j = 0; j < nf; ++j) {
+    const int32_t f = reverse ? nf - 1 - j : j;
+    const int32_t i = pos[f];
+    if (i < 0) continue;
+    const int32_t R = reverse ? nei[f] : own[f];
+    const int32_t W = reverse ? own[f] : nei[f];
+    const int32_t a = cell_last[W], b = cell_last[R];
+    if (a >= i || b >= i) {
+      gbf::set_error("sweep_flow_links: face %d is scheduled before a face it reads", f);
+      return GBF_ERR_ARG;
+    }
+    prev[2 * (int64_t)i] = a;
+    prev[2 * (int64_t)i + 1] = b;
+    cell_last[W] = i;
+  }
+  return GBF_OK;
+}
+
 // Per-cell lists of boundary faces in ascending face order (the order in
 // which fvm.laplacian's boundary scatter_add, operators.py:508-515, adds
 // them).  owner_b holds owner[n_internal .. n_internal + n_bnd); the listed

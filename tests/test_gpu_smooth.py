@@ -181,3 +181,31 @@ def test_gauss_seidel_flow_matches_level_walks(N, perm):
                 ref = O.gauss_seidel(c["owner"], c["neighbour"], c["diag"], c["lower"],
                                      c["upper"], c["r"], c["x"], 2)
                 np.testing.assert_array_equal(out["flow"], ref)
+
+
+@pytest.mark.parametrize("N,perm", [(12, True), (32, False), (40, True)])
+def test_apply_full_flow_matches_level_walks(N, perm):
+    """DIC and DILU apply_full with their triangular sweeps as dataflow walks
+    (gbf_sweep_flow_f64, the default) give the bits of the barrier walk and
+    of the per-level launches, and of the oracle, on sorted and shuffled
+    face orders (a face may read a cell that later faces still update)."""
+    from pyopenfoam_gb300.solvers.preconditioners import DICPreconditioner, DILUPreconditioner
+    from pyopenfoam_gb300.solvers.sweeps import SWEEP_FORMS, dic_apply_full, dilu_apply_full
+
+    c = random_ldu(N, seed=33, permute_faces=perm)
+    m = LduMatrix(c["n"], torch.as_tensor(c["owner"]), torch.as_tensor(c["neighbour"]),
+                  device="cuda")
+    m.diag, m.lower, m.upper = (torch.as_tensor(k) for k in (c["diag"], c["lower"], c["upper"]))
+    r = torch.as_tensor(c["r"]).cuda()
+    for cls, fn, ofn in ((DICPreconditioner, dic_apply_full, O.dic_apply_full),
+                         (DILUPreconditioner, dilu_apply_full, O.dilu_apply_full)):
+        pre = cls(m)
+        out = {f: fn(pre, r, form=f).cpu().numpy() for f in SWEEP_FORMS}
+        for f in SWEEP_FORMS[1:]:
+            np.testing.assert_array_equal(out["flow"], out[f], err_msg=f"{cls.__name__} {f}")
+        pd = pre.precond_diag.cpu().numpy()
+        if cls is DICPreconditioner:
+            ref = ofn(c["owner"], c["neighbour"], c["upper"], pd, c["r"])
+        else:
+            ref = ofn(c["owner"], c["neighbour"], c["lower"], c["upper"], pd, c["r"])
+        np.testing.assert_array_equal(out["flow"], ref)

@@ -208,6 +208,50 @@ def test_dilu_flow_links_name_the_previous_face_of_each_end(perm):
     assert _flow_links(n, own, nei, np.arange(nf)[::-1].copy())[0] != 0
 
 
+@pytest.mark.parametrize("perm,reverse,lower_only", [(False, 0, True), (True, 1, False),
+                                                     (True, 0, False), (False, 1, True)])
+def test_sweep_flow_links_name_the_last_writes(perm, reverse, lower_only):
+    """Slot links of the dataflow triangular sweep against a plain
+    restatement of the sequential face loop (preconditioners.py:170-201):
+    each item reads the slot last written for its written cell and for its
+    read cell, earlier in sweep order; a bad item list is refused."""
+    c = random_ldu(5, seed=12, permute_faces=perm)
+    n, own, nei = c["n"], c["owner"], c["neighbour"]
+    nf = own.shape[0]
+    o = np.ascontiguousarray(own, np.int32)
+    q = np.ascontiguousarray(nei, np.int32)
+    ptr = np.empty(nf + 1, np.int32)
+    items = np.empty(nf, np.int32)
+    nl, mx = ctypes.c_int32(), ctypes.c_int32()
+    _lib.check(_lib.lib().gbf_sweep_schedule(n, nf, o.ctypes.data, q.ctypes.data, reverse,
+                                             int(lower_only), ptr.ctypes.data, items.ctypes.data,
+                                             ctypes.byref(nl), ctypes.byref(mx)))
+    ni = int(ptr[nl.value])
+    prev = np.empty(2 * ni, np.int32)
+    last = np.empty(n, np.int32)
+    _lib.check(_lib.lib().gbf_sweep_flow_links(n, nf, o.ctypes.data, q.ctypes.data, reverse, ni,
+                                               items.ctypes.data, prev.ctypes.data,
+                                               last.ctypes.data))
+    pos = {int(f): i for i, f in enumerate(items[:ni])}
+    lastw = {}
+    order = range(nf - 1, -1, -1) if reverse else range(nf)
+    for f in order:
+        if f not in pos:
+            assert lower_only and not own[f] < nei[f]
+            continue
+        i = pos[f]
+        R, W = (nei[f], own[f]) if reverse else (own[f], nei[f])
+        assert prev[2 * i] == lastw.get(W, -1) and prev[2 * i + 1] == lastw.get(R, -1)
+        assert max(prev[2 * i], prev[2 * i + 1]) < i
+        lastw[W] = i
+    assert all(last[cl] == lastw.get(cl, -1) for cl in range(n))
+    bad = items[:ni].copy()
+    bad[1] = bad[0]
+    assert _lib.lib().gbf_sweep_flow_links(n, nf, o.ctypes.data, q.ctypes.data, reverse, ni,
+                                           bad.ctypes.data, prev.ctypes.data,
+                                           last.ctypes.data) != 0
+
+
 def test_topology_rejects_bad_addressing():
     L = _lib.lib()
     o = np.array([0, 5], np.int32)
