@@ -381,8 +381,9 @@ int gbf_pcg_solve_f64(const gbf_layout* L, const double* slot_coef, const double
  * instead of a workspace, so at most 1,048,576 cells (larger systems return
  * GBF_ERR_ARG).  It always runs three kernels per iteration: P->variant 0
  * and 1 are accepted alike, 2 (single launch required) and anything else
- * return GBF_ERR_ARG.  The first call on a device looks up and caches the
- * array's address there and should precede any stream capture; the cached
+ * return GBF_ERR_ARG.  It cannot run inside a stream capture (it reads its
+ * state back to the host between chunks of iterations).  The first call on
+ * a device looks up and caches the array's address there; the cached
  * address does not survive cudaDeviceReset.  Calls that overlap on the GPU
  * share the array and race.                                                */
 int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* slot_coef, const double* diag,

@@ -494,11 +494,14 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
 //   * it always runs the three-kernel-per-iteration form (variant 0 and 1
 //     alike); variant 2, which demands the single cooperative launch, is
 //     refused with GBF_ERR_ARG, as is any value outside 0..2;
+//   * the solve cannot run inside a stream capture: between chunks of
+//     iterations it copies the state block to the host and synchronises the
+//     stream, which a capturing stream refuses;
 //   * the first call on a device looks up the array's device address on that
 //     device (cudaGetSymbolAddress, with the device current) and caches it;
-//     make that first call before any stream capture begins; the cached
-//     address does not survive cudaDeviceReset, so a process that resets a
-//     device must not call this entry point on that device afterwards;
+//     the cached address does not survive cudaDeviceReset, so a process that
+//     resets a device must not call this entry point on that device
+//     afterwards;
 //   * all calls share the one array, which keeps the previous call's
 //     contents: the state block is cleared at the start of every call, and
 //     calls whose work overlaps on the GPU (different streams, or different
