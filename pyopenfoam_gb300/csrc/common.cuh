@@ -243,13 +243,15 @@ __device__ __forceinline__ T block_sum(T v, T* sh) {
 }
 
 // Returns true in every thread of the block that finished last.  The caller
-// wrote its partials (thread 0) before calling.  The ticket counter is reset
-// by the last block.
+// wrote its partials (thread 0) before calling; the last block reads only
+// partials (and state written by earlier kernels), so only thread 0 fences
+// its writes before taking the ticket -- the other threads' stores need no
+// ordering here, and a fence in every thread stalls each on its own
+// outstanding stores.  The ticket counter is reset by the last block.
 __device__ __forceinline__ bool last_block_done(unsigned int* ticket) {
   __shared__ bool am_last;
-  __threadfence();
-  __syncthreads();
   if (threadIdx.x == 0) {
+    __threadfence();
     const unsigned int t = atomicAdd(ticket, 1u);
     am_last = (t == gridDim.x - 1);
   }
@@ -262,11 +264,24 @@ __device__ __forceinline__ bool last_block_done(unsigned int* ticket) {
 }
 
 // Sum of partials[0..n) in a fixed order, by the whole block; result in
-// thread 0.  Reads through L2 (other blocks wrote them).
+// thread 0.  Reads through L2 (other blocks wrote them).  Thread t adds
+// partials t, t + B, t + 2B, ... in that order; the loads of up to eight of
+// them are issued before the first add, so a thread waits for one L2 round
+// trip instead of one per partial (the grids of one wave leave ~5 partials
+// per thread of the reducing block).
 template <typename T>
 __device__ __forceinline__ T reduce_partials(const T* partials, int n, T* sh) {
+  constexpr int U = 8;
+  const int B = blockDim.x;
   T v = (T)0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v += __ldcg(partials + i);
+  for (int i0 = threadIdx.x; i0 < n; i0 += U * B) {
+    T q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) q[u] = (i0 + u * B < n) ? __ldcg(partials + i0 + u * B) : (T)0;
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i0 + u * B < n) v += q[u];
+  }
   return block_sum(v, sh);
 }
 
