@@ -117,6 +117,8 @@ __device__ __forceinline__ bool flow_pass_end(bool done, long long& polls, long 
     *quit = true;
     return false;
   }
+  // the pass is bound by the polls' L2 round trip: 0, 16 or 64 ns of sleep
+  // measured the same on GB300 (DILU 128^3 2.61-2.62 ms), 256 ns 2 % slower
   __nanosleep(64);
   return false;
 }
