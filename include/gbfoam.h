@@ -382,10 +382,10 @@ int gbf_pcg_solve_f64(const gbf_layout* L, const double* slot_coef, const double
  * GBF_ERR_ARG).  It always runs three kernels per iteration: P->variant 0
  * and 1 are accepted alike, 2 (single launch required) and anything else
  * return GBF_ERR_ARG.  It cannot run inside a stream capture (it reads its
- * state back to the host between chunks of iterations).  The first call on
- * a device looks up and caches the array's address there; the cached
- * address does not survive cudaDeviceReset.  Calls that overlap on the GPU
- * share the array and race.                                                */
+ * state back to the host between chunks of iterations).  Every call looks
+ * up the array's address on the current device, so a cudaDeviceReset
+ * between calls is safe.  Calls that overlap on the GPU share the array and
+ * race.                                                                    */
 int gbf_pcg_solve_f64_noalloc(const gbf_layout* L, const double* slot_coef, const double* diag,
                               const double* precond_d, const double* b, double* x,
                               double* history, const gbf_solve_params* P, gbf_solve_result* R,

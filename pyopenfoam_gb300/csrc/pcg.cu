@@ -497,11 +497,10 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
 //   * the solve cannot run inside a stream capture: between chunks of
 //     iterations it copies the state block to the host and synchronises the
 //     stream, which a capturing stream refuses;
-//   * the first call on a device looks up the array's device address on that
-//     device (cudaGetSymbolAddress, with the device current) and caches it;
-//     the cached address does not survive cudaDeviceReset, so a process that
-//     resets a device must not call this entry point on that device
-//     afterwards;
+//   * every call looks up the array's device address on the current device
+//     (cudaGetSymbolAddress; no cache, so an address never outlives a
+//     cudaDeviceReset that reloads the module); the first call on a device
+//     loads the module there if it is not loaded yet;
 //   * all calls share the one array, which keeps the previous call's
 //     contents: the state block is cleared at the start of every call, and
 //     calls whose work overlaps on the GPU (different streams, or different
@@ -509,8 +508,6 @@ extern "C" int gbf_pcg_solve_f64(const gbf_layout* L, const double* coef, const 
 //     by the caller;
 //   * nothing here calls cudaMalloc, cudaFree or any allocating routine.
 // ---------------------------------------------------------------------------
-#include <mutex>
-
 namespace gbf {
 
 constexpr int kNoAllocMaxCells = 1 << 20;
@@ -521,24 +518,13 @@ constexpr size_t kNoAllocBytes = 4 * kNoAllocVecBytes + kNoAllocPartialBytes + k
 
 static __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
-
-// Device address of the scratch array on the current device (looked up once
-// per device).
+// Device address of the scratch array on the current device, looked up on
+// every call (a few microseconds of host time).
 static int noalloc_scratch(void** out) {
-  int dev = 0;
-  GBF_CHECK_CUDA(cudaGetDevice(&dev));
-  GBF_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "pcg_noalloc: device %d out of range", dev);
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (g_noalloc_addr[dev] == nullptr) {
-    void* p = nullptr;
-    GBF_CHECK_CUDA(cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch));
-    GBF_REQUIRE(p != nullptr, "pcg_noalloc: scratch address lookup returned NULL");
-    g_noalloc_addr[dev] = p;
-  }
-  *out = g_noalloc_addr[dev];
+  void* p = nullptr;
+  GBF_CHECK_CUDA(cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch));
+  GBF_REQUIRE(p != nullptr, "pcg_noalloc: scratch address lookup returned NULL");
+  *out = p;
   return GBF_OK;
 }
 
