@@ -56,11 +56,13 @@ def to_device(t, device: torch.device, dtype: torch.dtype) -> torch.Tensor:
     from .. import _lib
 
     out = torch.empty(t.shape, dtype=dtype, device=device)
-    stream = torch.cuda.current_stream(device)
-    _lib.check(_lib.lib().gbf_copy_from_host(out.data_ptr(), t.data_ptr(),
-                                             t.numel() * t.element_size(), stream.cuda_stream),
-               "gbf_copy_from_host")
-    stream.synchronize()
+    with torch.cuda.device(out.device):  # the library launches on the current device
+        stream = torch.cuda.current_stream(out.device)
+        _lib.check(_lib.lib().gbf_copy_from_host(out.data_ptr(), t.data_ptr(),
+                                                 t.numel() * t.element_size(),
+                                                 stream.cuda_stream),
+                   "gbf_copy_from_host")
+        stream.synchronize()
     return out
 
 
@@ -78,9 +80,11 @@ def to_host(t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         return out
     from .. import _lib
 
-    stream = torch.cuda.current_stream(src.device)
-    _lib.check(_lib.lib().gbf_copy_to_host(out.data_ptr(), src.data_ptr(),
-                                           src.numel() * src.element_size(), stream.cuda_stream),
-               "gbf_copy_to_host")
-    stream.synchronize()
+    with torch.cuda.device(src.device):
+        stream = torch.cuda.current_stream(src.device)
+        _lib.check(_lib.lib().gbf_copy_to_host(out.data_ptr(), src.data_ptr(),
+                                               src.numel() * src.element_size(),
+                                               stream.cuda_stream),
+                   "gbf_copy_to_host")
+        stream.synchronize()
     return out
