@@ -1255,6 +1255,26 @@ def reference_gradient_24cube(dev) -> dict:
             "reference_solver": "PCGSolver(tolerance=0, rel_tol=1e-13, preconditioner='none')"}
 
 
+def reference_gradient_full_size(N: int, g: np.ndarray, loss: float) -> dict:
+    """This run's gradient and loss against the gradient the reference itself
+    computed on the same N^3 case (tests/golden/reference_unroll96.npz,
+    sampled faces, norm and loss: its fvm.laplacian under autograd and
+    DifferentiableLinearSolve per step, PCG to 1e-13 without
+    preconditioner, on a target from the oracle)."""
+    path = os.path.join(ROOT, "tests", "golden", f"reference_unroll{N}.npz")
+    if not os.path.exists(path):
+        return {"unavailable": f"no reference gradient fixture at {N}^3"}
+    R = np.load(path)
+    ref = R["grad_at_faces"]
+    return {"n_cells": N ** 3, "sampled_faces": int(R["faces"].shape[0]),
+            "max_rel_err_sampled_faces": float(np.abs(g[R["faces"]] - ref).max()
+                                               / np.abs(ref).max()),
+            "grad_norm_rel_err": float(abs(np.linalg.norm(g) - float(R["grad_norm"]))
+                                       / float(R["grad_norm"])),
+            "loss_rel_err": float(abs(loss - float(R["loss"])) / float(R["loss"])),
+            "reference_solver": "PCGSolver(tolerance=0, rel_tol=1e-13, preconditioner='none')"}
+
+
 def run_adjoint96(args, rank, world, local):
     """Adjoint gradient through 20 implicit diffusion steps at 96^3."""
     from pyopenfoam_gb300 import PCGSolver
@@ -1295,6 +1315,7 @@ def run_adjoint96(args, rank, world, local):
     t_fd = time.perf_counter() - t0
     f_s, b_s = statistics.median(fw), statistics.median(bw)
     ref24 = reference_gradient_24cube(dev)
+    ref_full = reference_gradient_full_size(N, grad.cpu().numpy(), loss)
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = len(os.sched_getaffinity(0))
@@ -1319,7 +1340,7 @@ def run_adjoint96(args, rank, world, local):
                "solver_iterations_per_solve": statistics.mean(iters),
                "fd_faces": len(errs), "fd_h": 1e-6, "fd_max_rel_err": max(errs),
                "fd_median_rel_err": statistics.median(errs), "fd_seconds": t_fd,
-               "reference_gradient_24cube": ref24},
+               "reference_gradient_24cube": ref24, f"reference_gradient_{N}cube": ref_full},
               cpu_baseline=cpu)
 
 

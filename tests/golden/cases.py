@@ -115,11 +115,14 @@ def jitter_case(N: int = 6, seed: int = 1, store: bool = True):
     return d
 
 
-def unroll_case(N: int = 10, dt: float = 1e-3, steps: int = 20, seed: int = 4) -> dict:
-    """The 96^3 adjoint workload's structure at a small size: uniform N^3 mesh (fixed value on
-    x0), per-face diffusivity gamma ~ LogNormal(0, 1), x0 ~ U[0, 1], and a
-    target produced by the same 20 implicit steps with a second draw gamma'
-    (computed here with the oracle restatement: fvm.laplacian + PCG)."""
+def unroll_case(N: int = 10, dt: float = 1e-3, steps: int = 20, seed: int = 4,
+                with_target: bool = True, threads: int = 1) -> dict:
+    """The adjoint workload's structure on a uniform N^3 mesh (fixed value on
+    x0): per-face diffusivity gamma ~ LogNormal(0, 1), a second draw gamma',
+    x0 ~ U[0, 1] (the draws of the 96^3 workload when N = 96), and a target
+    produced by the same 20 implicit steps with gamma' (computed here with
+    the oracle restatement, fvm.laplacian + PCG on ``threads`` threads;
+    ``with_target=False`` leaves it out, ``target`` is then None)."""
     from pyopenfoam_gb300.mesh import HexMesh
 
     m = HexMesh(N)
@@ -131,16 +134,18 @@ def unroll_case(N: int = 10, dt: float = 1e-3, steps: int = 20, seed: int = 4) -
              owner=m.numpy("owner"), neighbour=m.numpy("neighbour"),
              face_areas=m.numpy("face_areas"), delta=m.numpy("delta_coefficients"),
              volumes=m.numpy("cell_volumes"))
-    from oracle import oracle as O
+    x = None
+    if with_target:
+        from oracle import oracle as O
 
-    nint = m.n_internal_faces
-    lo, up, dg = O.laplacian(m.n_cells, d["owner"], d["neighbour"], d["face_areas"], d["delta"],
-                             gamma2, d["volumes"])
-    x = x0.copy()
-    for _ in range(steps):
-        x = O.pcg(d["owner"][:nint], d["neighbour"], dg + 1.0 / dt, lo, up, x / dt, x, None, 0.0,
-                  1e-14, 5000).x
-    d.update(gamma=gamma, x0=x0, target=x, dt=dt, steps=steps)
+        nint = m.n_internal_faces
+        lo, up, dg = O.laplacian(m.n_cells, d["owner"], d["neighbour"], d["face_areas"],
+                                 d["delta"], gamma2, d["volumes"])
+        x = x0.copy()
+        for _ in range(steps):
+            x = O.pcg(d["owner"][:nint], d["neighbour"], dg + 1.0 / dt, lo, up, x / dt, x, None,
+                      0.0, 1e-14, 5000, threads=threads).x
+    d.update(gamma=gamma, gamma2=gamma2, x0=x0, target=x, dt=dt, steps=steps)
     d["mesh"] = mesh_from_arrays(d)
     return d
 

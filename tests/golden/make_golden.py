@@ -11,6 +11,7 @@ Run in a checkout that has the reference project next to it:
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --pbicg
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --ldu128
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --unroll24
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/pyOpenFOAM --unroll96
 
 It imports the reference's own classes (``pyfoam.core.ldu_matrix``,
 ``pyfoam.solvers.*``, ``pyfoam.discretisation.operators.fvm``,
@@ -542,18 +543,21 @@ def ldu128(ref_root: str) -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
-UNROLL24_SAMPLES = 1024
+UNROLL_SAMPLES = {24: 1024, 96: 4096}
 
 
-def unroll24(ref_root: str) -> None:
-    """The adjoint workload's structure at 24^3 (13,824 cells; per-face
-    LogNormal(0, 1) diffusivity, x0 ~ U[0, 1], 20 implicit steps of dt =
-    1e-3, loss ||x_T - x_target||^2), differentiated by the reference itself:
-    fvm.laplacian under autograd and DifferentiableLinearSolve per step with
+def unroll(ref_root: str, N: int) -> None:
+    """The adjoint workload (per-face LogNormal(0, 1) diffusivity, x0 ~
+    U[0, 1], 20 implicit steps of dt = 1e-3, loss ||x_T - x_target||^2) on
+    the uniform N^3 mesh -- 24^3 (13,824 cells) or the full 96^3 (884,736
+    cells) -- differentiated by the reference itself: fvm.laplacian under
+    autograd and DifferentiableLinearSolve per step with
     PCGSolver(tolerance=0, rel_tol=1e-13, preconditioner="none")
     (differentiable/linear_solver.py:99-151).  The full gradient is large, so
-    the fixture keeps it on UNROLL24_SAMPLES seeded faces, plus its L2 norm,
-    its sum, the loss and x_T on seeded cells."""
+    the fixture keeps it on UNROLL_SAMPLES[N] seeded faces, plus its L2 norm,
+    its sum, the loss and x_T on seeded cells.  The target comes from the
+    oracle (one thread at 24^3; all cores at 96^3, where the reference's
+    forward and backward take about 7 minutes on 8 cores)."""
     sys.path.insert(0, os.path.join(ref_root, "src"))
     import torch
     from pyfoam.differentiable.linear_solver import DifferentiableLinearSolve
@@ -562,29 +566,29 @@ def unroll24(ref_root: str) -> None:
 
     torch.set_num_threads(8)
     t = torch.from_numpy
-    uc = unroll_case(24)
+    uc = unroll_case(N, threads=1 if N <= 24 else len(os.sched_getaffinity(0)))
     mesh = uc["mesh"]
     gam = t(uc["gamma"]).clone().requires_grad_(True)
-    solver = PCGSolver(tolerance=0.0, rel_tol=1e-13, max_iter=5000, preconditioner="none")
+    solver = PCGSolver(tolerance=0.0, rel_tol=1e-13, max_iter=50000, preconditioner="none")
     own = mesh.owner[: mesh.n_internal_faces]
     lap = fvm.laplacian(gam, torch.zeros(mesh.n_cells, dtype=torch.float64), mesh=mesh)
     d = lap.diag + 1.0 / uc["dt"]
     x = t(uc["x0"])
     for _ in range(uc["steps"]):
         x = DifferentiableLinearSolve.apply(d, lap.lower, lap.upper, x / uc["dt"], solver, own,
-                                            mesh.neighbour, x, 0.0, 5000)
+                                            mesh.neighbour, x, 0.0, 50000)
     loss = ((x - t(uc["target"])) ** 2).sum()
     loss.backward()
     g = gam.grad.numpy()
-    rng = np.random.default_rng(24)
-    faces = np.sort(rng.choice(g.shape[0], UNROLL24_SAMPLES, replace=False))
+    rng = np.random.default_rng(N)
+    faces = np.sort(rng.choice(g.shape[0], UNROLL_SAMPLES[N], replace=False))
     cells = np.sort(rng.choice(x.shape[0], 256, replace=False))
     xT = x.detach().numpy()
     out = dict(faces=faces, grad_at_faces=g[faces], grad_norm=np.float64(np.linalg.norm(g)),
                grad_sum=np.float64(g.sum()), loss=np.float64(loss.item()), cells=cells,
                xT_at_cells=xT[cells], xT_norm=np.float64(np.linalg.norm(xT)),
                rel_tol=np.float64(1e-13))
-    path = os.path.join(HERE, "reference_unroll24.npz")
+    path = os.path.join(HERE, f"reference_unroll{N}.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes; loss", float(loss))
 
@@ -607,6 +611,8 @@ if __name__ == "__main__":
     elif "--ldu128" in sys.argv:
         ldu128(root)
     elif "--unroll24" in sys.argv:
-        unroll24(root)
+        unroll(root, 24)
+    elif "--unroll96" in sys.argv:
+        unroll(root, 96)
     else:
         main(root)

@@ -116,6 +116,40 @@ def test_unrolled_gradient_against_reference_autograd_24cube():
     assert rel(xT[R["cells"]], R["xT_at_cells"]) < 1e-10
 
 
+def test_unrolled_gradient_against_reference_autograd_96cube():
+    """The full-size adjoint workload (96^3, 884,736 cells, 2,681,856 faces,
+    20 steps) against the reference's own autograd chain at that size
+    (reference_unroll96.npz, made by make_golden.py --unroll96: the
+    reference's fvm.laplacian under autograd and DifferentiableLinearSolve
+    per step, PCG to 1e-13 without preconditioner): the gradient on 4096
+    seeded faces, its norm and sum, the loss and x_T.  Here the target
+    x_T(gamma') comes from the GPU solver, there from the oracle; both solve
+    every step to 1e-13..1e-14.  Measured on GB300: loss 4.1e-13, faces
+    2.8e-12, norm 2.3e-12, sum 1.6e-11, x_T 7.7e-13; the bars are those
+    values times 4 to 7 (the GPU path is deterministic)."""
+    import os
+
+    R = np.load(os.path.join(os.path.dirname(FIXTURE), "reference_unroll96.npz"))
+    uc = unroll_case(96, with_target=False)
+    model = _model(uc, 5)
+    gamma, gamma2, x0 = (torch.as_tensor(uc[k]).cuda() for k in ("gamma", "gamma2", "x0"))
+    target = model.final_state(gamma2, x0)
+    loss, grad = model.loss_and_grad(gamma, x0, target)
+    g = grad.cpu().numpy()
+    xT = model.final_state(gamma, x0).cpu().numpy()
+    errs = {"loss": abs(loss - float(R["loss"])) / float(R["loss"]),
+            "faces": rel(g[R["faces"]], R["grad_at_faces"]),
+            "norm": abs(np.linalg.norm(g) - float(R["grad_norm"])) / float(R["grad_norm"]),
+            "sum": abs(g.sum() - float(R["grad_sum"])) / np.abs(g).sum(),
+            "xT": rel(xT[R["cells"]], R["xT_at_cells"])}
+    print("96^3 against the reference:", errs)
+    assert errs["loss"] <= 2e-12, errs
+    assert errs["faces"] < 2e-11, errs
+    assert errs["norm"] <= 1e-11, errs
+    assert errs["sum"] <= 1e-10, errs
+    assert errs["xT"] < 5e-12, errs
+
+
 def test_checkpoint_interval_does_not_change_the_gradient():
     uc = unroll_case(10)
     gamma = torch.as_tensor(uc["gamma"]).cuda()
