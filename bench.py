@@ -1171,54 +1171,6 @@ def run_batch64(args, rank, world, local):
               roofline=roof, cpu_baseline=cpu)
 
 
-def cpu_unrolled_adjoint(h, gamma, x0, target, dt, steps, threads):
-    """The adjoint workload on the host cores: the oracle's restatement of
-    fvm.laplacian, then ``steps`` implicit steps by the oracle's threaded
-    FP64 PCG+DIC to 1e-14 (all states kept), then the adjoint sweep -- one
-    transposed solve per step (right-hand side scaled by a power of two, as
-    the GPU does, so the 1e-30 breakdown test does not stop a small adjoint
-    solve) and the face gradient s_f (x_N - x_P)(lam_P/V_P - lam_N/V_N),
-    -s_b lam_P x_P / V_P on boundary faces.  Returns (loss, gradient,
-    forward s, backward s)."""
-    import math
-
-    from oracle import oracle as O
-
-    own_all, nei = h.numpy("owner"), h.numpy("neighbour")
-    S, dl, V = h.numpy("face_areas"), h.numpy("delta_coefficients"), h.numpy("cell_volumes")
-    nint = nei.shape[0]
-    own = own_all[:nint]
-    t0 = time.perf_counter()
-    lo, up, dg = O.laplacian(h.n_cells, own_all, nei, S, dl, gamma, V)
-    d = dg + 1.0 / dt
-    pd = O.dic_build(own, nei, d, up)
-    xs = [x0]
-    x = x0
-    for _ in range(steps):
-        x = O.pcg(own, nei, d, lo, up, x / dt, x, pd, 0.0, 1e-14, 50000, threads=threads).x
-        xs.append(x)
-    t1 = time.perf_counter()
-    diff = x - target
-    loss = float(diff @ diff)
-    g = 2.0 * diff
-    sd = np.sqrt((S * S).sum(axis=1)) * dl
-    grad = np.zeros(own_all.shape[0])
-    pdT = O.dic_build(own, nei, d, lo)
-    for t in range(steps, 0, -1):
-        k = 30 - math.frexp(float(np.abs(g).max()))[1]
-        sc = math.ldexp(1.0, k)
-        lam = O.pcg(own, nei, d, up, lo, g * sc, np.zeros_like(g), pdT, 0.0, 1e-14, 50000,
-                    threads=threads).x * math.ldexp(1.0, -k)
-        xt = xs[t]
-        lv = lam / V
-        grad[:nint] += sd[:nint] * (xt[nei] - xt[own]) * (lv[own] - lv[nei])
-        ob = own_all[nint:]
-        grad[nint:] += sd[nint:] * (-lv[ob] * xt[ob])
-        g = lam / dt
-    t2 = time.perf_counter()
-    return loss, grad, t1 - t0, t2 - t1
-
-
 def reference_gradient_24cube(dev) -> dict:
     """The 24^3 case of the adjoint workload against the gradient the
     reference itself computed (tests/golden/reference_unroll24.npz: its
@@ -1319,7 +1271,9 @@ def run_adjoint96(args, rank, world, local):
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = len(os.sched_getaffinity(0))
-        c_loss, c_grad, c_f, c_b = cpu_unrolled_adjoint(
+        from oracle.adjoint import unrolled_adjoint
+
+        c_loss, c_grad, c_f, c_b = unrolled_adjoint(
             hm, gamma_h, x0_h, target.cpu().numpy(), 1e-3, 20, threads)
         gh = grad.cpu().numpy()
         cpu = {"value": c_f + c_b, "unit": "s", "cores": threads, "kind": "port",

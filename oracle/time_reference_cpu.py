@@ -200,11 +200,9 @@ def case_c3(torch, ref) -> None:
 
 
 def case_c5(torch, ref) -> None:
-    from tests.golden.cases import unroll_case
-
-    sys.path.insert(0, ROOT)
-    import bench
+    from oracle.adjoint import unrolled_adjoint
     from pyopenfoam_gb300.mesh import HexMesh
+    from tests.golden.cases import unroll_case
 
     N = 96
     uc = unroll_case(N)
@@ -229,9 +227,8 @@ def case_c5(torch, ref) -> None:
     g_ref = gam.grad.numpy().copy()
 
     hm = HexMesh(N)
-    p_loss, p_grad, p_f, p_b = bench.cpu_unrolled_adjoint(hm, uc["gamma"], uc["x0"],
-                                                          uc["target"], uc["dt"],
-                                                          uc["steps"], _cores())
+    p_loss, p_grad, p_f, p_b = unrolled_adjoint(hm, uc["gamma"], uc["x0"], uc["target"],
+                                                uc["dt"], uc["steps"], _cores())
     _emit("c5: 96^3 adjoint, 20 implicit steps", reference_forward_s=t_f,
           reference_backward_s=t_b, reference_total_s=t_f + t_b,
           reference_solver="PCG, no preconditioner, rel_tol 1e-13",
